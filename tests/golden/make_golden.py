@@ -1,0 +1,58 @@
+"""Regenerate the golden vectors from the reference's own C sources.
+
+    python tests/golden/make_golden.py [case ...]
+
+Builds oracle/_ref/libfdtdref.so from the reference sources (oracle/ref.mk;
+they must be present, default /root/reference or $MPIFDTD_REFERENCE), runs
+every case of cases.py through the reference exactly as simulator.c drives it,
+and writes tests/golden/<case>.npz.  The fixtures are committed; this script
+is how they were made.
+"""
+from __future__ import annotations
+
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from oracle.pyoracle import FieldInfo, RefSim  # noqa: E402
+from tests.golden.cases import CASES, make_model  # noqa: E402
+from tests.golden.golden_io import capture, crop  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def run_case(name, c):
+    fi = FieldInfo(*c["fi"])
+    model = make_model(c["model"])
+    sim = RefSim(c["solver"], fi, model)
+    sim.step(c["steps"])
+    mpi = c["solver"].startswith("MPI")
+    fields = [crop(sim.field(w), mpi) for w in range(3)]
+    eps = [crop(sim.eps(w), mpi) for w in range(3)]
+    ntff = [sim.ntff(w) for w in range(3)]
+    out = capture(fields, eps, ntff, sim.array_size, c["kind"], c.get("rows", "all"))
+    extras = c.get("extras", ())
+    if "spectrum" in extras:
+        with tempfile.TemporaryDirectory() as d:
+            out["spectrum"] = sim.time_output(d)
+    if "frequency" in extras:
+        out["frequency"] = sim.frequency_from(*fields)
+    out["meta_time"] = np.array(sim.time)
+    out["meta_array_size"] = np.array(sim.array_size)
+    return out
+
+
+def main(names):
+    for name in names or CASES:
+        out = run_case(name, CASES[name])
+        np.savez_compressed(OUT / f"{name}.npz", **out)
+        print(f"{name}: {sum(v.nbytes for v in out.values()) / 1e6:.2f} MB raw")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])
