@@ -1,0 +1,144 @@
+/*
+ * mpifdtd_gb300.h -- C ABI of the GB300 (sm_103a) 2-D UPML FDTD engine.
+ *
+ * The engine time-steps the reference's TM_UPML / TE_UPML solvers
+ * (rennone/mpiFDTD) on one GPU: the fused Yee + UPML auxiliary updates of
+ * mpiTM_UPML.c / mpiTE_UPML.c (and of the serial fdtdTM_upml.c /
+ * fdtdTE_upml.c), the scattered-field sources of field.c, and the
+ * time-domain near-to-far-field (NTFF) accumulation into the flat
+ * [360][arraySize] U/W arrays.  Plain C types only: no CUDA or torch types.
+ *
+ * The reference's own entry points (mpi_fdtdTM_upml_getUpdate() ... ) are
+ * provided on top of this ABI by libmpifdtd_upml.so, see mpifdtd_upml.h.
+ *
+ * Every call returns FDTD_OK (0) or an error code; fdtd_last_error() gives a
+ * message for the calling thread.  Nothing here falls back to the CPU: if no
+ * usable GPU is present fdtd_create() fails with FDTD_E_CUDA.
+ */
+#ifndef MPIFDTD_GB300_H
+#define MPIFDTD_GB300_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define FDTD_OK 0
+#define FDTD_E_ARG 1           /* invalid argument or configuration            */
+#define FDTD_E_CUDA 2          /* CUDA runtime error (no device, launch error)  */
+#define FDTD_E_NOMEM 3         /* device or host allocation failed              */
+#define FDTD_E_STATE 4         /* call not valid in the simulation's state      */
+#define FDTD_E_UNSUPPORTED 5   /* valid request the engine does not implement   */
+
+/* Solver ids: the values of enum SOLVER in simulator.h:8-18. */
+#define FDTD_TM_UPML 2         /* serial TM UPML  (fdtdTM_upml.c)  */
+#define FDTD_TE_UPML 3         /* serial TE UPML  (fdtdTE_upml.c)  */
+#define FDTD_MPI_TM_UPML 4     /* MPI TM UPML     (mpiTM_UPML.c), one-rank semantics */
+#define FDTD_MPI_TE_UPML 5     /* MPI TE UPML     (mpiTE_UPML.c), one-rank semantics */
+
+/* Field precision of the stencil.  The NTFF accumulation is FP64 in both. */
+#define FDTD_F64 0
+#define FDTD_F32 1
+
+/* Built-in permittivity models evaluated on the GPU (models.c:139-164 ids). */
+#define FDTD_MODEL_NONE 0      /* noModel.c                                     */
+#define FDTD_MODEL_CIRCLE 1    /* circleModel.c: {radius_nm, eps}                */
+#define FDTD_MODEL_MORPHO 3    /* morphoScaleModel.c: {width_nm, thick0_nm, thick1_nm,
+                                  layers, branch_nm, edge_rate, eps, per_lamella(0/1),
+                                  width_0_nm, width_1_nm, ...}                   */
+
+/* Which array: fields (TM: 0 Ez, 1 Hx, 2 Hy; TE: 0 Ex, 1 Ey, 2 Hz),
+ * NTFF accumulators (TM: 0 Ux, 1 Uy, 2 Wz; TE: 0 Wx, 1 Wy, 2 Uz). */
+
+/* Layout of copied-out fields / permittivity:
+ *   FDTD_LAYOUT_GLOBAL : N_PX x N_PY cells, y contiguous (global frame)
+ *   FDTD_LAYOUT_SOLVER : the reference solver's own array: (N_PX+2) x (N_PY+2)
+ *                        with a zero halo for the MPI solvers
+ *                        (mpiTM_UPML.c:737-741), N_PX x N_PY for the serial ones */
+#define FDTD_LAYOUT_GLOBAL 0
+#define FDTD_LAYOUT_SOLVER 1
+
+typedef struct fdtd_config {
+  /* field.h:20-28 FieldInfo, physical sizes in nm */
+  int width_nm, height_nm, h_u_nm, pml, lambda_nm, angle_deg, step_num;
+  int precision;       /* FDTD_F64 or FDTD_F32                                 */
+  int reserved[8];     /* must be zero                                         */
+} fdtd_config;
+
+/* Grid and NTFF geometry derived exactly as field_init() does (field.c:89-143). */
+typedef struct fdtd_geometry {
+  int n_px, n_py, n_pml, n_x, n_y;
+  int ntff_top, ntff_bottom, ntff_left, ntff_right, ntff_cx, ntff_cy;
+  double rf_per_c;
+  int array_size;      /* NTFFInfo.arraySize = stepNum + 2*RFperC              */
+  double lambda_s, k_s, omega_s;
+} fdtd_geometry;
+
+typedef struct fdtd_sim fdtd_sim;
+
+/* Computes the geometry without touching the GPU. */
+int fdtd_geometry_of(const fdtd_config *cfg, fdtd_geometry *out);
+
+/* Allocates the device state (all fields zero, time 0, ray_coef 0).
+ * Replaces: the solver init() bodies mpiTM_UPML.c:187-193 / mpiTE_UPML.c:283-288
+ * (allocation and coefficients; permittivity comes from fdtd_set_eps or
+ * fdtd_fill_eps_model). */
+int fdtd_create(int solver, const fdtd_config *cfg, fdtd_sim **out);
+int fdtd_destroy(fdtd_sim *sim);
+int fdtd_get_geometry(const fdtd_sim *sim, fdtd_geometry *out);
+
+/* Permittivity in the global frame, N_PX*N_PY doubles each, host pointers.
+ * TM: e0 = EPS_EZ(x,y,D_XY), e1 = EPS_HX(x,y+.5,D_Y), e2 = EPS_HY(x+.5,y,D_X)
+ * TE: e0 = EPS_EX(x+.5,y,D_Y), e1 = EPS_EY(x,y+.5,D_X), e2 = EPS_HZ
+ * (mpiTM_UPML.c:680-682, mpiTE_UPML.c:503-505; the serial solvers use the
+ * modes of fdtdTM_upml.c:237-239).  e1/e2 may be NULL for TM and e2 for TE:
+ * the updates read only the E-component permittivity. */
+int fdtd_set_eps(fdtd_sim *sim, const double *e0, const double *e1, const double *e2);
+/* Evaluates a built-in model on the GPU at the same staggered points and
+ * sub-cell modes as the solver's setCoefficient(). */
+int fdtd_fill_eps_model(fdtd_sim *sim, int model, const double *params, int n_params);
+
+/* One update() at the caller's clock (drop-in path: the caller owns time and
+ * ray_coef, as simulator_calc() + field_nextStep() do, simulator.c:247-251).
+ * time must lie in [0, step_num-1]: the reference's driver stops at maxTime
+ * (field.c:317-319) and the flat NTFF index is only allocated up to there. */
+int fdtd_update(fdtd_sim *sim, double time, double ray_coef);
+/* n steps of update() followed by the engine's own field_nextStep()
+ * (field.c:312-315); starts from the engine clock (fdtd_get_time). */
+int fdtd_run(fdtd_sim *sim, int n_steps);
+int fdtd_get_time(const fdtd_sim *sim, double *time);
+int fdtd_set_time(fdtd_sim *sim, double time);
+int fdtd_synchronize(fdtd_sim *sim);
+
+/* Copy-out.  Sizes in complex elements: GLOBAL n_px*n_py, SOLVER
+ * (n_px+2)*(n_py+2) for MPI solvers, n_px*n_py for serial ones. */
+int fdtd_get_field(fdtd_sim *sim, int which, int layout, double *out_complex);
+int fdtd_get_eps(fdtd_sim *sim, int which, int layout, double *out);
+/* NTFF accumulator: 360*array_size complex, the reference's flat indexing. */
+int fdtd_get_ntff(fdtd_sim *sim, int which, double *out_complex);
+/* Values the flat indexing wrote outside the 360*array_size block (each side
+ * has `guard` cells; the reference writes past its allocation there). */
+int fdtd_get_ntff_guard(fdtd_sim *sim, int which, double *out_complex, int *guard);
+
+/* reset() of the solvers (mpiTM_UPML.c:219-232): zero every field; the
+ * serial solvers also zero the NTFF arrays (fdtdTM_upml.c:110-113). The
+ * engine clock returns to 0. */
+int fdtd_reset(fdtd_sim *sim);
+
+/* Device pointers of the state for zero-copy consumers (pitch in elements). */
+int fdtd_device_field(fdtd_sim *sim, int which, void **dptr, int *pitch, int *rows);
+
+/* Device status word: bit 0 = an NTFF deposit fell outside the accumulator
+ * and was dropped (cannot happen within [0, step_num) on valid geometry). */
+#define FDTD_STATUS_NTFF_RANGE 1u
+int fdtd_get_status(fdtd_sim *sim, unsigned int *flags);
+
+/* Number of kernel launches the engine issued since creation. */
+long long fdtd_launch_count(const fdtd_sim *sim);
+
+const char *fdtd_last_error(void);
+const char *fdtd_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,96 @@
+"""Builds the in-tree native libraries of mpifdtd_gb300.
+
+* ``_build/libmpifdtd_gb300.so``  CUDA engine (C ABI of include/mpifdtd_gb300.h),
+  compiled for sm_103a only.
+* ``_build/libmpifdtd_upml.so``   drop-in entry points of the reference
+  (include/mpifdtd_upml.h); needs the host program's field_*/models_* symbols.
+* ``_build/libmpifdtd_field.so``  the library's own implementation of the
+  reference's field.h / models.h host API (for programs without field.c).
+
+Translation units compile in parallel; no cmake.  Host code is compiled with
+-ffp-contract=off because it evaluates the reference's one-time formulas
+(sigma profiles, coefficients, NTFF shifts) and must round as the reference.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+INCLUDE = ROOT / "include"
+
+ENGINE_SO = BUILD / "libmpifdtd_gb300.so"
+UPML_SO = BUILD / "libmpifdtd_upml.so"
+FIELD_SO = BUILD / "libmpifdtd_field.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
+                     f"-I{INCLUDE}"]
+CC_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-Wall", f"-I{INCLUDE}"]
+
+ENGINE_SOURCES = ["fdtd_kernels.cu", "fdtd_api.cu"]
+
+
+def nvcc() -> str:
+    cand = os.environ.get("NVCC") or shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    return cand
+
+
+def _run(cmd, verbose):
+    if verbose:
+        print(" ".join(str(c) for c in cmd), flush=True)
+    r = subprocess.run([str(c) for c in cmd], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"build step failed: {' '.join(map(str, cmd))}\n{r.stdout}\n{r.stderr}")
+    return r
+
+
+def _stale(target: Path, deps) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    return any(Path(d).stat().st_mtime > t for d in deps)
+
+
+def _headers():
+    return list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list(INCLUDE.glob("*.h"))
+
+
+def build(verbose: bool = False, force: bool = False) -> Path:
+    """Compile every extension for sm_103a; returns the engine library path."""
+    BUILD.mkdir(parents=True, exist_ok=True)
+    hdrs = _headers()
+    objs = []
+    jobs = []
+    for src in ENGINE_SOURCES:
+        s = CSRC / src
+        o = BUILD / (s.stem + ".o")
+        objs.append(o)
+        if force or _stale(o, [s] + hdrs):
+            jobs.append([nvcc()] + NVCC_FLAGS + ["-c", s, "-o", o])
+    with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
+        list(ex.map(lambda c: _run(c, verbose), jobs))
+    if force or jobs or _stale(ENGINE_SO, objs):
+        _run([nvcc()] + ARCH + ["-shared", "-o", ENGINE_SO] + objs, verbose)
+    # drop-in layer (C) and the library's own field/models host API
+    upml_src = CSRC / "compat_upml.c"
+    if upml_src.exists() and (force or _stale(UPML_SO, [upml_src] + hdrs + [ENGINE_SO])):
+        _run(["gcc", "-std=gnu99"] + CC_FLAGS + ["-shared", "-o", UPML_SO, upml_src,
+                                                 f"-L{BUILD}", "-lmpifdtd_gb300",
+                                                 f"-Wl,-rpath,{BUILD}", "-lm"], verbose)
+    field_src = CSRC / "field_host.cu"
+    if field_src.exists() and (force or _stale(FIELD_SO, [field_src] + hdrs)):
+        _run([nvcc()] + NVCC_FLAGS + ["-shared", "-o", FIELD_SO, field_src], verbose)
+    return ENGINE_SO
+
+
+if __name__ == "__main__":
+    import sys
+    build(verbose=True, force="--force" in sys.argv)
+    print("built", ENGINE_SO)

@@ -1,0 +1,695 @@
+// fdtd_api.cu -- host side of the C ABI declared in include/mpifdtd_gb300.h.
+//
+// Host responsibilities: derive the grid exactly as field_init() does
+// (field.c:89-143), build the 1-D PML coefficient tables with the
+// reference's own formulas (mpiTM_UPML.c:663-716, mpiTE_UPML.c:489-536,
+// fdtdTM_upml.c:224-274, fdtdTE_upml.c:361-412), build the NTFF surface and
+// retarded-time shift tables (mpiTM_UPML.c:849-1037, ntffTM.c:293-371), and
+// sequence the per-step launches.  All arithmetic that the reference does once
+// per run (sigma, coefficients, shifts, source phases) is done here in double
+// with the same expressions; this file must be compiled with
+// -ffp-contract=off so the host compiler does not fuse them.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "fdtd_internal.cuh"
+#include "fdtd_sim.h"
+
+using namespace fdtd;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...)
+{
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(call)                                                                                   \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess) return fail(FDTD_E_CUDA, "%s: %s", #call, cudaGetErrorString(e_));      \
+  } while (0)
+
+bool is_tm(int solver) { return solver == FDTD_TM_UPML || solver == FDTD_MPI_TM_UPML; }
+bool is_mpi(int solver) { return solver == FDTD_MPI_TM_UPML || solver == FDTD_MPI_TE_UPML; }
+
+// field.c:259-283 (M = 2)
+double sigma_axis(double x, int n_pml, int n_inner, int n_full)
+{
+  if (x < n_pml) return std::pow(1.0 * (n_pml - x) / n_pml, 2);
+  if (x < n_inner + n_pml) return 0;
+  return std::pow(1.0 * (x - (n_full - n_pml - 1)) / n_pml, 2);
+}
+
+}  // namespace
+
+extern "C" const char *fdtd_last_error(void) { return g_err.c_str(); }
+extern "C" const char *fdtd_version(void) { return "mpifdtd_gb300 0.1 (sm_103a)"; }
+
+extern "C" int fdtd_geometry_of(const fdtd_config *cfg, fdtd_geometry *g)
+{
+  if (!cfg || !g) return fail(FDTD_E_ARG, "null argument");
+  if (cfg->h_u_nm <= 0 || cfg->width_nm <= 0 || cfg->height_nm <= 0 || cfg->lambda_nm <= 0)
+    return fail(FDTD_E_ARG, "sizes must be positive");
+  if (cfg->pml <= 0) return fail(FDTD_E_ARG, "pml must be positive (field.c:259-283 divides by it)");
+  if (cfg->step_num < 0) return fail(FDTD_E_ARG, "step_num must be >= 0");
+  // field.c:95-100 (field_toCellUnit divides as double, the int conversion truncates)
+  g->n_px = (int)((double)cfg->width_nm / cfg->h_u_nm);
+  g->n_py = (int)((double)cfg->height_nm / cfg->h_u_nm);
+  g->n_pml = cfg->pml;
+  g->n_x = g->n_px - 2 * g->n_pml;
+  g->n_y = g->n_py - 2 * g->n_pml;
+  // field.c:105-109
+  g->lambda_s = (double)cfg->lambda_nm / cfg->h_u_nm;
+  g->k_s = 2 * M_PI / g->lambda_s;
+  g->omega_s = kC * g->k_s;
+  // field.c:133-142
+  g->ntff_cx = g->n_px / 2;
+  g->ntff_cy = g->n_py / 2;
+  g->ntff_top = g->n_py - g->n_pml - 5;
+  g->ntff_bottom = g->n_pml + 5;
+  g->ntff_left = g->n_pml + 5;
+  g->ntff_right = g->n_px - g->n_pml - 5;
+  double len = (g->ntff_top - g->ntff_bottom) / 2;
+  g->rf_per_c = len * 2;
+  g->array_size = (int)(cfg->step_num + 2 * g->rf_per_c);
+  if (g->ntff_right - g->ntff_left < 2 || g->ntff_top - g->ntff_bottom < 2)
+    return fail(FDTD_E_ARG, "grid %dx%d too small for pml %d plus the 5-cell NTFF inset", g->n_px, g->n_py,
+                g->n_pml);
+  return FDTD_OK;
+}
+
+// ---------------------------------------------------------------- create
+
+static int build_tables(fdtd_sim *s)
+{
+  const fdtd_geometry &g = s->geo;
+  const bool tm = s->tm;
+  const double R = 1.0e-8, M = 2.0;
+  // mpiTM_UPML.c:672 / fdtdTM_upml.c:232 (TM, with 1/cos(pi/3)); mpiTE_UPML.c:497 (TE)
+  const double sig_max = tm ? -(M + 1.0) * kEps0 * kC / 2.0 / g.n_pml / cos(M_PI / 3) * log(R)
+                            : -(M + 1.0) * kEps0 * kC / 2.0 / g.n_pml * log(R);
+  const double e2 = 2 * kEps0, sz = 0;
+  const double mu0 = 1.0 / kC / kC;  // field.h:74
+  const double inv_mu = 1.0 / mu0;
+  s->inv_mu = inv_mu;
+  std::vector<Coef4<double>> txi(s->nxa), txh(s->nxa), tyi(s->ncols), tyh(s->ncols);
+  for (int i = 0; i < s->nxa; i++) {
+    const double x = i + s->ox;
+    const double si = sig_max * sigma_axis(x, g.n_pml, g.n_x, g.n_px);
+    const double sh = sig_max * sigma_axis(x + 0.5, g.n_pml, g.n_x, g.n_px);
+    if (tm) {
+      txi[i] = {(e2 - si) / (e2 + si), (e2) / (e2 + si), (e2 + si) / (e2 + sz), (e2 - si) / (e2 + sz)};
+      txh[i] = {(e2 - sh) / (e2 + sh), 1.0 / (e2 + sh), 0, 0};
+    } else {
+      txi[i] = {(e2 - si) / (e2 + si), 1.0 / (e2 + si), 0, 0};
+      txh[i] = {(e2 + sh) / (e2 + sz), (e2 - sh) / (e2 + sz), (e2 - sh) / (e2 + sh), (e2) / (e2 + sh) * inv_mu};
+    }
+  }
+  for (int j = 0; j < s->ncols; j++) {
+    const double y = j + s->ox;
+    const double si = sig_max * sigma_axis(y, g.n_pml, g.n_y, g.n_py);
+    const double sh = sig_max * sigma_axis(y + 0.5, g.n_pml, g.n_y, g.n_py);
+    if (tm) {
+      tyi[j] = {(e2 - si) / (e2 + si), (e2 + sz) / (e2 + si), e2 + si, e2 - si};
+      tyh[j] = {(e2 - sh) / (e2 + sh), (e2) / (e2 + sh) * inv_mu, 0, 0};
+    } else {
+      tyi[j] = {(e2 - si) / (e2 + si), (e2) / (e2 + si), 0, 0};
+      tyh[j] = {(e2 - sh) / (e2 + sh), (e2 + sz) / (e2 + sh), e2 + sh, e2 - sh};
+    }
+  }
+  // interior: every sigma zero (field.c:265,278): x in [n_pml, n_px - n_pml)
+  s->in_x0 = g.n_pml;
+  s->in_x1 = g.n_px - g.n_pml;
+  s->in_y0 = g.n_pml;
+  s->in_y1 = g.n_py - g.n_pml;
+  auto up = [&](std::vector<Coef4<double>> &h, void **d64, void **d32) -> int {
+    CK(cudaMalloc(d64, h.size() * sizeof(Coef4<double>)));
+    CK(cudaMemcpy(*d64, h.data(), h.size() * sizeof(Coef4<double>), cudaMemcpyHostToDevice));
+    std::vector<Coef4<float>> f(h.size());
+    for (size_t q = 0; q < h.size(); q++) f[q] = {(float)h[q].a, (float)h[q].b, (float)h[q].c, (float)h[q].d};
+    CK(cudaMalloc(d32, f.size() * sizeof(Coef4<float>)));
+    CK(cudaMemcpy(*d32, f.data(), f.size() * sizeof(Coef4<float>), cudaMemcpyHostToDevice));
+    return FDTD_OK;
+  };
+  int rc;
+  if ((rc = up(txi, &s->d_tab64[0], &s->d_tab32[0]))) return rc;
+  if ((rc = up(txh, &s->d_tab64[1], &s->d_tab32[1]))) return rc;
+  if ((rc = up(tyi, &s->d_tab64[2], &s->d_tab32[2]))) return rc;
+  if ((rc = up(tyh, &s->d_tab64[3], &s->d_tab32[3]))) return rc;
+
+  // CW source phase tables (mpiTM_UPML.c:343-347, :369): kr = x ks_cos + y ks_sin
+  const double rad = s->cfg.angle_deg * M_PI / 180;
+  const double ks_cos = cos(rad) * g.k_s, ks_sin = sin(rad) * g.k_s;
+  std::vector<double2> ex(s->nxa), ey(s->ncols);
+  for (int i = 0; i < s->nxa; i++) {
+    const int x = i + s->ox;
+    const double ph = x * ks_cos;
+    ex[i] = make_double2(cos(ph), sin(ph));
+  }
+  for (int j = 0; j < s->ncols; j++) {
+    const int y = j + s->ox;
+    const double ph = y * ks_sin;
+    ey[j] = make_double2(cos(ph), sin(ph));
+  }
+  CK(cudaMalloc(&s->d_ex, ex.size() * sizeof(double2)));
+  CK(cudaMemcpy(s->d_ex, ex.data(), ex.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&s->d_ey, ey.size() * sizeof(double2)));
+  CK(cudaMemcpy(s->d_ey, ey.data(), ey.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  return FDTD_OK;
+}
+
+// NTFF path cells in the reference's side order and their per-angle shifts.
+static int build_ntff(fdtd_sim *s)
+{
+  const fdtd_geometry &g = s->geo;
+  const bool tm = s->tm, mpi = s->mpi;
+  const int P = s->pitch;
+  const int tp = g.ntff_top, bm = g.ntff_bottom, rt = g.ntff_right, lt = g.ntff_left;
+  const int cx = g.ntff_cx, cy = g.ntff_cy;
+  std::vector<SurfCell> cells;
+  // geometry of each cell for the shift: r2 = (rx, ry) (double), side id
+  std::vector<double> r2x, r2y;
+  std::vector<int> side;
+  auto add = [&](int i, int j, int hoff, int sign, int eslot, int hslot, int uid, int wid, double rx, double ry,
+                 int sd) {
+    SurfCell c;
+    c.k = (long long)i * P + j;
+    c.hoff = hoff;
+    c.sign = (signed char)sign;
+    c.e_slot = (signed char)eslot;
+    c.h_slot = (signed char)hslot;
+    c.uid_wid = (signed char)(uid | (wid << 4));
+    cells.push_back(c);
+    r2x.push_back(rx);
+    r2y.push_back(ry);
+    side.push_back(sd);
+  };
+  // array row/col range of the path: MPI clips to the sub-domain
+  // (mpiTM_UPML.c:886-887,926-927), serial uses [left,right) x [bottom,top)
+  const int nrow = s->nxa, ncol = s->ncols;
+  const int i0 = mpi ? (lt > 1 ? lt : 1) : lt, i1 = mpi ? (rt < nrow ? rt : nrow) : rt;
+  const int j0 = mpi ? (bm > 1 ? bm : 1) : bm, j1 = mpi ? (tp < ncol ? tp : ncol) : tp;
+  const double hx = tm ? 0.0 : 0.5;  // TE samples sit half a cell along the side
+  // TM: U slots Ux 0 / Uy 1, W Wz 2 ; TE: U Uz 2, W Wx 0 / Wy 1
+  if (tm) {
+    for (int i = i0; i < i1; i++) add(i, bm, -1, +1, 0, 3, 0, 2, i - cx, bm - cy, 0);        // bottom
+    for (int j = j0; j < j1; j++) add(rt, j, -P, +1, 0, 4, 1, 2, rt - cx, j - cy, 1);        // right
+    for (int i = i0; i < i1; i++) add(i, tp, -1, -1, 0, 3, 0, 2, i - cx, tp - cy, 2);        // top
+    for (int j = j0; j < j1; j++) add(lt, j, -P, -1, 0, 4, 1, 2, lt - cx, j - cy, 3);        // left
+  } else {
+    for (int i = i0; i < i1; i++) add(i, bm, -1, -1, 0, 6, 2, 0, i - cx + hx, bm - cy, 0);
+    for (int j = j0; j < j1; j++) add(rt, j, -P, -1, 1, 6, 2, 1, rt - cx, j - cy + hx, 1);
+    for (int i = i0; i < i1; i++) add(i, tp, -1, +1, 0, 6, 2, 0, i - cx + hx, tp - cy, 2);
+    for (int j = j0; j < j1; j++) add(lt, j, -P, +1, 1, 6, 2, 1, lt - cx, j - cy + hx, 3);
+  }
+  const int n = (int)cells.size();
+  s->ncell = n;
+  std::vector<double> shift((size_t)360 * n);
+  for (int ang = 0; ang < 360; ang++) {
+    double *row = &shift[(size_t)ang * n];
+    if (mpi) {
+      // mpiTM_UPML.c:875-876, :894 ; mpiTE_UPML.c:634-635, :654
+      const double rad = ang * M_PI / 180.0;
+      const double r1x = cos(rad), r1y = sin(rad);
+      for (int c = 0; c < n; c++) row[c] = -(r1x * r2x[c] + r1y * r2y[c]) / kC + g.rf_per_c;
+    } else {
+      // ntffTM.c:318-368 / ntffTE.c:92-155: shift advanced incrementally along each side
+      const double rad = ang * (M_PI / 180.0);
+      const double r1x = cos(rad) / kC, r1y = sin(rad) / kC;
+      int c = 0;
+      for (int sd = 0; sd < 4; sd++) {
+        int c0 = c;
+        while (c < n && side[c] == sd) c++;
+        if (c == c0) continue;
+        // start point of the side in the reference's loop (left/bottom corner frame)
+        double sx0 = r2x[c0], sy0 = r2y[c0];
+        double sh = -(r1x * sx0 + r1y * sy0) + g.rf_per_c;
+        const double step = (sd == 0 || sd == 2) ? r1x : r1y;
+        for (int q = c0; q < c; q++) {
+          row[q] = sh;
+          sh -= step;
+        }
+      }
+    }
+  }
+  CK(cudaMalloc(&s->d_cells, sizeof(SurfCell) * n));
+  CK(cudaMemcpy(s->d_cells, cells.data(), sizeof(SurfCell) * n, cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&s->d_shift, sizeof(double) * shift.size()));
+  CK(cudaMemcpy(s->d_shift, shift.data(), sizeof(double) * shift.size(), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&s->d_vals, sizeof(double2) * 2 * n));
+  s->ntff_len = (size_t)360 * g.array_size + 2 * kGuard;
+  for (int a = 0; a < 3; a++) {
+    CK(cudaMalloc(&s->d_ntff[a], sizeof(double2) * s->ntff_len));
+    CK(cudaMemsetAsync(s->d_ntff[a], 0, sizeof(double2) * s->ntff_len, s->stream));
+  }
+  CK(cudaMalloc(&s->d_status, sizeof(unsigned int)));
+  CK(cudaMemsetAsync(s->d_status, 0, sizeof(unsigned int), s->stream));
+  return FDTD_OK;
+}
+
+static void free_sim(fdtd_sim *s)
+{
+  if (!s) return;
+  for (int a = 0; a < kMaxSlots; a++) cudaFree(s->d_f[a]);
+  for (int a = 0; a < 2; a++) { cudaFree(s->d_ieps64[a]); cudaFree(s->d_ieps32[a]); }
+  for (int a = 0; a < 4; a++) { cudaFree(s->d_tab64[a]); cudaFree(s->d_tab32[a]); }
+  cudaFree(s->d_ex);
+  cudaFree(s->d_ey);
+  cudaFree(s->d_cells);
+  cudaFree(s->d_shift);
+  cudaFree(s->d_vals);
+  for (int a = 0; a < 3; a++) cudaFree(s->d_ntff[a]);
+  cudaFree(s->d_status);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+}
+
+extern "C" int fdtd_create(int solver, const fdtd_config *cfg, fdtd_sim **out)
+{
+  if (!cfg || !out) return fail(FDTD_E_ARG, "null argument");
+  *out = nullptr;
+  if (solver != FDTD_TM_UPML && solver != FDTD_TE_UPML && solver != FDTD_MPI_TM_UPML &&
+      solver != FDTD_MPI_TE_UPML)
+    return fail(FDTD_E_ARG, "solver %d is not a UPML solver (2..5)", solver);
+  if (cfg->precision != FDTD_F64 && cfg->precision != FDTD_F32)
+    return fail(FDTD_E_ARG, "precision must be FDTD_F64 or FDTD_F32");
+  for (int q = 0; q < 8; q++)
+    if (cfg->reserved[q]) return fail(FDTD_E_ARG, "reserved fields must be zero");
+  fdtd_geometry geo;
+  int rc = fdtd_geometry_of(cfg, &geo);
+  if (rc) return rc;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(FDTD_E_CUDA, "no CUDA device is visible (the engine has no CPU path)");
+  }
+  fdtd_sim *s = new (std::nothrow) fdtd_sim();
+  if (!s) return fail(FDTD_E_NOMEM, "host allocation failed");
+  s->solver = solver;
+  s->tm = is_tm(solver);
+  s->mpi = is_mpi(solver);
+  s->cfg = *cfg;
+  s->geo = geo;
+  s->f32 = cfg->precision == FDTD_F32;
+  // array frame: MPI -> (N_PX+2) x (N_PY+2) halo ring, x = i-1; serial -> N_PX x N_PY, x = i
+  s->ox = s->mpi ? -1 : 0;
+  s->ni = s->mpi ? geo.n_px : geo.n_px - 2;
+  s->nj = s->mpi ? geo.n_py : geo.n_py - 2;
+  s->nxa = s->ni + 2;
+  s->ncols = s->nj + 2;
+  s->pitch = (s->ncols + 7) / 8 * 8;
+  s->esize = s->f32 ? sizeof(float2) : sizeof(double2);
+  s->nslots = s->tm ? 7 : 8;
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete s;
+    return fail(FDTD_E_CUDA, "cudaStreamCreate failed");
+  }
+  const size_t bytes = (size_t)s->nxa * s->pitch * s->esize;
+  for (int a = 0; a < s->nslots; a++) {
+    if (cudaMalloc(&s->d_f[a], bytes) != cudaSuccess) {
+      cudaGetLastError();
+      free_sim(s);
+      return fail(FDTD_E_NOMEM, "cudaMalloc of %zu bytes for a field failed", bytes);
+    }
+    cudaMemsetAsync(s->d_f[a], 0, bytes, s->stream);
+  }
+  const int neps = s->tm ? 1 : 2;
+  const size_t ecount = (size_t)s->nxa * s->pitch;
+  for (int a = 0; a < neps; a++) {
+    if (cudaMalloc(&s->d_ieps64[a], ecount * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&s->d_ieps32[a], ecount * sizeof(float)) != cudaSuccess) {
+      cudaGetLastError();
+      free_sim(s);
+      return fail(FDTD_E_NOMEM, "cudaMalloc of permittivity failed");
+    }
+  }
+  s->host_eps.assign(3, std::vector<double>((size_t)geo.n_px * geo.n_py, 1.0));
+  if ((rc = build_tables(s)) || (rc = build_ntff(s)) || (rc = fdtd_set_eps(s, nullptr, nullptr, nullptr))) {
+    std::string msg = g_err;
+    free_sim(s);
+    g_err = msg;
+    return rc;
+  }
+  s->time = 0;
+  *out = s;
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_destroy(fdtd_sim *s)
+{
+  if (!s) return FDTD_OK;
+  cudaStreamSynchronize(s->stream);
+  free_sim(s);
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_get_geometry(const fdtd_sim *s, fdtd_geometry *out)
+{
+  if (!s || !out) return fail(FDTD_E_ARG, "null argument");
+  *out = s->geo;
+  return FDTD_OK;
+}
+
+// ---------------------------------------------------------------- permittivity
+
+// Map the global-frame permittivity of the E components into the padded
+// device arrays as 1/eps (halo and unused cells 1.0).
+int upload_inv_eps(fdtd_sim *s)
+{
+  const fdtd_geometry &g = s->geo;
+  const int neps = s->tm ? 1 : 2;
+  const size_t count = (size_t)s->nxa * s->pitch;
+  std::vector<double> h64(count);
+  std::vector<float> h32(count);
+  for (int a = 0; a < neps; a++) {
+    const std::vector<double> &src = s->host_eps[a];
+    std::fill(h64.begin(), h64.end(), 1.0);
+    for (int i = 0; i < s->nxa; i++) {
+      const int x = i + s->ox;
+      if (x < 0 || x >= g.n_px) continue;
+      for (int j = 0; j < s->ncols; j++) {
+        const int y = j + s->ox;
+        if (y < 0 || y >= g.n_py) continue;
+        h64[(size_t)i * s->pitch + j] = kEps0 / src[(size_t)x * g.n_py + y];
+      }
+    }
+    for (size_t q = 0; q < count; q++) h32[q] = (float)h64[q];
+    CK(cudaMemcpyAsync(s->d_ieps64[a], h64.data(), count * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemcpyAsync(s->d_ieps32[a], h32.data(), count * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+  }
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_set_eps(fdtd_sim *s, const double *e0, const double *e1, const double *e2)
+{
+  if (!s) return fail(FDTD_E_ARG, "null simulation");
+  const size_t n = (size_t)s->geo.n_px * s->geo.n_py;
+  const double *src[3] = {e0, e1, e2};
+  for (int a = 0; a < 3; a++) {
+    if (src[a]) {
+      for (size_t q = 0; q < n; q++)
+        if (!(src[a][q] > 0) || !std::isfinite(src[a][q]))
+          return fail(FDTD_E_ARG, "permittivity %d at cell %zu is %g (must be finite and > 0)", a, q, src[a][q]);
+      std::memcpy(s->host_eps[a].data(), src[a], n * sizeof(double));
+    }
+  }
+  return upload_inv_eps(s);
+}
+
+// ---------------------------------------------------------------- stepping
+
+template <typename R>
+static StencilView<R> view_of(fdtd_sim *s)
+{
+  StencilView<R> v{};
+  for (int a = 0; a < kMaxSlots; a++) v.f[a] = (typename Cplx<R>::T *)s->d_f[a];
+  for (int a = 0; a < 2; a++)
+    v.inv_eps[a] = std::is_same<R, double>::value ? (const R *)s->d_ieps64[a] : (const R *)s->d_ieps32[a];
+  void *const *tab = std::is_same<R, double>::value ? s->d_tab64 : s->d_tab32;
+  v.tx_i = (const Coef4<R> *)tab[0];
+  v.tx_h = (const Coef4<R> *)tab[1];
+  v.ty_i = (const Coef4<R> *)tab[2];
+  v.ty_h = (const Coef4<R> *)tab[3];
+  v.ex = (const double2 *)s->d_ex;
+  v.ey = (const double2 *)s->d_ey;
+  v.P = s->pitch;
+  v.nxa = s->nxa;
+  v.ni = s->ni;
+  v.nj = s->nj;
+  v.ox = s->ox;
+  v.in_x0 = s->in_x0;
+  v.in_x1 = s->in_x1;
+  v.in_y0 = s->in_y0;
+  v.in_y1 = s->in_y1;
+  v.inv_mu = (R)s->inv_mu;
+  return v;
+}
+
+static NtffView ntff_view(fdtd_sim *s)
+{
+  NtffView n{};
+  for (int a = 0; a < 3; a++) n.acc[a] = (double2 *)s->d_ntff[a];
+  n.shift = (const double *)s->d_shift;
+  n.cells = (const SurfCell *)s->d_cells;
+  n.vals = (double2 *)s->d_vals;
+  n.ncell = s->ncell;
+  n.array_size = s->geo.array_size;
+  n.len = (long long)s->ntff_len;
+  n.status = s->d_status;
+  return n;
+}
+
+// field.c:224-256 per-step constants of the pulse for one component
+static SourceStep pulse_step(const fdtd_sim *s, double time, double gap_x, double gap_y, double dot)
+{
+  SourceStep p{};
+  p.kind = 2;
+  const double rad = s->cfg.angle_deg * M_PI / 180.0;
+  p.cos_per_c = cos(rad) / kC;
+  p.sin_per_c = sin(rad) / kC;
+  const double center_peak =
+      (s->geo.n_px / 2.0 + gap_x) * p.cos_per_c + (s->geo.n_py / 2 + gap_y) * p.sin_per_c;
+  p.t0 = -center_peak + 500;
+  p.time = time;
+  p.w = s->geo.omega_s;
+  p.gap_x = gap_x;
+  p.gap_y = gap_y;
+  p.dot = dot;
+  return p;
+}
+
+template <typename R>
+static void enqueue_step(fdtd_sim *s, double time, double ray_coef)
+{
+  const StencilView<R> v = view_of<R>(s);
+  const NtffView n = ntff_view(s);
+  cudaStream_t st = s->stream;
+  const double coef = s->mpi ? 1.0 / (4 * M_PI * kC * 1.0e6) : 1.0;  // mpiTM_UPML.c:852-854
+  if (s->mpi) {
+    SourceStep cw{};
+    cw.kind = 1;
+    const double wt = s->geo.omega_s * time;
+    cw.s_re = ray_coef * cos(wt);
+    cw.s_im = -ray_coef * sin(wt);
+    if (s->tm) {
+      launch_tm_e<R>(v, cw, st);
+      launch_tm_h<R>(v, st);
+    } else {
+      SourceStep none{};
+      launch_te_e<R>(v, none, cw, st);
+      launch_te_h<R>(v, st);
+    }
+  } else if (s->tm) {  // fdtdTM_upml.c:54-66
+    launch_tm_h<R>(v, st);
+    launch_tm_e<R>(v, pulse_step(s, time, 0, 0, 1.0), st);
+  } else {             // fdtdTE_upml.c:168-192
+    launch_te_h<R>(v, st);
+    const double co = cos((s->cfg.angle_deg + 90) * M_PI / 180.0);
+    const double si = sin((s->cfg.angle_deg + 90) * M_PI / 180.0);
+    SourceStep sx{}, sy{};
+    if (co != 0.0) sx = pulse_step(s, time, 0.5, 0.0, co);
+    if (si != 0.0) sy = pulse_step(s, time, 0.0, 0.5, si);
+    launch_te_e<R>(v, sx, sy, st);
+  }
+  launch_ntff_gather<R>(v, n, coef, st);
+  launch_ntff_accumulate(n, time - 1, time - 0.5, st);
+  s->launches += 4;
+}
+
+// The reference steps only while time < maxTime (field.c:317-319); past it
+// the flat NTFF index leaves its allocation, so the engine refuses.
+static int check_clock(const fdtd_sim *s, double time)
+{
+  if (!(time >= 0) || time > (double)s->cfg.step_num - 1)
+    return fail(FDTD_E_STATE, "time %g outside [0, step_num-1 = %d]", time, s->cfg.step_num - 1);
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_update(fdtd_sim *s, double time, double ray_coef)
+{
+  if (!s) return fail(FDTD_E_ARG, "null simulation");
+  if (int rc = check_clock(s, time)) return rc;
+  if (s->f32) enqueue_step<float>(s, time, ray_coef);
+  else enqueue_step<double>(s, time, ray_coef);
+  CK(cudaGetLastError());
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_run(fdtd_sim *s, int n_steps)
+{
+  if (!s) return fail(FDTD_E_ARG, "null simulation");
+  if (n_steps < 0) return fail(FDTD_E_ARG, "n_steps < 0");
+  if (n_steps > 0)
+    if (int rc = check_clock(s, s->time + (n_steps - 1))) return rc;
+  for (int q = 0; q < n_steps; q++) {
+    const double t = s->time;
+    const double rc = s->ray_coef;
+    if (s->f32) enqueue_step<float>(s, t, rc);
+    else enqueue_step<double>(s, t, rc);
+    // field.c:312-315
+    s->time = t + 1.0;
+    s->ray_coef = 1.0 - exp(-pow(0.01 * s->time, 2));
+  }
+  CK(cudaGetLastError());
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_get_time(const fdtd_sim *s, double *t)
+{
+  if (!s || !t) return fail(FDTD_E_ARG, "null argument");
+  *t = s->time;
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_set_time(fdtd_sim *s, double t)
+{
+  if (!s) return fail(FDTD_E_ARG, "null simulation");
+  s->time = t;
+  s->ray_coef = t == 0 ? 0.0 : 1.0 - exp(-pow(0.01 * t, 2));
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_synchronize(fdtd_sim *s)
+{
+  if (!s) return fail(FDTD_E_ARG, "null simulation");
+  CK(cudaStreamSynchronize(s->stream));
+  return FDTD_OK;
+}
+
+extern "C" long long fdtd_launch_count(const fdtd_sim *s) { return s ? s->launches : 0; }
+
+extern "C" int fdtd_get_status(fdtd_sim *s, unsigned int *flags)
+{
+  if (!s || !flags) return fail(FDTD_E_ARG, "null argument");
+  CK(cudaStreamSynchronize(s->stream));
+  CK(cudaMemcpy(flags, s->d_status, sizeof(unsigned int), cudaMemcpyDeviceToHost));
+  return FDTD_OK;
+}
+
+// ---------------------------------------------------------------- copy-out
+
+static int field_slot(const fdtd_sim *s, int which)
+{
+  static const int tm_slot[3] = {0, 3, 4}, te_slot[3] = {0, 1, 6};
+  if (which < 0 || which > 2) return -1;
+  return s->tm ? tm_slot[which] : te_slot[which];
+}
+
+extern "C" int fdtd_get_field(fdtd_sim *s, int which, int layout, double *out)
+{
+  if (!s || !out) return fail(FDTD_E_ARG, "null argument");
+  const int slot = field_slot(s, which);
+  if (slot < 0) return fail(FDTD_E_ARG, "field index %d out of range", which);
+  if (layout != FDTD_LAYOUT_GLOBAL && layout != FDTD_LAYOUT_SOLVER) return fail(FDTD_E_ARG, "bad layout");
+  // rows/cols of the array to copy, in array coordinates
+  int r0, c0, nr, nc;
+  if (s->mpi && layout == FDTD_LAYOUT_GLOBAL) { r0 = 1; c0 = 1; nr = s->geo.n_px; nc = s->geo.n_py; }
+  else { r0 = 0; c0 = 0; nr = s->nxa; nc = s->ncols; }
+  CK(cudaStreamSynchronize(s->stream));
+  const char *src = (const char *)s->d_f[slot] + ((size_t)r0 * s->pitch + c0) * s->esize;
+  if (!s->f32) {
+    CK(cudaMemcpy2D(out, (size_t)nc * 16, src, (size_t)s->pitch * 16, (size_t)nc * 16, nr, cudaMemcpyDeviceToHost));
+  } else {
+    std::vector<float2> tmp((size_t)nr * nc);
+    CK(cudaMemcpy2D(tmp.data(), (size_t)nc * 8, src, (size_t)s->pitch * 8, (size_t)nc * 8, nr,
+                    cudaMemcpyDeviceToHost));
+    for (size_t q = 0; q < tmp.size(); q++) { out[2 * q] = tmp[q].x; out[2 * q + 1] = tmp[q].y; }
+  }
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_get_eps(fdtd_sim *s, int which, int layout, double *out)
+{
+  if (!s || !out) return fail(FDTD_E_ARG, "null argument");
+  if (which < 0 || which > 2) return fail(FDTD_E_ARG, "eps index %d out of range", which);
+  const fdtd_geometry &g = s->geo;
+  const std::vector<double> &e = s->host_eps[which];
+  if (layout == FDTD_LAYOUT_GLOBAL || !s->mpi) {
+    std::memcpy(out, e.data(), e.size() * sizeof(double));
+    return FDTD_OK;
+  }
+  const int ny = g.n_py + 2;
+  std::memset(out, 0, sizeof(double) * (size_t)(g.n_px + 2) * ny);
+  for (int x = 0; x < g.n_px; x++)
+    std::memcpy(out + (size_t)(x + 1) * ny + 1, &e[(size_t)x * g.n_py], sizeof(double) * g.n_py);
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_get_ntff(fdtd_sim *s, int which, double *out)
+{
+  if (!s || !out) return fail(FDTD_E_ARG, "null argument");
+  if (which < 0 || which > 2) return fail(FDTD_E_ARG, "ntff index %d out of range", which);
+  CK(cudaStreamSynchronize(s->stream));
+  CK(cudaMemcpy(out, (const double2 *)s->d_ntff[which] + kGuard, sizeof(double2) * 360 * s->geo.array_size,
+                cudaMemcpyDeviceToHost));
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_get_ntff_guard(fdtd_sim *s, int which, double *out, int *guard)
+{
+  if (!s || !out) return fail(FDTD_E_ARG, "null argument");
+  if (which < 0 || which > 2) return fail(FDTD_E_ARG, "ntff index %d out of range", which);
+  CK(cudaStreamSynchronize(s->stream));
+  const double2 *base = (const double2 *)s->d_ntff[which];
+  CK(cudaMemcpy(out, base, sizeof(double2) * kGuard, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(out + 2 * kGuard, base + kGuard + (size_t)360 * s->geo.array_size, sizeof(double2) * kGuard,
+                cudaMemcpyDeviceToHost));
+  if (guard) *guard = kGuard;
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_reset(fdtd_sim *s)
+{
+  if (!s) return fail(FDTD_E_ARG, "null simulation");
+  const size_t bytes = (size_t)s->nxa * s->pitch * s->esize;
+  for (int a = 0; a < s->nslots; a++) CK(cudaMemsetAsync(s->d_f[a], 0, bytes, s->stream));
+  if (!s->mpi)
+    for (int a = 0; a < 3; a++) CK(cudaMemsetAsync(s->d_ntff[a], 0, sizeof(double2) * s->ntff_len, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  s->time = 0;
+  s->ray_coef = 0;
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_device_field(fdtd_sim *s, int which, void **dptr, int *pitch, int *rows)
+{
+  if (!s || !dptr) return fail(FDTD_E_ARG, "null argument");
+  const int slot = field_slot(s, which);
+  if (slot < 0) return fail(FDTD_E_ARG, "field index %d out of range", which);
+  *dptr = s->d_f[slot];
+  if (pitch) *pitch = s->pitch;
+  if (rows) *rows = s->nxa;
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_fill_eps_model(fdtd_sim *s, int model, const double *params, int n_params)
+{
+  (void)params;
+  (void)n_params;
+  if (!s) return fail(FDTD_E_ARG, "null simulation");
+  if (model == FDTD_MODEL_NONE) {
+    for (auto &e : s->host_eps) std::fill(e.begin(), e.end(), 1.0);
+    return upload_inv_eps(s);
+  }
+  return fail(FDTD_E_UNSUPPORTED, "model %d is not built into this engine yet", model);
+}

@@ -1,0 +1,100 @@
+// fdtd_internal.cuh -- device-side data structures of the GB300 FDTD engine.
+//
+// Layout in HBM (one simulation):
+//   every field is a pitched 2-D array of complex values, rows i in [0, nxa),
+//   columns j in [0, P), y (j) contiguous as in the reference (field.c:70-74).
+//   Active cells are i in [1, ni], j in [1, nj]; the ring around them is a
+//   zero halo (PEC): for the MPI solvers it is the one-rank sub-domain halo
+//   of mpiTM_UPML.c:737-741 (global x = i-1), for the serial solvers it is
+//   the boundary ring the reference never updates (global x = i).
+//   P is a multiple of 8 complex values so every row starts on a 128-byte
+//   boundary and a warp's 32 consecutive j are one coalesced 512-byte (FP64)
+//   or 256-byte (FP32) transaction.
+//
+// PML coefficients are separable (every C_* of mpiTM_UPML.c:697-713 and
+// mpiTE_UPML.c:517-533 depends on sigma_x at one stagger and/or sigma_y at
+// one stagger), so they live in four 1-D tables per simulation instead of the
+// reference's 15 per-cell arrays.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+
+#include "../../include/mpifdtd_gb300.h"
+
+namespace fdtd {
+
+constexpr double kC = 0.7071;                 // field.h:70 C_0_S
+constexpr double kEps0 = 1.0;                 // field.h:73
+constexpr double kZ0 = 1.41422712488;         // field.h:75
+constexpr int kGuard = 16;                    // NTFF guard cells each side
+constexpr int kNfft = 8192;                   // ntff.h:6 NTFF_NUM
+constexpr int kLambdaSt = 380, kLambdaEn = 700;  // ntff.h:4-5
+
+template <typename R> struct Cplx;
+template <> struct Cplx<double> { using T = double2; };
+template <> struct Cplx<float> { using T = float2; };
+
+// One entry of a 1-D coefficient table (meaning depends on table, see
+// fdtd_api.cu build_coefficients()).
+template <typename R> struct Coef4 { R a, b, c, d; };
+
+// Field slots.  TM: 0 Ez 1 Dz 2 Jz 3 Hx 4 Hy 5 Mx 6 My (M scaled by 1/mu0)
+//               TE: 0 Ex 1 Ey 2 Dx 3 Dy 4 Jx 5 Jy 6 Hz 7 Mz (M scaled by 1/mu0)
+constexpr int kMaxSlots = 8;
+
+template <typename R>
+struct StencilView {
+  typename Cplx<R>::T *f[kMaxSlots];
+  const R *inv_eps[2];          // TM: [0] 1/EPS_EZ ; TE: [0] 1/EPS_EX, [1] 1/EPS_EY
+  const Coef4<R> *tx_i, *tx_h;  // indexed by row i (sigma_x at x, x+1/2)
+  const Coef4<R> *ty_i, *ty_h;  // indexed by column j (sigma_y at y, y+1/2)
+  const double2 *ex, *ey;       // CW source phase tables e^{i x kcos}, e^{i y ksin}
+  int P, nxa, ni, nj, ox;
+  int in_x0, in_x1, in_y0, in_y1;  // interior (all sigma = 0): x in [in_x0,in_x1)
+  R inv_mu;
+};
+
+// Per-step source description.
+struct SourceStep {
+  int kind;          // 0 none, 1 CW scattered wave (MPI solvers), 2 Gaussian pulse (serial)
+  double s_re, s_im; // CW: ray_coef * e^{-i w t}
+  // pulse (field.c:224-256), applied to field slot `slot` with permittivity table `eps_slot`
+  double time, t0, w, cos_per_c, sin_per_c, gap_x, gap_y, dot;
+};
+
+// Surface cell of the NTFF integration path.
+struct SurfCell {
+  long long k;       // array index of the E sample
+  int hoff;          // offset of the second H sample (-1 bottom/top, -P right/left)
+  signed char sign;  // +1 / -1 (normal orientation, mpiTM_UPML.c:877-1035)
+  signed char e_slot, h_slot, uid_wid;   // uid_wid = uid | (wid << 4)
+};
+
+struct NtffView {
+  double2 *acc[3];        // base pointers incl. guard (flat [360][AS] + 2*guard)
+  const double *shift;    // [360][ncell] retarded-time shift per (angle, cell)
+  const SurfCell *cells;
+  double2 *vals;          // [2][ncell] surface values of this step (E then H)
+  int ncell, array_size;
+  long long len;          // elements of each accumulator incl. guards
+  unsigned int *status;   // device status word (kStatus* bits)
+};
+
+// Device status bits (fdtd_get_status).
+constexpr unsigned int kStatusNtffRange = 1u;   // a deposit fell outside the accumulator
+
+// Launchers (fdtd_kernels.cu).  All take the stream they run on.
+template <typename R>
+void launch_tm_e(const StencilView<R> &v, const SourceStep &s, cudaStream_t st);
+template <typename R>
+void launch_tm_h(const StencilView<R> &v, cudaStream_t st);
+template <typename R>
+void launch_te_e(const StencilView<R> &v, const SourceStep &sx, const SourceStep &sy, cudaStream_t st);
+template <typename R>
+void launch_te_h(const StencilView<R> &v, cudaStream_t st);
+template <typename R>
+void launch_ntff_gather(const StencilView<R> &v, const NtffView &n, double coef, cudaStream_t st);
+void launch_ntff_accumulate(const NtffView &n, double timeE, double timeH, cudaStream_t st);
+
+}  // namespace fdtd

@@ -1,0 +1,357 @@
+// fdtd_kernels.cu -- sm_103a kernels of the 2-D UPML FDTD time step.
+//
+// One time step of the MPI solvers (mpiTM_UPML.c:196-217, mpiTE_UPML.c:290-304)
+// is four launches:
+//   e-half  : calcJD + calcE + scatteredWave fused (one sweep over the grid)
+//   h-half  : calcMB + calcH fused
+//   gather  : the tangential E/H samples of the NTFF surface
+//   accum   : the 360-angle retarded-time deposit (mpiTM_UPML.c:849-1037)
+// The serial solvers run h-half, e-half (+ pulse), gather, accum
+// (fdtdTM_upml.c:54-66, fdtdTE_upml.c:168-192).
+//
+// Interior cells (sigma_x = sigma_y = 0 at every stagger) have every UPML
+// coefficient exactly 1, so the J/M auxiliaries drop out algebraically:
+//   TM: Dz += curl H ; Hx -= dEz/dy / mu0 ; Hy += dEz/dx / mu0
+// which is the reference's update with C_* = 1 up to rounding (the reference
+// computes (Dz + Jz') - Jz where this computes Dz + (Jz' - Jz)).  PML cells run
+// the full Gedney update with coefficients from the 1-D tables.  H is stored
+// instead of B (B/mu0, mpiTM_UPML.c:526-527) and M is stored scaled by 1/mu0,
+// which turns every H update into one FMA per component.
+#include <cuda_runtime.h>
+
+#include "fdtd_internal.cuh"
+
+namespace fdtd {
+
+template <typename T> struct Cx;
+template <> struct Cx<double2> { using R = double; };
+template <> struct Cx<float2> { using R = float; };
+
+template <typename T> __device__ __forceinline__ T cadd(T a, T b) { a.x += b.x; a.y += b.y; return a; }
+template <typename T> __device__ __forceinline__ T csub(T a, T b) { a.x -= b.x; a.y -= b.y; return a; }
+template <typename T, typename R> __device__ __forceinline__ T cscale(T a, R s) { a.x *= s; a.y *= s; return a; }
+template <typename T> __device__ __forceinline__ T ldro(const T *p) { return __ldg(p); }
+
+__device__ __forceinline__ bool is_one(double v) { return __double_as_longlong(v) == 0x3FF0000000000000LL; }
+__device__ __forceinline__ bool is_one(float v) { return __float_as_int(v) == 0x3F800000; }
+
+// CW scattered-wave increment at array cell (i, j): ray_coef (1/eps - 1) e^{i(kr - w t)}
+// (mpiTM_UPML.c:369-370).  kr is split as x*kcos + y*ksin, so e^{ikr} is the
+// product of two 1-D tables; e^{-i w t} * ray_coef comes from the host per step.
+template <typename R>
+__device__ __forceinline__ void cw_source(const StencilView<R> &v, const SourceStep &s, int i, int j, R ie,
+                                          typename Cplx<R>::T &e)
+{
+  const double2 ex = v.ex[i], ey = v.ey[j];
+  const double pr = ex.x * ey.x - ex.y * ey.y;
+  const double pi = ex.x * ey.y + ex.y * ey.x;
+  const double amp = (double)ie - 1.0;
+  const double qr = (pr * s.s_re - pi * s.s_im) * amp;
+  const double qi = (pr * s.s_im + pi * s.s_re) * amp;
+  e.x = (R)((double)e.x + qr);
+  e.y = (R)((double)e.y + qi);
+}
+
+// Gaussian-pulse scattered field (field.c:224-256) at array cell (i, j).
+template <typename R>
+__device__ __forceinline__ void pulse_source(const SourceStep &s, int i, int j, R ie, typename Cplx<R>::T &e)
+{
+  const double pos = __dadd_rn(__dmul_rn((double)i + s.gap_x, s.cos_per_c),
+                               __dmul_rn((double)j + s.gap_y, s.sin_per_c));
+  const double r = __dsub_rn(pos, s.time - s.t0);
+  const double q = __ddiv_rn(r, 50.0);
+  const double g = exp(-(q * q));
+  const double amp = s.dot * g * ((double)ie - 1.0);
+  double sn, cs;
+  sincos(r * s.w, &sn, &cs);
+  e.x = (R)((double)e.x + amp * cs);
+  e.y = (R)((double)e.y + amp * sn);
+}
+
+template <typename R>
+__device__ __forceinline__ void apply_source(const StencilView<R> &v, const SourceStep &s, int i, int j, R ie,
+                                             typename Cplx<R>::T &e)
+{
+  if (s.kind == 1) cw_source<R>(v, s, i, j, ie, e);
+  else if (s.kind == 2) pulse_source<R>(s, i, j, ie, e);
+}
+
+template <typename R>
+__device__ __forceinline__ bool interior(const StencilView<R> &v, int i, int j)
+{
+  const int x = i + v.ox, y = j + v.ox;
+  return x >= v.in_x0 && x < v.in_x1 && y >= v.in_y0 && y < v.in_y1;
+}
+
+// ------------------------------------------------------------------ TM
+
+// calcJD + calcE + scatteredWave (mpiTM_UPML.c:431-458, :337-374)
+template <typename R>
+__global__ void __launch_bounds__(256) tm_e_kernel(StencilView<R> v, SourceStep s)
+{
+  using T = typename Cplx<R>::T;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i < 1 || i > v.ni || j < 1 || j > v.nj) return;
+  const size_t k = (size_t)i * v.P + j;
+  T *Ez = v.f[0], *Dz = v.f[1], *Jz = v.f[2];
+  const T *Hx = v.f[3], *Hy = v.f[4];
+  const T hyk = ldro(Hy + k), hyl = ldro(Hy + k - v.P), hxk = ldro(Hx + k), hxb = ldro(Hx + k - 1);
+  T curl;
+  curl.x = ((hyk.x - hyl.x) - hxk.x) + hxb.x;
+  curl.y = ((hyk.y - hyl.y) - hxk.y) + hxb.y;
+  T dz = Dz[k];
+  if (interior(v, i, j)) {
+    dz = cadd(dz, curl);
+  } else {
+    const Coef4<R> cx = v.tx_i[i], cy = v.ty_i[j];
+    const T jz = Jz[k];
+    T jn;
+    jn.x = cx.a * jz.x + cx.b * curl.x;          // C_JZ Jz + C_JZHXHY curl
+    jn.y = cx.a * jz.y + cx.b * curl.y;
+    dz.x = (cy.a * dz.x + cy.b * jn.x) - cy.b * jz.x;   // C_DZ Dz + C_DZJZ1 Jz' - C_DZJZ0 Jz
+    dz.y = (cy.a * dz.y + cy.b * jn.y) - cy.b * jz.y;
+    Jz[k] = jn;
+  }
+  Dz[k] = dz;
+  const R ie = v.inv_eps[0][k];
+  T ez = dz;
+  if (!is_one(ie)) {
+    ez = cscale(dz, ie);
+    apply_source<R>(v, s, i, j, ie, ez);
+  }
+  Ez[k] = ez;
+}
+
+// calcMB + calcH (mpiTM_UPML.c:491-530)
+template <typename R>
+__global__ void __launch_bounds__(256) tm_h_kernel(StencilView<R> v)
+{
+  using T = typename Cplx<R>::T;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i < 1 || i > v.ni || j < 1 || j > v.nj) return;
+  const size_t k = (size_t)i * v.P + j;
+  const T *Ez = v.f[0];
+  T *Hx = v.f[3], *Hy = v.f[4], *Mx = v.f[5], *My = v.f[6];
+  const T ek = ldro(Ez + k), et = ldro(Ez + k + 1), er = ldro(Ez + k + v.P);
+  const T dEx = csub(et, ek);           // Ez[k_top] - Ez[k]
+  const T dEy = csub(ek, er);           // -Ez[k_rht] + Ez[k]
+  T hx = Hx[k], hy = Hy[k];
+  if (interior(v, i, j)) {
+    hx.x -= v.inv_mu * dEx.x; hx.y -= v.inv_mu * dEx.y;
+    hy.x -= v.inv_mu * dEy.x; hy.y -= v.inv_mu * dEy.y;
+  } else {
+    const Coef4<R> cxi = v.tx_i[i], cxh = v.tx_h[i], cyi = v.ty_i[j], cyh = v.ty_h[j];
+    const T mx = Mx[k], my = My[k];
+    T mxn, myn;
+    mxn.x = cyh.a * mx.x - cyh.b * dEx.x;        // C_MX Mx - C_MXEZ/mu0 dE
+    mxn.y = cyh.a * mx.y - cyh.b * dEx.y;
+    hx.x = (hx.x + cxi.c * mxn.x) - cxi.d * mx.x;   // C_BX(=1) H + C_BXMX1 Mx' - C_BXMX0 Mx
+    hx.y = (hx.y + cxi.c * mxn.y) - cxi.d * mx.y;
+    myn.x = my.x - v.inv_mu * dEy.x;              // C_MY(=1) My - C_MYEZ(=1)/mu0 dE
+    myn.y = my.y - v.inv_mu * dEy.y;
+    const R c1 = cyi.c * cxh.b, c0 = cyi.d * cxh.b;  // C_BYMY1, C_BYMY0
+    hy.x = (cxh.a * hy.x + c1 * myn.x) - c0 * my.x;
+    hy.y = (cxh.a * hy.y + c1 * myn.y) - c0 * my.y;
+    Mx[k] = mxn;
+    My[k] = myn;
+  }
+  Hx[k] = hx;
+  Hy[k] = hy;
+}
+
+// ------------------------------------------------------------------ TE
+
+// calcJD + calcE + scatteredWave on Ey (mpiTE_UPML.c:337-375, :250-281)
+template <typename R>
+__global__ void __launch_bounds__(256) te_e_kernel(StencilView<R> v, SourceStep sx, SourceStep sy)
+{
+  using T = typename Cplx<R>::T;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i < 1 || i > v.ni || j < 1 || j > v.nj) return;
+  const size_t k = (size_t)i * v.P + j;
+  T *Ex = v.f[0], *Ey = v.f[1], *Dx = v.f[2], *Dy = v.f[3], *Jx = v.f[4], *Jy = v.f[5];
+  const T *Hz = v.f[6];
+  const T hzk = ldro(Hz + k), hzb = ldro(Hz + k - 1), hzl = ldro(Hz + k - v.P);
+  const T cxv = csub(hzk, hzb);          // Hz[k] - Hz[k_btm]
+  T cyv;                                 // -Hz[k] + Hz[k_lft]
+  cyv.x = -hzk.x + hzl.x;
+  cyv.y = -hzk.y + hzl.y;
+  T dx = Dx[k], dy = Dy[k];
+  if (interior(v, i, j)) {
+    dx = cadd(dx, cxv);
+    dy = cadd(dy, cyv);
+  } else {
+    const Coef4<R> cxh = v.tx_h[i], cxi = v.tx_i[i], cyi = v.ty_i[j], cyh = v.ty_h[j];
+    const T jx = Jx[k], jy = Jy[k];
+    T jxn, jyn;
+    jxn.x = cyi.a * jx.x + cyi.b * cxv.x;         // C_JX Jx + C_JXHZ curl
+    jxn.y = cyi.a * jx.y + cyi.b * cxv.y;
+    dx.x = (dx.x + cxh.a * jxn.x) - cxh.b * jx.x;  // C_DX(=1) Dx + C_DXJX1 Jx' - C_DXJX0 Jx
+    dx.y = (dx.y + cxh.a * jxn.y) - cxh.b * jx.y;
+    jyn = cadd(jy, cyv);                          // C_JY(=1) Jy + C_JYHZ(=1) curl
+    const R c1 = cyh.c * cxi.b, c0 = cyh.d * cxi.b;  // C_DYJY1, C_DYJY0
+    dy.x = (cxi.a * dy.x + c1 * jyn.x) - c0 * jy.x;
+    dy.y = (cxi.a * dy.y + c1 * jyn.y) - c0 * jy.y;
+    Jx[k] = jxn;
+    Jy[k] = jyn;
+  }
+  Dx[k] = dx;
+  Dy[k] = dy;
+  const R iex = v.inv_eps[0][k], iey = v.inv_eps[1][k];
+  T ex = dx, ey = dy;
+  if (!is_one(iex)) {
+    ex = cscale(dx, iex);
+    if (sx.kind) apply_source<R>(v, sx, i, j, iex, ex);
+  }
+  if (!is_one(iey)) {
+    ey = cscale(dy, iey);
+    apply_source<R>(v, sy, i, j, iey, ey);
+  }
+  Ex[k] = ex;
+  Ey[k] = ey;
+}
+
+// calcMB + calcH (mpiTE_UPML.c:377-399)
+template <typename R>
+__global__ void __launch_bounds__(256) te_h_kernel(StencilView<R> v)
+{
+  using T = typename Cplx<R>::T;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i < 1 || i > v.ni || j < 1 || j > v.nj) return;
+  const size_t k = (size_t)i * v.P + j;
+  const T *Ex = v.f[0], *Ey = v.f[1];
+  T *Hz = v.f[6], *Mz = v.f[7];
+  const T eyr = ldro(Ey + k + v.P), eyk = ldro(Ey + k), ext = ldro(Ex + k + 1), exk = ldro(Ex + k);
+  T ce;                                  // Ey[k_rht] - Ey[k] - Ex[k_top] + Ex[k]
+  ce.x = ((eyr.x - eyk.x) - ext.x) + exk.x;
+  ce.y = ((eyr.y - eyk.y) - ext.y) + exk.y;
+  T hz = Hz[k];
+  if (interior(v, i, j)) {
+    hz.x -= v.inv_mu * ce.x;
+    hz.y -= v.inv_mu * ce.y;
+  } else {
+    const Coef4<R> cxh = v.tx_h[i], cyh = v.ty_h[j];
+    const T mz = Mz[k];
+    T mzn;
+    mzn.x = cxh.c * mz.x - cxh.d * ce.x;          // C_MZ Mz - C_MZEXEY/mu0 curl
+    mzn.y = cxh.c * mz.y - cxh.d * ce.y;
+    hz.x = (cyh.a * hz.x + cyh.b * mzn.x) - cyh.b * mz.x;   // C_BZ H + C_BZMZ1 Mz' - C_BZMZ0 Mz
+    hz.y = (cyh.a * hz.y + cyh.b * mzn.y) - cyh.b * mz.y;
+    Mz[k] = mzn;
+  }
+  Hz[k] = hz;
+}
+
+// ------------------------------------------------------------------ NTFF
+
+// Tangential samples of the NTFF path, already signed and scaled:
+//   e = sign * E[k] * coef,  h = sign * 0.5 * (H[k] + H[k+hoff]) * coef
+template <typename R>
+__global__ void ntff_gather_kernel(StencilView<R> v, NtffView n, double coef)
+{
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n.ncell) return;
+  const SurfCell sc = n.cells[c];
+  const typename Cplx<R>::T *E = v.f[sc.e_slot], *H = v.f[sc.h_slot];
+  const auto e = E[sc.k];
+  const auto h0 = H[sc.k], h1 = H[sc.k + sc.hoff];
+  const double sg = sc.sign;
+  double2 ev, hv;
+  ev.x = sg * (double)e.x * coef;
+  ev.y = sg * (double)e.y * coef;
+  hv.x = (sg * 0.5) * ((double)h0.x + (double)h1.x) * coef;
+  hv.y = (sg * 0.5) * ((double)h0.y + (double)h1.y) * coef;
+  n.vals[c] = ev;
+  n.vals[n.ncell + c] = hv;
+}
+
+// Three-tap deposit of mpiTM_UPML.c:840-847 (and ntffTM.c:279-288):
+//   m = floor(t+0.5), a = 0.5+t-m, b = 1-a:  U[m-1] += v b, U[m] += v (a-b), U[m+1] -= v a
+__device__ __forceinline__ void deposit(const NtffView &n, double2 *acc, long long row, double t, double2 val)
+{
+  const double u = t + 0.5;
+  const double mf = floor(u);
+  const double a = u - mf, b = 1.0 - a, ab = a - b;
+  const long long at = row + (long long)mf;
+  if (!(mf > -1e15 && mf < 1e15) || at - 1 < 0 || at + 1 >= n.len) {  // never write outside
+    atomicOr(n.status, kStatusNtffRange);
+    return;
+  }
+  double2 *p = acc + at;
+  atomicAdd(&p[-1].x, val.x * b);
+  atomicAdd(&p[-1].y, val.y * b);
+  atomicAdd(&p[0].x, val.x * ab);
+  atomicAdd(&p[0].y, val.y * ab);
+  atomicAdd(&p[1].x, -(val.x * a));
+  atomicAdd(&p[1].y, -(val.y * a));
+}
+
+__global__ void __launch_bounds__(256) ntff_accumulate_kernel(NtffView n, double timeE, double timeH)
+{
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ang = blockIdx.y;
+  if (c >= n.ncell) return;
+  const double sh = n.shift[(size_t)ang * n.ncell + c];
+  const unsigned char uw = (unsigned char)n.cells[c].uid_wid;
+  const long long row = (long long)kGuard + (long long)ang * n.array_size;
+  deposit(n, n.acc[uw & 15], row, timeE + sh, n.vals[c]);
+  deposit(n, n.acc[uw >> 4], row, timeH + sh, n.vals[n.ncell + c]);
+}
+
+// ------------------------------------------------------------------ launchers
+
+template <typename R>
+static dim3 grid_of(const StencilView<R> &v, dim3 b)
+{
+  return dim3((unsigned)((v.nj + 2 + b.x - 1) / b.x), (unsigned)((v.nxa + b.y - 1) / b.y));
+}
+
+static const dim3 kBlock(32, 8);
+
+template <typename R>
+void launch_tm_e(const StencilView<R> &v, const SourceStep &s, cudaStream_t st)
+{
+  tm_e_kernel<R><<<grid_of(v, kBlock), kBlock, 0, st>>>(v, s);
+}
+template <typename R>
+void launch_tm_h(const StencilView<R> &v, cudaStream_t st)
+{
+  tm_h_kernel<R><<<grid_of(v, kBlock), kBlock, 0, st>>>(v);
+}
+template <typename R>
+void launch_te_e(const StencilView<R> &v, const SourceStep &sx, const SourceStep &sy, cudaStream_t st)
+{
+  te_e_kernel<R><<<grid_of(v, kBlock), kBlock, 0, st>>>(v, sx, sy);
+}
+template <typename R>
+void launch_te_h(const StencilView<R> &v, cudaStream_t st)
+{
+  te_h_kernel<R><<<grid_of(v, kBlock), kBlock, 0, st>>>(v);
+}
+template <typename R>
+void launch_ntff_gather(const StencilView<R> &v, const NtffView &n, double coef, cudaStream_t st)
+{
+  ntff_gather_kernel<R><<<(n.ncell + 255) / 256, 256, 0, st>>>(v, n, coef);
+}
+void launch_ntff_accumulate(const NtffView &n, double timeE, double timeH, cudaStream_t st)
+{
+  dim3 g((unsigned)((n.ncell + 255) / 256), 360);
+  ntff_accumulate_kernel<<<g, 256, 0, st>>>(n, timeE, timeH);
+}
+
+#define INST(R)                                                                                    \
+  template void launch_tm_e<R>(const StencilView<R> &, const SourceStep &, cudaStream_t);        \
+  template void launch_tm_h<R>(const StencilView<R> &, cudaStream_t);                            \
+  template void launch_te_e<R>(const StencilView<R> &, const SourceStep &, const SourceStep &,   \
+                               cudaStream_t);                                                    \
+  template void launch_te_h<R>(const StencilView<R> &, cudaStream_t);                            \
+  template void launch_ntff_gather<R>(const StencilView<R> &, const NtffView &, double, cudaStream_t);
+INST(double)
+INST(float)
+#undef INST
+
+}  // namespace fdtd

@@ -1,0 +1,39 @@
+// fdtd_sim.h -- host-side state of one simulation (opaque fdtd_sim of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "../../include/mpifdtd_gb300.h"
+#include "fdtd_internal.cuh"
+
+struct fdtd_sim {
+  int solver = 0;
+  bool tm = false, mpi = false, f32 = false;
+  fdtd_config cfg{};
+  fdtd_geometry geo{};
+  // array frame (see fdtd_internal.cuh)
+  int ox = 0, ni = 0, nj = 0, nxa = 0, ncols = 0, pitch = 0;
+  size_t esize = 0;
+  int nslots = 0;
+  int in_x0 = 0, in_x1 = 0, in_y0 = 0, in_y1 = 0;
+  double inv_mu = 0;
+  cudaStream_t stream = nullptr;
+  void *d_f[fdtd::kMaxSlots] = {};
+  void *d_ieps64[2] = {}, *d_ieps32[2] = {};
+  void *d_tab64[4] = {}, *d_tab32[4] = {};
+  void *d_ex = nullptr, *d_ey = nullptr;
+  // NTFF
+  void *d_cells = nullptr, *d_shift = nullptr, *d_vals = nullptr;
+  void *d_ntff[3] = {};
+  unsigned int *d_status = nullptr;
+  int ncell = 0;
+  size_t ntff_len = 0;
+  // permittivity as given (global frame), for fdtd_get_eps
+  std::vector<std::vector<double>> host_eps;
+  // engine clock (field.c:21-22 time, ray_coef)
+  double time = 0, ray_coef = 0;
+  long long launches = 0;
+};
+
+int upload_inv_eps(fdtd_sim *s);

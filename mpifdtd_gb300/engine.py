@@ -1,0 +1,266 @@
+"""Python binding of the C ABI in include/mpifdtd_gb300.h (ctypes).
+
+The native library is required: importing this module on a machine where the
+library was not built raises, and creating a Simulation without a CUDA device
+fails with the engine's own error.  There is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+# simulator.h:8-18 enum SOLVER values of the UPML solvers
+TM_UPML_2D, TE_UPML_2D, MPI_TM_UPML_2D, MPI_TE_UPML_2D = 2, 3, 4, 5
+SOLVERS = {"TM_UPML": TM_UPML_2D, "TE_UPML": TE_UPML_2D,
+           "MPI_TM_UPML": MPI_TM_UPML_2D, "MPI_TE_UPML": MPI_TE_UPML_2D}
+F64, F32 = 0, 1
+LAYOUT_GLOBAL, LAYOUT_SOLVER = 0, 1
+MODEL_NONE, MODEL_CIRCLE, MODEL_MORPHO = 0, 1, 3
+
+_ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "bad state", 5: "unsupported"}
+
+
+class FdtdError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{_ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+@dataclass
+class FieldInfo:
+    """field.h:20-28 FieldInfo (physical sizes in nm)."""
+    width_nm: int
+    height_nm: int
+    h_u_nm: int
+    pml: int
+    lambda_nm: int
+    angle_deg: int
+    step_num: int
+
+    def astuple(self):
+        return (self.width_nm, self.height_nm, self.h_u_nm, self.pml, self.lambda_nm,
+                self.angle_deg, self.step_num)
+
+
+class _Config(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("width_nm", "height_nm", "h_u_nm", "pml", "lambda_nm",
+                                       "angle_deg", "step_num", "precision")] + [("reserved", C.c_int * 8)]
+
+
+class Geometry(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("n_px", "n_py", "n_pml", "n_x", "n_y", "ntff_top", "ntff_bottom",
+                                       "ntff_left", "ntff_right", "ntff_cx", "ntff_cy")] + \
+               [("rf_per_c", C.c_double), ("array_size", C.c_int), ("lambda_s", C.c_double),
+                ("k_s", C.c_double), ("omega_s", C.c_double)]
+
+
+_lib = None
+
+
+def library_path() -> Path:
+    return _build.ENGINE_SO
+
+
+def load():
+    """Load the engine library (built by mpifdtd_gb300.build / __graft_entry__.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    so = library_path()
+    if not so.exists():
+        raise ImportError(f"mpifdtd_gb300 engine library missing ({so}); run mpifdtd_gb300.build.build()")
+    lib = C.CDLL(str(so))
+    P, I, D = C.c_void_p, C.c_int, C.c_double
+    dp = C.POINTER(C.c_double)
+    sig = {
+        "fdtd_geometry_of": (I, [C.POINTER(_Config), C.POINTER(Geometry)]),
+        "fdtd_create": (I, [I, C.POINTER(_Config), C.POINTER(P)]),
+        "fdtd_destroy": (I, [P]),
+        "fdtd_get_geometry": (I, [P, C.POINTER(Geometry)]),
+        "fdtd_set_eps": (I, [P, dp, dp, dp]),
+        "fdtd_fill_eps_model": (I, [P, I, dp, I]),
+        "fdtd_update": (I, [P, D, D]),
+        "fdtd_run": (I, [P, I]),
+        "fdtd_get_time": (I, [P, dp]),
+        "fdtd_set_time": (I, [P, D]),
+        "fdtd_synchronize": (I, [P]),
+        "fdtd_get_field": (I, [P, I, I, dp]),
+        "fdtd_get_eps": (I, [P, I, I, dp]),
+        "fdtd_get_ntff": (I, [P, I, dp]),
+        "fdtd_get_ntff_guard": (I, [P, I, dp, C.POINTER(I)]),
+        "fdtd_reset": (I, [P]),
+        "fdtd_device_field": (I, [P, I, C.POINTER(P), C.POINTER(I), C.POINTER(I)]),
+        "fdtd_launch_count": (C.c_longlong, [P]),
+        "fdtd_get_status": (I, [P, C.POINTER(C.c_uint)]),
+        "fdtd_last_error": (C.c_char_p, []),
+        "fdtd_version": (C.c_char_p, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(rc):
+    if rc != 0:
+        raise FdtdError(rc, load().fdtd_last_error().decode())
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+
+
+def _config(fi: FieldInfo, precision: int) -> _Config:
+    c = _Config()
+    (c.width_nm, c.height_nm, c.h_u_nm, c.pml, c.lambda_nm, c.angle_deg, c.step_num) = fi.astuple()
+    c.precision = precision
+    return c
+
+
+def geometry_of(fi: FieldInfo) -> Geometry:
+    g = Geometry()
+    _check(load().fdtd_geometry_of(C.byref(_config(fi, F64)), C.byref(g)))
+    return g
+
+
+class Simulation:
+    """One GPU simulation of a UPML solver (see include/mpifdtd_gb300.h)."""
+
+    def __init__(self, solver, fi: FieldInfo, precision: int | str = F64):
+        self.lib = load()
+        self.solver = SOLVERS[solver] if isinstance(solver, str) else int(solver)
+        if isinstance(precision, str):
+            precision = {"f64": F64, "f32": F32}[precision]
+        self.precision = precision
+        self.fi = fi
+        h = C.c_void_p()
+        _check(self.lib.fdtd_create(self.solver, C.byref(_config(fi, precision)), C.byref(h)))
+        self.h = h
+        self.geo = Geometry()
+        _check(self.lib.fdtd_get_geometry(self.h, C.byref(self.geo)))
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fdtd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- properties
+    @property
+    def tm(self):
+        return self.solver in (TM_UPML_2D, MPI_TM_UPML_2D)
+
+    @property
+    def mpi(self):
+        return self.solver in (MPI_TM_UPML_2D, MPI_TE_UPML_2D)
+
+    @property
+    def n_px(self):
+        return self.geo.n_px
+
+    @property
+    def n_py(self):
+        return self.geo.n_py
+
+    @property
+    def array_size(self):
+        return self.geo.array_size
+
+    @property
+    def time(self) -> float:
+        t = C.c_double()
+        _check(self.lib.fdtd_get_time(self.h, C.byref(t)))
+        return t.value
+
+    @time.setter
+    def time(self, t):
+        _check(self.lib.fdtd_set_time(self.h, float(t)))
+
+    @property
+    def status(self) -> int:
+        f = C.c_uint()
+        _check(self.lib.fdtd_get_status(self.h, C.byref(f)))
+        return f.value
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.fdtd_launch_count(self.h))
+
+    # -- inputs
+    def set_eps(self, e0, e1=None, e2=None):
+        arrs = []
+        for e in (e0, e1, e2):
+            if e is None:
+                arrs.append(None)
+            else:
+                e = np.ascontiguousarray(e, dtype=np.float64)
+                if e.shape != (self.n_px, self.n_py):
+                    raise ValueError(f"eps must be ({self.n_px}, {self.n_py}), got {e.shape}")
+                arrs.append(e)
+        _check(self.lib.fdtd_set_eps(self.h, *[_dptr(a) for a in arrs]))
+
+    def fill_model(self, model: int, params=()):
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        _check(self.lib.fdtd_fill_eps_model(self.h, int(model), _dptr(p) if p.size else None, int(p.size)))
+
+    # -- stepping
+    def update(self, time: float, ray_coef: float):
+        _check(self.lib.fdtd_update(self.h, float(time), float(ray_coef)))
+
+    def run(self, n: int):
+        _check(self.lib.fdtd_run(self.h, int(n)))
+
+    def synchronize(self):
+        _check(self.lib.fdtd_synchronize(self.h))
+
+    def reset(self):
+        _check(self.lib.fdtd_reset(self.h))
+
+    # -- outputs
+    def _shape(self, layout):
+        if layout == LAYOUT_SOLVER and self.mpi:
+            return (self.n_px + 2, self.n_py + 2)
+        return (self.n_px, self.n_py)
+
+    def field(self, which: int, layout: int = LAYOUT_GLOBAL) -> np.ndarray:
+        shp = self._shape(layout)
+        out = np.empty(shp, dtype=np.complex128)
+        _check(self.lib.fdtd_get_field(self.h, int(which), int(layout),
+                                       out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def eps(self, which: int, layout: int = LAYOUT_GLOBAL) -> np.ndarray:
+        out = np.empty(self._shape(layout), dtype=np.float64)
+        _check(self.lib.fdtd_get_eps(self.h, int(which), int(layout), _dptr(out)))
+        return out
+
+    def ntff(self, which: int) -> np.ndarray:
+        out = np.empty(360 * self.array_size, dtype=np.complex128)
+        _check(self.lib.fdtd_get_ntff(self.h, int(which), out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def ntff_guard(self, which: int) -> np.ndarray:
+        g = C.c_int()
+        out = np.empty(64, dtype=np.complex128)
+        _check(self.lib.fdtd_get_ntff_guard(self.h, int(which), out.ctypes.data_as(C.POINTER(C.c_double)),
+                                            C.byref(g)))
+        return out[:2 * g.value]

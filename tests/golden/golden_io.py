@@ -15,21 +15,30 @@ def crop(a, mpi):
     return a[1:-1, 1:-1] if mpi else a
 
 
+def sketch_vector(n, salt):
+    """Fixed seeded complex vector for linear sketches.  Plain sums are useless
+    here: each three-tap NTFF deposit has weights b + (a-b) - a = 0, so the sum
+    of a row is rounding noise; a random projection is not."""
+    rng = np.random.default_rng(20261203 + 7919 * salt + n)
+    return rng.standard_normal(n) + 1j * rng.standard_normal(n)
+
+
 def capture(fields, eps, ntff, array_size, kind, rows="all"):
     out = {}
     for w, f in enumerate(fields):
         f = np.asarray(f, dtype=np.complex128)
         out[f"field{w}_rownorm"] = np.linalg.norm(f, axis=1)
-        out[f"field{w}_rowsum"] = f.sum(axis=1)
+        out[f"field{w}_rowproj"] = f @ sketch_vector(f.shape[1], 1)
         if kind == "full":
             out[f"field{w}"] = f
     if kind == "full":
         for w, e in enumerate(eps):
             out[f"eps{w}"] = np.asarray(e, dtype=np.float64)
     keep = NTFF_ROWS_FEW if rows == "few" else NTFF_ROWS
+    r = sketch_vector(array_size, 2)
     for w, u in enumerate(ntff):
         block = np.asarray(u, dtype=np.complex128).reshape(360, array_size)
-        out[f"ntff{w}_anglesum"] = block.sum(axis=1)
+        out[f"ntff{w}_angleproj"] = block @ r
         out[f"ntff{w}_anglenorm"] = np.linalg.norm(block, axis=1)
         if kind == "full":
             out[f"ntff{w}_rows"] = block[keep]
