@@ -1,0 +1,355 @@
+#!/usr/bin/env python3
+"""Benchmark of the UPML time-stepping path (one JSON line on stdout).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Workload (the configuration the HBM-fraction target is quoted on): the
+morpho-scale ridge on a 16416 x 16416 grid (16384^2 + 16-cell UPML per side),
+2 nm cells, lambda 500 nm, 0 deg, step_num 20000, MPI_TM_UPML in FP64, with the
+360-angle time-domain NTFF every step.  Ridge: 8 lamellae, 80 nm eps 2.43 /
+90 nm air, lamella widths uniform in [300, 600] nm (seeded), 50 nm trunk.
+One bench step is one update() + field_nextStep() over the whole grid.
+
+value : Gcell-updates/s with the state resident in HBM (device-timed with CUDA
+        events on the engine's stream; 32 GB of state, larger than L2, so no
+        flush is needed between steps).
+e2e   : the same metric through the C ABI with host buffers: the permittivity
+        goes host->device (fdtd_set_eps), K per-step fdtd_update() calls driven
+        by a host clock as simulator_calc() does, then Ez and the three NTFF
+        accumulators come back device->host, all inside the timed region.
+roofline : the stencil half-step pair (E + H kernels) against the measured
+        HBM copy bandwidth, with the algorithmic 200 B per FP64 TM cell-update.
+cpu_baseline / --impl reference : the oracle's C restatement of the reference
+        (oracle/fdtd_oracle.c, the reference's own loops) on every host core,
+        one independent down-scaled instance per core (the reference's own
+        task parallelism, main.c:114-138).
+With --gpus N > 1 every rank runs its own replica (the path is not sharded
+across GPUs here), value = all ranks' cell-updates / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Gcell-updates/s & %HBM peak"
+UNIT = "Gcell-updates/s"
+# FieldInfo: width_nm, height_nm, h_u_nm, pml, lambda_nm, angle_deg, step_num
+FIELD = (32832, 32832, 2, 16, 500, 0, 20000)
+SAMPLE_FIELD = (2080, 2080, 2, 16, 500, 0, 20000)     # CPU sample: 1040^2, same ridge and cell size
+B_ALG = {("tm", "f64"): 200, ("te", "f64"): 208, ("tm", "f32"): 100, ("te", "f32"): 104}
+
+
+def morpho_params(seed=20261203 + 3):
+    """morphoScaleModel parameters of the workload (per-lamella widths)."""
+    rng = np.random.default_rng(seed)
+    widths = rng.uniform(300.0, 600.0, size=8)
+    # width, thick0, thick1, layers, branch, edge_rate, eps, per_lamella, widths...
+    return [float(widths.max()), 80.0, 90.0, 8.0, 50.0, 0.0, 2.43, 1.0] + [float(w) for w in widths]
+
+
+def workload_config():
+    n = FIELD[0] // FIELD[2]
+    return {
+        "workload": f"morpho-scale ridge, MPI_TM_UPML FP64, {n}x{n} ({n - 32}^2 + 16-cell UPML), "
+                    "2 nm cells, lambda 500 nm, 360-angle time-domain NTFF every step",
+        "grid": [n, n], "cells_per_step": n * n, "h_u_nm": 2, "pml": 16,
+        "lambda_nm": 500, "angle_deg": 0, "step_num": 20000, "solver": "MPI_TM_UPML", "precision": "f64",
+        "model": {"kind": "morpho", "layers": 8, "thick_nm": [80, 90], "eps": 2.43,
+                  "widths_nm": "uniform[300,600] seeded", "branch_nm": 50},
+        "l2": "no flush: 32 GB of state per step, far larger than the 129 MB L2",
+        "step": "one update() + field_nextStep() over the whole grid",
+    }
+
+
+# ---------------------------------------------------------------- helpers
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out = ""
+
+    def summary(self):
+        rows = []
+        for line in (self.out or "").splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                rows.append((float(parts[0]), float(parts[1]), parts[4:8]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[q] for _, _, flags in rows for q, f in enumerate(flags) if f.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak_hbm():
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs, STREAM-style copy)"
+    except Exception:
+        return 6800.0, "fallback 6.8 TB/s (MEASURED_PEAKS.json absent)"
+
+
+def ncu_traffic_per_cell():
+    """DRAM bytes per cell-update of the E and H kernels from the committed ncu summary."""
+    p = ROOT / "profiles" / "ncu_traffic.json"
+    try:
+        d = json.loads(p.read_text())
+        return float(d["stencil_dram_bytes_per_cell"]), d.get("source", "")
+    except Exception:
+        return None, ""
+
+
+# ---------------------------------------------------------------- CPU arms
+
+def cpu_sample_run(steps, threads):
+    """Oracle restatement on `threads` cores, one independent instance each."""
+    from oracle.pyoracle import FieldInfo, Model, oracle_bench
+    p = morpho_params()
+    model = Model(2, p)  # MODEL_MORPHO with the same parameter vector layout
+    fi = FieldInfo(*SAMPLE_FIELD)
+    dt = oracle_bench("MPI_TM_UPML", fi, model, steps, threads)
+    if dt <= 0:
+        raise RuntimeError("oracle sample failed")
+    n = (SAMPLE_FIELD[0] // SAMPLE_FIELD[2]) * (SAMPLE_FIELD[1] // SAMPLE_FIELD[2])
+    return n * steps * threads / dt / 1e9, dt, n
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_reference_arm(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = host_threads()
+    # warm-up: W steps per instance, untimed (also builds the oracle)
+    if args.warmup > 0:
+        cpu_sample_run(max(1, min(args.warmup, 3)), threads)
+    value, dt, n = cpu_sample_run(args.steps, threads)
+    sample = (f"{threads} independent {SAMPLE_FIELD[0] // 2}x{SAMPLE_FIELD[1] // 2} instances of the same ridge "
+              f"(2 nm cells, MPI_TM_UPML FP64 with NTFF), {args.steps} steps each")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's loops restated in C (oracle/fdtd_oracle.c, bit-identical to the reference "
+                "on its golden vectors); the reference sources are not present on this host",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------- GPU arm
+
+def run_gpu_arm(args):
+    import torch
+
+    import mpifdtd_gb300 as m
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    fi = m.FieldInfo(*FIELD)
+    sim = m.Simulation("MPI_TM_UPML", fi, "f64")
+    sim.fill_model(m.MODEL_MORPHO, morpho_params())
+    cells = sim.n_px * sim.n_py
+    stream = torch.cuda.ExternalStream(sim.stream)
+
+    # warm-up
+    sim.run(args.warmup)
+    sim.synchronize()
+
+    # timed region: K steps, device-timed on the engine stream
+    launches0 = sim.launches
+    sim.profile(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clk:
+        e0.record(stream)
+        sim.run(args.steps)
+        e1.record(stream)
+        e1.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    prof = sim.profile_read()
+    sim.profile(False)
+    launches = sim.launches - launches0
+    if sim.status != 0:
+        raise RuntimeError(f"engine status {sim.status:#x}")
+    t_max = ms
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = cells * args.steps * ws / (t_max * 1e-3) / 1e9
+
+    # roofline of the stencil pair (E + H half-step kernels)
+    peak, peak_src = measured_peak_hbm()
+    stencil_ms = (prof["e_half"] + prof["h_half"]) / max(1, prof["steps"])
+    b_alg = B_ALG[("tm", "f64")]
+    achieved = cells * b_alg / (stencil_ms * 1e-3) / 1e9
+    tr_cell, tr_src = ncu_traffic_per_cell()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": (tr_cell * cells if tr_cell else None),
+                "kernel": "stencil half-step pair (tm_e_kernel + tm_h_kernel), per step",
+                "bytes_per_cell_alg": b_alg, "peak_source": peak_src,
+                "traffic_source": tr_src or "no committed ncu summary",
+                "ms_per_launch": {"e_half": prof["e_half"] / prof["steps"], "h_half": prof["h_half"] / prof["steps"],
+                                  "ntff_gather": prof["ntff_gather"] / prof["steps"],
+                                  "ntff_deposit": prof["ntff_deposit"] / prof["steps"]}}
+
+    # e2e through the C ABI with host buffers
+    e2e = None if args.no_e2e else run_e2e(m, sim, args, torch)
+    sim.close()
+
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            threads = host_threads()
+            steps = 6
+            v, dt, n = cpu_sample_run(steps, threads)
+            cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": f"{threads} independent {SAMPLE_FIELD[0] // 2}x{SAMPLE_FIELD[1] // 2} instances of "
+                             f"the same ridge (2 nm cells, MPI_TM_UPML FP64 with NTFF), {steps} steps each, "
+                             f"{dt:.1f} s"}
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "clocks": clk.summary(), "gpu_launches": launches,
+            "hbm_frac": roofline["frac"],
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def run_e2e(m, sim, args, torch):
+    """K steps through the C ABI with host buffers, copies inside the timed region."""
+    n_px, n_py = sim.n_px, sim.n_py
+    n = n_px * n_py
+    eps_h = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    sim.eps_into(0, eps_h.data_ptr())                     # the workload's EPS_EZ on the host
+    ez_h = torch.empty(2 * n, dtype=torch.float64, pin_memory=True)
+    nt_len = 360 * sim.array_size
+    nt_h = [torch.empty(2 * nt_len, dtype=torch.float64, pin_memory=True) for _ in range(3)]
+    sim.reset()
+    sim.synchronize()
+    t = time.perf_counter()
+    sim.set_eps_ptr(eps_h.data_ptr())                      # H2D
+    clock, ray = 0.0, 0.0
+    for _ in range(args.steps):                            # simulator_calc(): update() then field_nextStep()
+        sim.update(clock, ray)
+        clock += 1.0
+        ray = 1.0 - float(np.exp(-(0.01 * clock) ** 2))
+    sim.field_into(0, ez_h.data_ptr())                     # D2H (synchronizes)
+    for w in range(3):
+        sim.ntff_into(w, nt_h[w].data_ptr())
+    dt = time.perf_counter() - t
+    h2d = n * 8
+    d2h = n * 16 + 3 * nt_len * 16
+    return {"value": n * args.steps / dt / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
+            "d2h_bytes_per_step": d2h / args.steps, "seconds": dt,
+            "path": "fdtd_set_eps (pinned host) + fdtd_update x K + fdtd_get_field/fdtd_get_ntff (pinned host)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--grid", type=int, default=0,
+                    help="interior cells per side for a smaller case of the same workload (profiling)")
+    args = ap.parse_args()
+    if args.grid:
+        global FIELD
+        side = (args.grid + 2 * FIELD[3]) * FIELD[2]
+        FIELD = (side, side) + FIELD[2:]
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.warmup + args.steps > FIELD[6]:
+        raise SystemExit("steps + warmup must not exceed step_num (20000)")
+    if args.impl == "reference":
+        return run_reference_arm(args)
+    return run_gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -124,6 +124,9 @@ int fdtd_get_ntff_guard(fdtd_sim *sim, int which, double *out_complex, int *guar
  * engine clock returns to 0. */
 int fdtd_reset(fdtd_sim *sim);
 
+/* The CUDA stream (cudaStream_t) every launch of this simulation is issued on. */
+int fdtd_get_stream(fdtd_sim *sim, void **stream);
+
 /* Device pointers of the state for zero-copy consumers (pitch in elements). */
 int fdtd_device_field(fdtd_sim *sim, int which, void **dptr, int *pitch, int *rows);
 
@@ -131,6 +134,19 @@ int fdtd_device_field(fdtd_sim *sim, int which, void **dptr, int *pitch, int *ro
  * and was dropped (cannot happen within [0, step_num) on valid geometry). */
 #define FDTD_STATUS_NTFF_RANGE 1u
 int fdtd_get_status(fdtd_sim *sim, unsigned int *flags);
+
+/* Tuning knobs (results are the same up to summation order). */
+#define FDTD_OPT_NTFF_MODE 1     /* 0 direct global atomics, 1 shared-memory window (default) */
+#define FDTD_OPT_NTFF_CHUNK 2    /* cells of a side per window block (64..4096, default 1024) */
+int fdtd_set_option(fdtd_sim *sim, int key, int value);
+int fdtd_get_option(fdtd_sim *sim, int key, int *value);
+
+/* Per-kernel timing with CUDA events recorded on the engine's own stream
+ * around every launch class while enabled.  ms_out[4] receives the summed
+ * milliseconds of: 0 E half-step, 1 H half-step, 2 NTFF gather, 3 NTFF deposit;
+ * *steps the number of steps timed.  Reading synchronizes and clears. */
+int fdtd_profile_enable(fdtd_sim *sim, int on);
+int fdtd_profile_read(fdtd_sim *sim, double *ms_out, long long *steps);
 
 /* Number of kernel launches the engine issued since creation. */
 long long fdtd_launch_count(const fdtd_sim *sim);

@@ -34,7 +34,11 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp
                      f"-I{INCLUDE}"]
 CC_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-Wall", f"-I{INCLUDE}"]
 
-ENGINE_SOURCES = ["fdtd_kernels.cu", "fdtd_api.cu"]
+ENGINE_SOURCES = ["fdtd_kernels.cu", "fdtd_api.cu", "fdtd_setup.cu"]
+# The model evaluators classify sub-cell samples with comparisons such as
+# px*px + py*py <= r*r (circleModel.c:45-57); a fused multiply-add could flip a
+# sample on the boundary, so that file is compiled without contraction.
+PER_FILE_FLAGS = {"fdtd_setup.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:
@@ -73,7 +77,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         o = BUILD / (s.stem + ".o")
         objs.append(o)
         if force or _stale(o, [s] + hdrs):
-            jobs.append([nvcc()] + NVCC_FLAGS + ["-c", s, "-o", o])
+            jobs.append([nvcc()] + NVCC_FLAGS + PER_FILE_FLAGS.get(src, []) + ["-c", s, "-o", o])
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         list(ex.map(lambda c: _run(c, verbose), jobs))
     if force or jobs or _stale(ENGINE_SO, objs):

@@ -254,6 +254,9 @@ static int build_ntff(fdtd_sim *s)
   CK(cudaMemcpy(s->d_cells, cells.data(), sizeof(SurfCell) * n, cudaMemcpyHostToDevice));
   CK(cudaMalloc(&s->d_shift, sizeof(double) * shift.size()));
   CK(cudaMemcpy(s->d_shift, shift.data(), sizeof(double) * shift.size(), cudaMemcpyHostToDevice));
+  s->h_shift.swap(shift);
+  s->h_side.swap(side);
+  s->window_dirty = true;
   CK(cudaMalloc(&s->d_vals, sizeof(double2) * 2 * n));
   s->ntff_len = (size_t)360 * g.array_size + 2 * kGuard;
   for (int a = 0; a < 3; a++) {
@@ -270,6 +273,7 @@ static void free_sim(fdtd_sim *s)
   if (!s) return;
   for (int a = 0; a < kMaxSlots; a++) cudaFree(s->d_f[a]);
   for (int a = 0; a < 2; a++) { cudaFree(s->d_ieps64[a]); cudaFree(s->d_ieps32[a]); }
+  for (int a = 0; a < 3; a++) cudaFree(s->d_eps[a]);
   for (int a = 0; a < 4; a++) { cudaFree(s->d_tab64[a]); cudaFree(s->d_tab32[a]); }
   cudaFree(s->d_ex);
   cudaFree(s->d_ey);
@@ -278,6 +282,9 @@ static void free_sim(fdtd_sim *s)
   cudaFree(s->d_vals);
   for (int a = 0; a < 3; a++) cudaFree(s->d_ntff[a]);
   cudaFree(s->d_status);
+  cudaFree(s->d_chunk);
+  cudaFree(s->d_lo);
+  for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
 }
@@ -342,8 +349,14 @@ extern "C" int fdtd_create(int solver, const fdtd_config *cfg, fdtd_sim **out)
       return fail(FDTD_E_NOMEM, "cudaMalloc of permittivity failed");
     }
   }
-  s->host_eps.assign(3, std::vector<double>((size_t)geo.n_px * geo.n_py, 1.0));
-  if ((rc = build_tables(s)) || (rc = build_ntff(s)) || (rc = fdtd_set_eps(s, nullptr, nullptr, nullptr))) {
+  for (int a = 0; a < 3; a++) {
+    if (cudaMalloc(&s->d_eps[a], ecount * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      free_sim(s);
+      return fail(FDTD_E_NOMEM, "cudaMalloc of permittivity failed");
+    }
+  }
+  if ((rc = build_tables(s)) || (rc = build_ntff(s)) || (rc = fdtd_fill_eps_model(s, FDTD_MODEL_NONE, nullptr, 0))) {
     std::string msg = g_err;
     free_sim(s);
     g_err = msg;
@@ -371,49 +384,137 @@ extern "C" int fdtd_get_geometry(const fdtd_sim *s, fdtd_geometry *out)
 
 // ---------------------------------------------------------------- permittivity
 
-// Map the global-frame permittivity of the E components into the padded
-// device arrays as 1/eps (halo and unused cells 1.0).
-int upload_inv_eps(fdtd_sim *s)
+// Permittivity lives on the device in the padded array frame (d_eps, halo
+// cells 1.0).  The E components' 1/eps (FP64 and FP32 copies) are derived
+// from it on the device; a non-finite or non-positive value sets
+// kStatusBadEps and makes the call fail.
+static int derive_inv_eps(fdtd_sim *s)
 {
-  const fdtd_geometry &g = s->geo;
-  const int neps = s->tm ? 1 : 2;
   const size_t count = (size_t)s->nxa * s->pitch;
-  std::vector<double> h64(count);
-  std::vector<float> h32(count);
-  for (int a = 0; a < neps; a++) {
-    const std::vector<double> &src = s->host_eps[a];
-    std::fill(h64.begin(), h64.end(), 1.0);
-    for (int i = 0; i < s->nxa; i++) {
-      const int x = i + s->ox;
-      if (x < 0 || x >= g.n_px) continue;
-      for (int j = 0; j < s->ncols; j++) {
-        const int y = j + s->ox;
-        if (y < 0 || y >= g.n_py) continue;
-        h64[(size_t)i * s->pitch + j] = kEps0 / src[(size_t)x * g.n_py + y];
-      }
-    }
-    for (size_t q = 0; q < count; q++) h32[q] = (float)h64[q];
-    CK(cudaMemcpyAsync(s->d_ieps64[a], h64.data(), count * sizeof(double), cudaMemcpyHostToDevice, s->stream));
-    CK(cudaMemcpyAsync(s->d_ieps32[a], h32.data(), count * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-    CK(cudaStreamSynchronize(s->stream));
-  }
+  const int neps = s->tm ? 1 : 2;
+  CK(cudaMemsetAsync(s->d_status, 0, sizeof(unsigned int), s->stream));
+  for (int a = 0; a < neps; a++)
+    launch_inv_eps((const double *)s->d_eps[a], (double *)s->d_ieps64[a], (float *)s->d_ieps32[a], count,
+                   s->d_status, s->stream);
+  CK(cudaGetLastError());
+  unsigned int st = 0;
+  CK(cudaMemcpyAsync(&st, s->d_status, sizeof st, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  s->launches += neps;
+  if (st & kStatusBadEps) return fail(FDTD_E_ARG, "permittivity must be finite and > 0 everywhere");
   return FDTD_OK;
 }
+
+// array offset of global cell (0,0): MPI arrays carry a one-cell halo
+static size_t global_origin(const fdtd_sim *s) { return s->mpi ? (size_t)s->pitch + 1 : 0; }
 
 extern "C" int fdtd_set_eps(fdtd_sim *s, const double *e0, const double *e1, const double *e2)
 {
   if (!s) return fail(FDTD_E_ARG, "null simulation");
-  const size_t n = (size_t)s->geo.n_px * s->geo.n_py;
+  if (!e0) return fail(FDTD_E_ARG, "the E-component permittivity e0 is required");
+  if (!s->tm && !e1) return fail(FDTD_E_ARG, "TE needs e1 (EPS_EY) as well");
   const double *src[3] = {e0, e1, e2};
+  const int n_px = s->geo.n_px, n_py = s->geo.n_py;
   for (int a = 0; a < 3; a++) {
-    if (src[a]) {
-      for (size_t q = 0; q < n; q++)
-        if (!(src[a][q] > 0) || !std::isfinite(src[a][q]))
-          return fail(FDTD_E_ARG, "permittivity %d at cell %zu is %g (must be finite and > 0)", a, q, src[a][q]);
-      std::memcpy(s->host_eps[a].data(), src[a], n * sizeof(double));
+    if (!src[a]) continue;
+    double *dst = (double *)s->d_eps[a] + global_origin(s);
+    CK(cudaMemcpy2DAsync(dst, (size_t)s->pitch * sizeof(double), src[a], (size_t)n_py * sizeof(double),
+                         (size_t)n_py * sizeof(double), n_px, cudaMemcpyHostToDevice, s->stream));
+  }
+  return derive_inv_eps(s);
+}
+
+extern "C" int fdtd_fill_eps_model(fdtd_sim *s, int model, const double *params, int n_params)
+{
+  if (!s) return fail(FDTD_E_ARG, "null simulation");
+  if (n_params < 0 || (n_params > 0 && !params)) return fail(FDTD_E_ARG, "bad parameter vector");
+  mdl_params m{};
+  if (model != FDTD_MODEL_NONE && model != FDTD_MODEL_CIRCLE && model != FDTD_MODEL_MORPHO)
+    return fail(FDTD_E_UNSUPPORTED, "model %d is not built in (circle 1, morpho 3, none 0)", model);
+  if (mdl_init(&m, model, params, n_params, s->geo.n_px, s->geo.n_py, s->geo.n_pml, s->cfg.h_u_nm) != 0)
+    return fail(FDTD_E_ARG, "bad parameters for model %d (see mpifdtd_gb300.h)", model);
+  launch_eps_model((double *)s->d_eps[0], (double *)s->d_eps[1], (double *)s->d_eps[2], s->pitch, s->nxa,
+                   s->ncols, s->ox, s->geo.n_px, s->geo.n_py, s->tm, s->mpi, m, s->stream);
+  s->launches += 1;
+  CK(cudaGetLastError());
+  return derive_inv_eps(s);
+}
+
+// ---------------------------------------------------------------- NTFF windows
+
+// Chunks of at most ntff_chunk consecutive cells of one side, and per
+// (angle, chunk) the bin offsets of the E and H windows:
+//   E bins m = floor(timeE + sh + 0.5) lie in floor(timeE) + [floor(sh_min+.5)-1, floor(sh_max+.5)+1]
+//   H bins (timeH = timeE + 1/2) in floor(timeE) + [floor(sh_min+1)-1, floor(sh_max+1)+1]
+// the taps add one bin each side; one more bin of margin on each end.
+static int build_windows(fdtd_sim *s)
+{
+  const int n = s->ncell, ch = s->ntff_chunk;
+  std::vector<int2> chunks;
+  for (int c = 0; c < n;) {
+    int e = c;
+    while (e < n && s->h_side[e] == s->h_side[c] && e - c < ch) e++;
+    chunks.push_back(make_int2(c, e - c));
+    c = e;
+  }
+  const int nch = (int)chunks.size();
+  std::vector<int2> lo((size_t)360 * nch);
+  int width = 0;
+  for (int ang = 0; ang < 360; ang++) {
+    const double *row = &s->h_shift[(size_t)ang * n];
+    for (int q = 0; q < nch; q++) {
+      double mn = row[chunks[q].x], mx = mn;
+      for (int c = chunks[q].x; c < chunks[q].x + chunks[q].y; c++) {
+        mn = std::min(mn, row[c]);
+        mx = std::max(mx, row[c]);
+      }
+      const int loe = (int)std::floor(mn + 0.5) - 3, loh = (int)std::floor(mn + 1.0) - 3;
+      const int we = (int)std::floor(mx + 0.5) - loe + 4, wh = (int)std::floor(mx + 1.0) - loh + 4;
+      lo[(size_t)ang * nch + q] = make_int2(loe, loh);
+      width = std::max(width, std::max(we, wh));
     }
   }
-  return upload_inv_eps(s);
+  if ((size_t)width * 2 * sizeof(double2) > 200 * 1024)
+    return fail(FDTD_E_ARG, "NTFF window of %d bins exceeds shared memory; lower FDTD_OPT_NTFF_CHUNK", width);
+  cudaFree(s->d_chunk);
+  cudaFree(s->d_lo);
+  s->d_chunk = s->d_lo = nullptr;
+  CK(cudaMalloc(&s->d_chunk, sizeof(int2) * chunks.size()));
+  CK(cudaMemcpy(s->d_chunk, chunks.data(), sizeof(int2) * chunks.size(), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&s->d_lo, sizeof(int2) * lo.size()));
+  CK(cudaMemcpy(s->d_lo, lo.data(), sizeof(int2) * lo.size(), cudaMemcpyHostToDevice));
+  s->nchunk = nch;
+  s->win_width = width;
+  s->window_dirty = false;
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_set_option(fdtd_sim *s, int key, int value)
+{
+  if (!s) return fail(FDTD_E_ARG, "null simulation");
+  switch (key) {
+  case FDTD_OPT_NTFF_MODE:
+    if (value != 0 && value != 1) return fail(FDTD_E_ARG, "NTFF mode must be 0 or 1");
+    s->ntff_mode = value;
+    return FDTD_OK;
+  case FDTD_OPT_NTFF_CHUNK:
+    if (value < 64 || value > 4096) return fail(FDTD_E_ARG, "NTFF chunk must be in [64, 4096]");
+    CK(cudaStreamSynchronize(s->stream));
+    s->ntff_chunk = value;
+    s->window_dirty = true;
+    return FDTD_OK;
+  }
+  return fail(FDTD_E_ARG, "unknown option %d", key);
+}
+
+extern "C" int fdtd_get_option(fdtd_sim *s, int key, int *value)
+{
+  if (!s || !value) return fail(FDTD_E_ARG, "null argument");
+  switch (key) {
+  case FDTD_OPT_NTFF_MODE: *value = s->ntff_mode; return FDTD_OK;
+  case FDTD_OPT_NTFF_CHUNK: *value = s->ntff_chunk; return FDTD_OK;
+  }
+  return fail(FDTD_E_ARG, "unknown option %d", key);
 }
 
 // ---------------------------------------------------------------- stepping
@@ -478,6 +579,22 @@ static SourceStep pulse_step(const fdtd_sim *s, double time, double gap_x, doubl
   return p;
 }
 
+// Records the next profiling event of the step (5 per step) when enabled.
+static void mark(fdtd_sim *s)
+{
+  if (!s->profiling) return;
+  if (s->ev_used == s->ev_pool.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      cudaGetLastError();
+      s->profiling = false;
+      return;
+    }
+    s->ev_pool.push_back(e);
+  }
+  cudaEventRecord(s->ev_pool[s->ev_used++], s->stream);
+}
+
 template <typename R>
 static void enqueue_step(fdtd_sim *s, double time, double ray_coef)
 {
@@ -485,6 +602,7 @@ static void enqueue_step(fdtd_sim *s, double time, double ray_coef)
   const NtffView n = ntff_view(s);
   cudaStream_t st = s->stream;
   const double coef = s->mpi ? 1.0 / (4 * M_PI * kC * 1.0e6) : 1.0;  // mpiTM_UPML.c:852-854
+  mark(s);
   if (s->mpi) {
     SourceStep cw{};
     cw.kind = 1;
@@ -493,17 +611,21 @@ static void enqueue_step(fdtd_sim *s, double time, double ray_coef)
     cw.s_im = -ray_coef * sin(wt);
     if (s->tm) {
       launch_tm_e<R>(v, cw, st);
+      mark(s);
       launch_tm_h<R>(v, st);
     } else {
       SourceStep none{};
       launch_te_e<R>(v, none, cw, st);
+      mark(s);
       launch_te_h<R>(v, st);
     }
   } else if (s->tm) {  // fdtdTM_upml.c:54-66
     launch_tm_h<R>(v, st);
+    mark(s);
     launch_tm_e<R>(v, pulse_step(s, time, 0, 0, 1.0), st);
   } else {             // fdtdTE_upml.c:168-192
     launch_te_h<R>(v, st);
+    mark(s);
     const double co = cos((s->cfg.angle_deg + 90) * M_PI / 180.0);
     const double si = sin((s->cfg.angle_deg + 90) * M_PI / 180.0);
     SourceStep sx{}, sy{};
@@ -511,9 +633,55 @@ static void enqueue_step(fdtd_sim *s, double time, double ray_coef)
     if (si != 0.0) sy = pulse_step(s, time, 0.0, 0.5, si);
     launch_te_e<R>(v, sx, sy, st);
   }
+  mark(s);
   launch_ntff_gather<R>(v, n, coef, st);
-  launch_ntff_accumulate(n, time - 1, time - 0.5, st);
+  mark(s);
+  if (s->ntff_mode == 1) {
+    NtffWindow w{(const int2 *)s->d_chunk, (const int2 *)s->d_lo, s->nchunk, s->win_width};
+    launch_ntff_window(n, w, time - 1, time - 0.5, st);
+  } else {
+    launch_ntff_accumulate(n, time - 1, time - 0.5, st);
+  }
+  mark(s);
+  if (s->profiling) s->prof_steps++;
   s->launches += 4;
+}
+
+extern "C" int fdtd_profile_enable(fdtd_sim *s, int on)
+{
+  if (!s) return fail(FDTD_E_ARG, "null simulation");
+  CK(cudaStreamSynchronize(s->stream));
+  s->profiling = on != 0;
+  s->ev_used = 0;
+  s->prof_steps = 0;
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_profile_read(fdtd_sim *s, double *ms_out, long long *steps)
+{
+  if (!s || !ms_out) return fail(FDTD_E_ARG, "null argument");
+  CK(cudaStreamSynchronize(s->stream));
+  double acc[4] = {0, 0, 0, 0};
+  // event order per step: start, after 1st stencil, after 2nd stencil, after gather, after deposit
+  const int first = s->mpi ? 0 : 1, second = s->mpi ? 1 : 0;
+  const int cls[4] = {first, second, 2, 3};
+  for (size_t q = 0; q + 5 <= s->ev_used; q += 5)
+    for (int c = 0; c < 4; c++) {
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, s->ev_pool[q + c], s->ev_pool[q + c + 1]));
+      acc[cls[c]] += ms;
+    }
+  for (int c = 0; c < 4; c++) ms_out[c] = acc[c];
+  if (steps) *steps = s->prof_steps;
+  s->ev_used = 0;
+  s->prof_steps = 0;
+  return FDTD_OK;
+}
+
+static int prepare_step(fdtd_sim *s)
+{
+  if (s->ntff_mode == 1 && s->window_dirty) return build_windows(s);
+  return FDTD_OK;
 }
 
 // The reference steps only while time < maxTime (field.c:317-319); past it
@@ -529,6 +697,7 @@ extern "C" int fdtd_update(fdtd_sim *s, double time, double ray_coef)
 {
   if (!s) return fail(FDTD_E_ARG, "null simulation");
   if (int rc = check_clock(s, time)) return rc;
+  if (int rc = prepare_step(s)) return rc;
   if (s->f32) enqueue_step<float>(s, time, ray_coef);
   else enqueue_step<double>(s, time, ray_coef);
   CK(cudaGetLastError());
@@ -541,6 +710,7 @@ extern "C" int fdtd_run(fdtd_sim *s, int n_steps)
   if (n_steps < 0) return fail(FDTD_E_ARG, "n_steps < 0");
   if (n_steps > 0)
     if (int rc = check_clock(s, s->time + (n_steps - 1))) return rc;
+  if (int rc = prepare_step(s)) return rc;
   for (int q = 0; q < n_steps; q++) {
     const double t = s->time;
     const double rc = s->ray_coef;
@@ -622,16 +792,14 @@ extern "C" int fdtd_get_eps(fdtd_sim *s, int which, int layout, double *out)
 {
   if (!s || !out) return fail(FDTD_E_ARG, "null argument");
   if (which < 0 || which > 2) return fail(FDTD_E_ARG, "eps index %d out of range", which);
-  const fdtd_geometry &g = s->geo;
-  const std::vector<double> &e = s->host_eps[which];
-  if (layout == FDTD_LAYOUT_GLOBAL || !s->mpi) {
-    std::memcpy(out, e.data(), e.size() * sizeof(double));
-    return FDTD_OK;
-  }
-  const int ny = g.n_py + 2;
-  std::memset(out, 0, sizeof(double) * (size_t)(g.n_px + 2) * ny);
-  for (int x = 0; x < g.n_px; x++)
-    std::memcpy(out + (size_t)(x + 1) * ny + 1, &e[(size_t)x * g.n_py], sizeof(double) * g.n_py);
+  if (layout != FDTD_LAYOUT_GLOBAL && layout != FDTD_LAYOUT_SOLVER) return fail(FDTD_E_ARG, "bad layout");
+  // SOLVER layout of an MPI solver includes the halo ring (1.0 there)
+  const bool halo = s->mpi && layout == FDTD_LAYOUT_SOLVER;
+  const int nr = halo ? s->nxa : s->geo.n_px, nc = halo ? s->ncols : s->geo.n_py;
+  const double *src = (const double *)s->d_eps[which] + (halo ? 0 : global_origin(s));
+  CK(cudaStreamSynchronize(s->stream));
+  CK(cudaMemcpy2D(out, (size_t)nc * sizeof(double), src, (size_t)s->pitch * sizeof(double),
+                  (size_t)nc * sizeof(double), nr, cudaMemcpyDeviceToHost));
   return FDTD_OK;
 }
 
@@ -671,6 +839,13 @@ extern "C" int fdtd_reset(fdtd_sim *s)
   return FDTD_OK;
 }
 
+extern "C" int fdtd_get_stream(fdtd_sim *s, void **stream)
+{
+  if (!s || !stream) return fail(FDTD_E_ARG, "null argument");
+  *stream = (void *)s->stream;
+  return FDTD_OK;
+}
+
 extern "C" int fdtd_device_field(fdtd_sim *s, int which, void **dptr, int *pitch, int *rows)
 {
   if (!s || !dptr) return fail(FDTD_E_ARG, "null argument");
@@ -680,16 +855,4 @@ extern "C" int fdtd_device_field(fdtd_sim *s, int which, void **dptr, int *pitch
   if (pitch) *pitch = s->pitch;
   if (rows) *rows = s->nxa;
   return FDTD_OK;
-}
-
-extern "C" int fdtd_fill_eps_model(fdtd_sim *s, int model, const double *params, int n_params)
-{
-  (void)params;
-  (void)n_params;
-  if (!s) return fail(FDTD_E_ARG, "null simulation");
-  if (model == FDTD_MODEL_NONE) {
-    for (auto &e : s->host_eps) std::fill(e.begin(), e.end(), 1.0);
-    return upload_inv_eps(s);
-  }
-  return fail(FDTD_E_UNSUPPORTED, "model %d is not built into this engine yet", model);
 }

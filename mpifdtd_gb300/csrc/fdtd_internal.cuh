@@ -81,8 +81,19 @@ struct NtffView {
   unsigned int *status;   // device status word (kStatus* bits)
 };
 
+// Shared-memory window variant of the NTFF deposit.  The path is cut into
+// chunks (consecutive cells of one side); along a side the retarded-time
+// shift is linear in the cell index, so the bins one chunk touches in one step
+// form a short contiguous range [base, base+W) with base = floor(timeE) + lo.
+struct NtffWindow {
+  const int2 *chunk;      // [nchunk] (first cell, cell count)
+  const int2 *lo;         // [360][nchunk] (lo_e, lo_h) bin offsets
+  int nchunk, width;      // width W of both windows (bins)
+};
+
 // Device status bits (fdtd_get_status).
 constexpr unsigned int kStatusNtffRange = 1u;   // a deposit fell outside the accumulator
+constexpr unsigned int kStatusBadEps = 2u;      // a permittivity value was not finite and > 0
 
 // Launchers (fdtd_kernels.cu).  All take the stream they run on.
 template <typename R>
@@ -96,5 +107,19 @@ void launch_te_h(const StencilView<R> &v, cudaStream_t st);
 template <typename R>
 void launch_ntff_gather(const StencilView<R> &v, const NtffView &n, double coef, cudaStream_t st);
 void launch_ntff_accumulate(const NtffView &n, double timeE, double timeH, cudaStream_t st);
+void launch_ntff_window(const NtffView &n, const NtffWindow &w, double timeE, double timeH, cudaStream_t st);
+
+}  // namespace fdtd
+
+#include "models_eval.h"
+
+namespace fdtd {
+
+// fdtd_setup.cu
+void launch_eps_model(double *e0, double *e1, double *e2, int P, int nxa, int ncols, int ox, int n_px, int n_py,
+                      bool tm, bool mpi, const mdl_params &m, cudaStream_t st);
+void launch_inv_eps(const double *eps, double *ie64, float *ie32, size_t count, unsigned int *status,
+                    cudaStream_t st);
+void launch_fill(double *p, double v, size_t count, cudaStream_t st);
 
 }  // namespace fdtd

@@ -302,6 +302,88 @@ __global__ void __launch_bounds__(256) ntff_accumulate_kernel(NtffView n, double
   deposit(n, n.acc[uw >> 4], row, timeH + sh, n.vals[n.ncell + c]);
 }
 
+// Three-tap deposit into a shared-memory window [base, base+W) of bins, with
+// v b written as v - p and v (a-b) as 2p - v (p = v a): the same taps as
+// deposit() up to one rounding.  Taps outside the window go to global memory.
+__device__ __forceinline__ void window_deposit(const NtffView &n, double2 *win, int W, double2 *acc,
+                                               long long row, long long base, double t, double2 v)
+{
+  const double u = t + 0.5;
+  const double mf = floor(u);
+  if (!(mf > -1e15 && mf < 1e15)) {
+    atomicOr(n.status, kStatusNtffRange);
+    return;
+  }
+  const double a = u - mf;
+  const long long rel = (long long)mf - base;
+  const double px = v.x * a, py = v.y * a;
+  const double t0x = v.x - px, t0y = v.y - py;            // v b
+  const double t1x = 2.0 * px - v.x, t1y = 2.0 * py - v.y;  // v (a - b)
+  if (rel >= 1 && rel + 1 < W) {
+    double2 *p = win + rel;
+    atomicAdd(&p[-1].x, t0x);
+    atomicAdd(&p[-1].y, t0y);
+    atomicAdd(&p[0].x, t1x);
+    atomicAdd(&p[0].y, t1y);
+    atomicAdd(&p[1].x, -px);
+    atomicAdd(&p[1].y, -py);
+    return;
+  }
+  const long long at = row + (long long)mf;
+  if (at - 1 < 0 || at + 1 >= n.len) {
+    atomicOr(n.status, kStatusNtffRange);
+    return;
+  }
+  double2 *p = acc + at;
+  atomicAdd(&p[-1].x, t0x);
+  atomicAdd(&p[-1].y, t0y);
+  atomicAdd(&p[0].x, t1x);
+  atomicAdd(&p[0].y, t1y);
+  atomicAdd(&p[1].x, -px);
+  atomicAdd(&p[1].y, -py);
+}
+
+__device__ __forceinline__ void window_flush(const NtffView &n, double2 *acc, long long at, double2 v)
+{
+  if (v.x == 0.0 && v.y == 0.0) return;
+  if (at < 0 || at >= n.len) {
+    atomicOr(n.status, kStatusNtffRange);
+    return;
+  }
+  atomicAdd(&acc[at].x, v.x);
+  atomicAdd(&acc[at].y, v.y);
+}
+
+// One block per (chunk of a side, angle): deposit into shared memory, then
+// add the window to the flat [360][arraySize] accumulators.
+__global__ void __launch_bounds__(256) ntff_window_kernel(NtffView n, NtffWindow w, double timeE, double timeH)
+{
+  extern __shared__ double2 win[];
+  double2 *winE = win, *winH = win + w.width;
+  const int ch = blockIdx.x, ang = blockIdx.y;
+  const int2 cr = w.chunk[ch];
+  const int2 lo = w.lo[(size_t)ang * w.nchunk + ch];
+  const long long t0 = (long long)floor(timeE);
+  const long long row = (long long)kGuard + (long long)ang * n.array_size;
+  const long long baseE = t0 + lo.x, baseH = t0 + lo.y;
+  for (int r = threadIdx.x; r < 2 * w.width; r += blockDim.x) win[r] = make_double2(0.0, 0.0);
+  __syncthreads();
+  const unsigned char uw = (unsigned char)n.cells[cr.x].uid_wid;  // one side per chunk
+  double2 *U = n.acc[uw & 15], *Wa = n.acc[uw >> 4];
+  const double *sh = n.shift + (size_t)ang * n.ncell;
+  for (int q = threadIdx.x; q < cr.y; q += blockDim.x) {
+    const int c = cr.x + q;
+    const double s = sh[c];
+    window_deposit(n, winE, w.width, U, row, baseE, timeE + s, n.vals[c]);
+    window_deposit(n, winH, w.width, Wa, row, baseH, timeH + s, n.vals[n.ncell + c]);
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < w.width; r += blockDim.x) {
+    window_flush(n, U, row + baseE + r, winE[r]);
+    window_flush(n, Wa, row + baseH + r, winH[r]);
+  }
+}
+
 // ------------------------------------------------------------------ launchers
 
 template <typename R>
@@ -341,6 +423,17 @@ void launch_ntff_accumulate(const NtffView &n, double timeE, double timeH, cudaS
 {
   dim3 g((unsigned)((n.ncell + 255) / 256), 360);
   ntff_accumulate_kernel<<<g, 256, 0, st>>>(n, timeE, timeH);
+}
+void launch_ntff_window(const NtffView &n, const NtffWindow &w, double timeE, double timeH, cudaStream_t st)
+{
+  const size_t smem = sizeof(double2) * 2 * (size_t)w.width;
+  static size_t configured = 0;  // raise the dynamic shared-memory cap once per size
+  if (smem > 48 * 1024 && smem > configured) {
+    cudaFuncSetAttribute(ntff_window_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    configured = smem;
+  }
+  dim3 g((unsigned)w.nchunk, 360);
+  ntff_window_kernel<<<g, 256, smem, st>>>(n, w, timeE, timeH);
 }
 
 #define INST(R)                                                                                    \

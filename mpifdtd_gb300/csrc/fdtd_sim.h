@@ -29,11 +29,21 @@ struct fdtd_sim {
   unsigned int *d_status = nullptr;
   int ncell = 0;
   size_t ntff_len = 0;
-  // permittivity as given (global frame), for fdtd_get_eps
-  std::vector<std::vector<double>> host_eps;
+  std::vector<double> h_shift;   // [360][ncell], kept to rebuild the window tables
+  std::vector<int> h_side;       // side of each path cell (0 bottom, 1 right, 2 top, 3 left)
+  // shared-memory window variant (FDTD_OPT_NTFF_MODE 1)
+  int ntff_mode = 1, ntff_chunk = 1024;
+  void *d_chunk = nullptr, *d_lo = nullptr;
+  int nchunk = 0, win_width = 0;
+  bool window_dirty = true;
+  void *d_eps[3] = {};            // permittivity as given, padded array frame (fdtd_get_eps)
   // engine clock (field.c:21-22 time, ray_coef)
   double time = 0, ray_coef = 0;
   long long launches = 0;
+  // per-kernel event timing (fdtd_profile_*): 5 events per step
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  long long prof_steps = 0;
 };
 
-int upload_inv_eps(fdtd_sim *s);

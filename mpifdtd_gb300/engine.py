@@ -21,6 +21,7 @@ SOLVERS = {"TM_UPML": TM_UPML_2D, "TE_UPML": TE_UPML_2D,
 F64, F32 = 0, 1
 LAYOUT_GLOBAL, LAYOUT_SOLVER = 0, 1
 MODEL_NONE, MODEL_CIRCLE, MODEL_MORPHO = 0, 1, 3
+OPT_NTFF_MODE, OPT_NTFF_CHUNK = 1, 2
 
 _ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "bad state", 5: "unsupported"}
 
@@ -97,6 +98,11 @@ def load():
         "fdtd_device_field": (I, [P, I, C.POINTER(P), C.POINTER(I), C.POINTER(I)]),
         "fdtd_launch_count": (C.c_longlong, [P]),
         "fdtd_get_status": (I, [P, C.POINTER(C.c_uint)]),
+        "fdtd_get_stream": (I, [P, C.POINTER(P)]),
+        "fdtd_profile_enable": (I, [P, I]),
+        "fdtd_profile_read": (I, [P, dp, C.POINTER(C.c_longlong)]),
+        "fdtd_set_option": (I, [P, I, I]),
+        "fdtd_get_option": (I, [P, I, C.POINTER(I)]),
         "fdtd_last_error": (C.c_char_p, []),
         "fdtd_version": (C.c_char_p, []),
     }
@@ -217,6 +223,50 @@ class Simulation:
                     raise ValueError(f"eps must be ({self.n_px}, {self.n_py}), got {e.shape}")
                 arrs.append(e)
         _check(self.lib.fdtd_set_eps(self.h, *[_dptr(a) for a in arrs]))
+
+    @property
+    def stream(self) -> int:
+        """cudaStream_t of this simulation (every launch goes there)."""
+        p = C.c_void_p()
+        _check(self.lib.fdtd_get_stream(self.h, C.byref(p)))
+        return int(p.value or 0)
+
+    def set_eps_ptr(self, e0: int, e1: int = 0, e2: int = 0):
+        """Like set_eps, from raw host addresses (e.g. pinned buffers)."""
+        dp = C.POINTER(C.c_double)
+        _check(self.lib.fdtd_set_eps(self.h, *[C.cast(C.c_void_p(a), dp) if a else None for a in (e0, e1, e2)]))
+
+    def field_into(self, which: int, host_addr: int, layout: int = LAYOUT_GLOBAL):
+        """Copy a field to a raw host address (complex interleaved)."""
+        _check(self.lib.fdtd_get_field(self.h, int(which), int(layout),
+                                       C.cast(C.c_void_p(host_addr), C.POINTER(C.c_double))))
+
+    def ntff_into(self, which: int, host_addr: int):
+        _check(self.lib.fdtd_get_ntff(self.h, int(which), C.cast(C.c_void_p(host_addr), C.POINTER(C.c_double))))
+
+    def eps_into(self, which: int, host_addr: int, layout: int = LAYOUT_GLOBAL):
+        _check(self.lib.fdtd_get_eps(self.h, int(which), int(layout),
+                                     C.cast(C.c_void_p(host_addr), C.POINTER(C.c_double))))
+
+    def profile(self, on: bool = True):
+        """Record CUDA events around every launch class on the engine stream."""
+        _check(self.lib.fdtd_profile_enable(self.h, 1 if on else 0))
+
+    def profile_read(self) -> dict:
+        """Summed ms per launch class since profile(True) (synchronizes, clears)."""
+        ms = np.zeros(4)
+        steps = C.c_longlong()
+        _check(self.lib.fdtd_profile_read(self.h, _dptr(ms), C.byref(steps)))
+        return {"e_half": ms[0], "h_half": ms[1], "ntff_gather": ms[2], "ntff_deposit": ms[3],
+                "steps": int(steps.value)}
+
+    def set_option(self, key: int, value: int):
+        _check(self.lib.fdtd_set_option(self.h, int(key), int(value)))
+
+    def get_option(self, key: int) -> int:
+        v = C.c_int()
+        _check(self.lib.fdtd_get_option(self.h, int(key), C.byref(v)))
+        return v.value
 
     def fill_model(self, model: int, params=()):
         p = np.ascontiguousarray(params, dtype=np.float64)

@@ -277,7 +277,14 @@ static void field_setup(of_sim *s)
 
 /* ---------------------------------------------------------- allocation */
 
-static void *zalloc(size_t n) { void *p = calloc(1, n); return p; }
+/* malloc + memset as the reference's allocateMemories() does
+ * (mpiTM_UPML.c:604-661): every page is touched at setup, not in the timed loop */
+static void *zalloc(size_t n)
+{
+  void *p = malloc(n);
+  if (p) memset(p, 0, n);
+  return p;
+}
 
 static void coefficients(of_sim *s)
 {

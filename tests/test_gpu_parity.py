@@ -56,6 +56,85 @@ def test_gpu_fp64_matches_reference_golden(name):
     assert not bad, f"{name}: {bad}"
 
 
+MODEL_CASES = ["mpi_tm_circle", "mpi_te_circle", "mpi_tm_morpho", "mpi_te_morpho_eps225", "ser_tm_circle",
+               "ser_te_circle"]
+
+
+def _product_model(spec):
+    m = _engine()
+    if spec[0] == "circle":
+        return m.MODEL_CIRCLE, [spec[1], spec[2]]
+    if spec[0] == "morpho":
+        w, t0, t1, layers, branch, edge, eps = spec[1:8]
+        return m.MODEL_MORPHO, [w, t0, t1, layers, branch, edge, eps, 0.0]
+    raise ValueError(spec)
+
+
+@pytest.mark.parametrize("name", MODEL_CASES)
+def test_gpu_model_fill_equals_reference_eps(name):
+    """Device evaluators of circleModel.c / morphoScaleModel.c give the
+    reference's permittivity bit-for-bit at every staggered point."""
+    m = _engine()
+    c = CASES[name]
+    ref = np.load(GOLDEN / f"{name}.npz")
+    sim = m.Simulation(c["solver"], m.FieldInfo(*c["fi"]))
+    sim.fill_model(*_product_model(c["model"]))
+    for w in range(3):
+        np.testing.assert_array_equal(sim.eps(w), ref[f"eps{w}"], err_msg=f"{name} eps{w}")
+
+
+def test_gpu_model_fill_run_matches_golden():
+    """fill_model + run reproduces the golden fields (no host permittivity)."""
+    m = _engine()
+    name = "mpi_tm_morpho"
+    c = CASES[name]
+    ref = dict(np.load(GOLDEN / f"{name}.npz"))
+    sim = m.Simulation(c["solver"], m.FieldInfo(*c["fi"]))
+    sim.fill_model(*_product_model(c["model"]))
+    sim.run(c["steps"])
+    for w in range(3):
+        assert rel(sim.field(w), ref[f"field{w}"]) <= TOL
+
+
+def test_gpu_bad_eps_rejected():
+    m = _engine()
+    sim = m.Simulation("MPI_TM_UPML", m.FieldInfo(300, 320, 5, 6, 100, 0, 150))
+    e = np.ones((sim.n_px, sim.n_py))
+    e[3, 4] = -1.0
+    with pytest.raises(m.FdtdError):
+        sim.set_eps(e)
+
+
+def test_gpu_clock_outside_step_num_rejected():
+    m = _engine()
+    sim = m.Simulation("MPI_TM_UPML", m.FieldInfo(300, 320, 5, 6, 100, 0, 10))
+    sim.run(10)
+    with pytest.raises(m.FdtdError):
+        sim.run(1)
+    with pytest.raises(m.FdtdError):
+        sim.update(-1.0, 0.0)
+    assert sim.status == 0
+
+
+@pytest.mark.parametrize("mode,chunk", [(0, 1024), (1, 64), (1, 1024), (1, 4096)])
+def test_gpu_ntff_variants_agree(mode, chunk):
+    """Direct-atomic and shared-window NTFF deposits agree with the golden rows."""
+    m = _engine()
+    name = "mpi_tm_discs_30deg"
+    c = CASES[name]
+    ref = dict(np.load(GOLDEN / f"{name}.npz"))
+    sim = m.Simulation(c["solver"], m.FieldInfo(*c["fi"]))
+    sim.set_option(m.OPT_NTFF_MODE, mode)
+    sim.set_option(m.OPT_NTFF_CHUNK, chunk)
+    sim.set_eps(*_eps_for(name, c))
+    sim.run(c["steps"])
+    got = capture([sim.field(w) for w in range(3)], [sim.eps(w) for w in range(3)],
+                  [sim.ntff(w) for w in range(3)], sim.array_size, "full")
+    bad = compare(got, {k: v for k, v in ref.items() if k.startswith("ntff")}, TOL)
+    assert not bad, bad
+    assert sim.status == 0
+
+
 def test_gpu_vacuum_config1_exact_zero():
     """SURVEY config 1 (276^2, vacuum, 2000 steps): every output stays exactly 0."""
     _, got = run_gpu("mpi_tm_vacuum_c1")
