@@ -135,9 +135,15 @@ int fdtd_device_field(fdtd_sim *sim, int which, void **dptr, int *pitch, int *ro
 #define FDTD_STATUS_NTFF_RANGE 1u
 int fdtd_get_status(fdtd_sim *sim, unsigned int *flags);
 
-/* Tuning knobs (results are the same up to summation order). */
-#define FDTD_OPT_NTFF_MODE 1     /* 0 direct global atomics, 1 shared-memory window (default) */
-#define FDTD_OPT_NTFF_CHUNK 2    /* cells of a side per window block (64..4096, default 1024) */
+/* Tuning knobs (results are the same up to summation order).
+ * NTFF deposit modes: 0 direct (three atomic adds per tap set every step),
+ * 1 shared-memory window per side chunk, 2 time-blocked (default): the path
+ * samples of FDTD_OPT_NTFF_BLOCK consecutive steps are buffered and each
+ * (angle, cell) pair deposits them in one pass.  Buffered steps are deposited
+ * before any NTFF read-out, fdtd_synchronize, fdtd_reset or option change. */
+#define FDTD_OPT_NTFF_MODE 1     /* 0, 1 or 2 (default 2)                              */
+#define FDTD_OPT_NTFF_CHUNK 2    /* mode 1: cells of a side per block (64..4096, 1024)  */
+#define FDTD_OPT_NTFF_BLOCK 3    /* mode 2: steps per deposit (1..64, default 32)       */
 int fdtd_set_option(fdtd_sim *sim, int key, int value);
 int fdtd_get_option(fdtd_sim *sim, int key, int *value);
 

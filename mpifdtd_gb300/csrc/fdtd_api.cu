@@ -257,7 +257,7 @@ static int build_ntff(fdtd_sim *s)
   s->h_shift.swap(shift);
   s->h_side.swap(side);
   s->window_dirty = true;
-  CK(cudaMalloc(&s->d_vals, sizeof(double2) * 2 * n));
+  CK(cudaMalloc(&s->d_vals, sizeof(double2) * 2 * (size_t)n * kMaxNtffBlock));
   s->ntff_len = (size_t)360 * g.array_size + 2 * kGuard;
   for (int a = 0; a < 3; a++) {
     CK(cudaMalloc(&s->d_ntff[a], sizeof(double2) * s->ntff_len));
@@ -489,12 +489,16 @@ static int build_windows(fdtd_sim *s)
   return FDTD_OK;
 }
 
+static int flush_ntff(fdtd_sim *s);
+
 extern "C" int fdtd_set_option(fdtd_sim *s, int key, int value)
 {
   if (!s) return fail(FDTD_E_ARG, "null simulation");
+  int rc = flush_ntff(s);  // buffered steps are deposited with the settings they were taken under
+  if (rc) return rc;
   switch (key) {
   case FDTD_OPT_NTFF_MODE:
-    if (value != 0 && value != 1) return fail(FDTD_E_ARG, "NTFF mode must be 0 or 1");
+    if (value < 0 || value > 2) return fail(FDTD_E_ARG, "NTFF mode must be 0, 1 or 2");
     s->ntff_mode = value;
     return FDTD_OK;
   case FDTD_OPT_NTFF_CHUNK:
@@ -502,6 +506,10 @@ extern "C" int fdtd_set_option(fdtd_sim *s, int key, int value)
     CK(cudaStreamSynchronize(s->stream));
     s->ntff_chunk = value;
     s->window_dirty = true;
+    return FDTD_OK;
+  case FDTD_OPT_NTFF_BLOCK:
+    if (value < 1 || value > kMaxNtffBlock) return fail(FDTD_E_ARG, "NTFF block must be in [1, %d]", kMaxNtffBlock);
+    s->ntff_block = value;
     return FDTD_OK;
   }
   return fail(FDTD_E_ARG, "unknown option %d", key);
@@ -513,6 +521,7 @@ extern "C" int fdtd_get_option(fdtd_sim *s, int key, int *value)
   switch (key) {
   case FDTD_OPT_NTFF_MODE: *value = s->ntff_mode; return FDTD_OK;
   case FDTD_OPT_NTFF_CHUNK: *value = s->ntff_chunk; return FDTD_OK;
+  case FDTD_OPT_NTFF_BLOCK: *value = s->ntff_block; return FDTD_OK;
   }
   return fail(FDTD_E_ARG, "unknown option %d", key);
 }
@@ -634,17 +643,46 @@ static void enqueue_step(fdtd_sim *s, double time, double ray_coef)
     launch_te_e<R>(v, sx, sy, st);
   }
   mark(s);
-  launch_ntff_gather<R>(v, n, coef, st);
+  const bool blocked = s->ntff_mode == 2;
+  launch_ntff_gather<R>(v, n, coef, blocked ? s->nb_pending : 0, st);
   mark(s);
-  if (s->ntff_mode == 1) {
+  s->launches += 3;
+  if (blocked) {
+    if (s->nb_pending++ == 0) s->pending_t0 = time - 1;
+    if (s->nb_pending == s->ntff_block) {
+      launch_ntff_block(n, s->nb_pending, s->pending_t0, st);
+      s->nb_pending = 0;
+      s->launches += 1;
+    }
+  } else if (s->ntff_mode == 1) {
     NtffWindow w{(const int2 *)s->d_chunk, (const int2 *)s->d_lo, s->nchunk, s->win_width};
     launch_ntff_window(n, w, time - 1, time - 0.5, st);
+    s->launches += 1;
   } else {
     launch_ntff_accumulate(n, time - 1, time - 0.5, st);
+    s->launches += 1;
   }
   mark(s);
   if (s->profiling) s->prof_steps++;
-  s->launches += 4;
+}
+
+// Deposits the buffered steps of the time-blocked NTFF (mode 2).
+static int flush_ntff(fdtd_sim *s)
+{
+  if (s->nb_pending == 0) return FDTD_OK;
+  launch_ntff_block(ntff_view(s), s->nb_pending, s->pending_t0, s->stream);
+  s->nb_pending = 0;
+  s->launches += 1;
+  CK(cudaGetLastError());
+  return FDTD_OK;
+}
+
+// A buffered block holds consecutive steps only: a step that does not follow
+// the last buffered one first deposits the block.
+static int before_step(fdtd_sim *s, double time)
+{
+  if (s->ntff_mode == 2 && s->nb_pending > 0 && time - 1 != s->pending_t0 + s->nb_pending) return flush_ntff(s);
+  return FDTD_OK;
 }
 
 extern "C" int fdtd_profile_enable(fdtd_sim *s, int on)
@@ -698,6 +736,7 @@ extern "C" int fdtd_update(fdtd_sim *s, double time, double ray_coef)
   if (!s) return fail(FDTD_E_ARG, "null simulation");
   if (int rc = check_clock(s, time)) return rc;
   if (int rc = prepare_step(s)) return rc;
+  if (int rc = before_step(s, time)) return rc;
   if (s->f32) enqueue_step<float>(s, time, ray_coef);
   else enqueue_step<double>(s, time, ray_coef);
   CK(cudaGetLastError());
@@ -711,6 +750,8 @@ extern "C" int fdtd_run(fdtd_sim *s, int n_steps)
   if (n_steps > 0)
     if (int rc = check_clock(s, s->time + (n_steps - 1))) return rc;
   if (int rc = prepare_step(s)) return rc;
+  if (n_steps > 0)
+    if (int rc = before_step(s, s->time)) return rc;
   for (int q = 0; q < n_steps; q++) {
     const double t = s->time;
     const double rc = s->ray_coef;
@@ -742,6 +783,7 @@ extern "C" int fdtd_set_time(fdtd_sim *s, double t)
 extern "C" int fdtd_synchronize(fdtd_sim *s)
 {
   if (!s) return fail(FDTD_E_ARG, "null simulation");
+  if (int rc = flush_ntff(s)) return rc;
   CK(cudaStreamSynchronize(s->stream));
   return FDTD_OK;
 }
@@ -751,6 +793,7 @@ extern "C" long long fdtd_launch_count(const fdtd_sim *s) { return s ? s->launch
 extern "C" int fdtd_get_status(fdtd_sim *s, unsigned int *flags)
 {
   if (!s || !flags) return fail(FDTD_E_ARG, "null argument");
+  if (int rc = flush_ntff(s)) return rc;
   CK(cudaStreamSynchronize(s->stream));
   CK(cudaMemcpy(flags, s->d_status, sizeof(unsigned int), cudaMemcpyDeviceToHost));
   return FDTD_OK;
@@ -807,6 +850,7 @@ extern "C" int fdtd_get_ntff(fdtd_sim *s, int which, double *out)
 {
   if (!s || !out) return fail(FDTD_E_ARG, "null argument");
   if (which < 0 || which > 2) return fail(FDTD_E_ARG, "ntff index %d out of range", which);
+  if (int rc = flush_ntff(s)) return rc;
   CK(cudaStreamSynchronize(s->stream));
   CK(cudaMemcpy(out, (const double2 *)s->d_ntff[which] + kGuard, sizeof(double2) * 360 * s->geo.array_size,
                 cudaMemcpyDeviceToHost));
@@ -817,6 +861,7 @@ extern "C" int fdtd_get_ntff_guard(fdtd_sim *s, int which, double *out, int *gua
 {
   if (!s || !out) return fail(FDTD_E_ARG, "null argument");
   if (which < 0 || which > 2) return fail(FDTD_E_ARG, "ntff index %d out of range", which);
+  if (int rc = flush_ntff(s)) return rc;
   CK(cudaStreamSynchronize(s->stream));
   const double2 *base = (const double2 *)s->d_ntff[which];
   CK(cudaMemcpy(out, base, sizeof(double2) * kGuard, cudaMemcpyDeviceToHost));
@@ -829,6 +874,7 @@ extern "C" int fdtd_get_ntff_guard(fdtd_sim *s, int which, double *out, int *gua
 extern "C" int fdtd_reset(fdtd_sim *s)
 {
   if (!s) return fail(FDTD_E_ARG, "null simulation");
+  if (int rc = flush_ntff(s)) return rc;
   const size_t bytes = (size_t)s->nxa * s->pitch * s->esize;
   for (int a = 0; a < s->nslots; a++) CK(cudaMemsetAsync(s->d_f[a], 0, bytes, s->stream));
   if (!s->mpi)

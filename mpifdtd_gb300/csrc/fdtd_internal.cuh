@@ -28,6 +28,7 @@ constexpr double kC = 0.7071;                 // field.h:70 C_0_S
 constexpr double kEps0 = 1.0;                 // field.h:73
 constexpr double kZ0 = 1.41422712488;         // field.h:75
 constexpr int kGuard = 16;                    // NTFF guard cells each side
+constexpr int kMaxNtffBlock = 64;             // steps buffered per time-blocked NTFF deposit
 constexpr int kNfft = 8192;                   // ntff.h:6 NTFF_NUM
 constexpr int kLambdaSt = 380, kLambdaEn = 700;  // ntff.h:4-5
 
@@ -75,7 +76,7 @@ struct NtffView {
   double2 *acc[3];        // base pointers incl. guard (flat [360][AS] + 2*guard)
   const double *shift;    // [360][ncell] retarded-time shift per (angle, cell)
   const SurfCell *cells;
-  double2 *vals;          // [2][ncell] surface values of this step (E then H)
+  double2 *vals;          // [slot][2][ncell] surface values (E then H) of buffered steps
   int ncell, array_size;
   long long len;          // elements of each accumulator incl. guards
   unsigned int *status;   // device status word (kStatus* bits)
@@ -105,9 +106,11 @@ void launch_te_e(const StencilView<R> &v, const SourceStep &sx, const SourceStep
 template <typename R>
 void launch_te_h(const StencilView<R> &v, cudaStream_t st);
 template <typename R>
-void launch_ntff_gather(const StencilView<R> &v, const NtffView &n, double coef, cudaStream_t st);
+void launch_ntff_gather(const StencilView<R> &v, const NtffView &n, double coef, int slot, cudaStream_t st);
 void launch_ntff_accumulate(const NtffView &n, double timeE, double timeH, cudaStream_t st);
 void launch_ntff_window(const NtffView &n, const NtffWindow &w, double timeE, double timeH, cudaStream_t st);
+// Deposit nb buffered steps (slots 0..nb-1) whose first step has timeE = t0.
+void launch_ntff_block(const NtffView &n, int nb, double t0, cudaStream_t st);
 
 }  // namespace fdtd
 

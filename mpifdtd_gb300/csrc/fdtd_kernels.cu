@@ -251,10 +251,11 @@ __global__ void __launch_bounds__(256) te_h_kernel(StencilView<R> v)
 // Tangential samples of the NTFF path, already signed and scaled:
 //   e = sign * E[k] * coef,  h = sign * 0.5 * (H[k] + H[k+hoff]) * coef
 template <typename R>
-__global__ void ntff_gather_kernel(StencilView<R> v, NtffView n, double coef)
+__global__ void ntff_gather_kernel(StencilView<R> v, NtffView n, double coef, int slot)
 {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= n.ncell) return;
+  n.vals += (size_t)slot * 2 * n.ncell;
   const SurfCell sc = n.cells[c];
   const typename Cplx<R>::T *E = v.f[sc.e_slot], *H = v.f[sc.h_slot];
   const auto e = E[sc.k];
@@ -384,6 +385,70 @@ __global__ void __launch_bounds__(256) ntff_window_kernel(NtffView n, NtffWindow
   }
 }
 
+// Time-blocked deposit.  One thread owns one (angle, path cell) pair and walks
+// nb buffered steps.  With timeE integer and t = timeE + sh, the reference's
+// rounding gives fl(timeE + sh) = timeE + R(sh) for every step whose t and
+// t + 1/2 stay inside one binade (timeE is then a multiple of the ulp), so
+// m = floor(t + 1/2) advances by exactly one per step and a = 1/2 + t - m is
+// the same every step.  Each step then completes one bin:
+//   bin m-1 : A + v b   (flushed)     bin m : v (a-b) - P     bin m+1 : -v a
+// carried in registers (A, P).  A block whose t range crosses a binade, or a
+// non-integer clock, takes the exact per-step path (deposit()).
+__device__ __forceinline__ int binade(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7ff); }
+
+__device__ __forceinline__ void red_c(const NtffView &n, double2 *acc, long long at, double2 v)
+{
+  if (at < 0 || at >= n.len) {
+    atomicOr(n.status, kStatusNtffRange);
+    return;
+  }
+  atomicAdd(&acc[at].x, v.x);
+  atomicAdd(&acc[at].y, v.y);
+}
+
+__device__ __forceinline__ void block_field(const NtffView &n, double2 *acc, long long row, const double2 *vals,
+                                            int nb, double base, double sh, bool t0_integer)
+{
+  const double tf = base + sh;
+  const double ul = (base + (double)(nb - 1) + sh) + 0.5;
+  const int e = binade(tf);
+  if (t0_integer && tf >= 1.0 && e == binade(ul) && e <= 1023 + 50) {
+    const double uf = tf + 0.5;
+    const double mf = floor(uf);
+    const double a = uf - mf, b = 1.0 - a, ab = a - b;
+    const long long m0 = row + (long long)mf;
+    double2 A = make_double2(0.0, 0.0), P = make_double2(0.0, 0.0);
+    for (int s = 0; s < nb; s++) {
+      const double2 v = vals[(size_t)s * 2 * n.ncell];
+      double2 f;
+      f.x = fma(v.x, b, A.x);
+      f.y = fma(v.y, b, A.y);
+      red_c(n, acc, m0 + s - 1, f);
+      A.x = fma(v.x, ab, -P.x);
+      A.y = fma(v.y, ab, -P.y);
+      P.x = v.x * a;
+      P.y = v.y * a;
+    }
+    red_c(n, acc, m0 + nb - 1, A);
+    red_c(n, acc, m0 + nb, make_double2(-P.x, -P.y));
+    return;
+  }
+  for (int s = 0; s < nb; s++) deposit(n, acc, row, (base + (double)s) + sh, vals[(size_t)s * 2 * n.ncell]);
+}
+
+__global__ void __launch_bounds__(256) ntff_block_kernel(NtffView n, int nb, double t0)
+{
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ang = blockIdx.y;
+  if (c >= n.ncell) return;
+  const double sh = n.shift[(size_t)ang * n.ncell + c];
+  const unsigned char uw = (unsigned char)n.cells[c].uid_wid;
+  const long long row = (long long)kGuard + (long long)ang * n.array_size;
+  const bool integer_clock = t0 == floor(t0);
+  block_field(n, n.acc[uw & 15], row, n.vals + c, nb, t0, sh, integer_clock);              // E, timeE
+  block_field(n, n.acc[uw >> 4], row, n.vals + n.ncell + c, nb, t0 + 0.5, sh, integer_clock);  // H, timeH
+}
+
 // ------------------------------------------------------------------ launchers
 
 template <typename R>
@@ -415,9 +480,14 @@ void launch_te_h(const StencilView<R> &v, cudaStream_t st)
   te_h_kernel<R><<<grid_of(v, kBlock), kBlock, 0, st>>>(v);
 }
 template <typename R>
-void launch_ntff_gather(const StencilView<R> &v, const NtffView &n, double coef, cudaStream_t st)
+void launch_ntff_gather(const StencilView<R> &v, const NtffView &n, double coef, int slot, cudaStream_t st)
 {
-  ntff_gather_kernel<R><<<(n.ncell + 255) / 256, 256, 0, st>>>(v, n, coef);
+  ntff_gather_kernel<R><<<(n.ncell + 255) / 256, 256, 0, st>>>(v, n, coef, slot);
+}
+void launch_ntff_block(const NtffView &n, int nb, double t0, cudaStream_t st)
+{
+  dim3 g((unsigned)((n.ncell + 255) / 256), 360);
+  ntff_block_kernel<<<g, 256, 0, st>>>(n, nb, t0);
 }
 void launch_ntff_accumulate(const NtffView &n, double timeE, double timeH, cudaStream_t st)
 {
@@ -442,7 +512,7 @@ void launch_ntff_window(const NtffView &n, const NtffWindow &w, double timeE, do
   template void launch_te_e<R>(const StencilView<R> &, const SourceStep &, const SourceStep &,   \
                                cudaStream_t);                                                    \
   template void launch_te_h<R>(const StencilView<R> &, cudaStream_t);                            \
-  template void launch_ntff_gather<R>(const StencilView<R> &, const NtffView &, double, cudaStream_t);
+  template void launch_ntff_gather<R>(const StencilView<R> &, const NtffView &, double, int, cudaStream_t);
 INST(double)
 INST(float)
 #undef INST

@@ -19,7 +19,9 @@ __global__ void eps_model_kernel(double *e0, double *e1, double *e2, int P, int 
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= nxa || j >= ncols) return;
+  // every column of the pitch is written (padding and halo get 1.0) so the
+  // 1/eps pass over the whole allocation never reads unset memory
+  if (i >= nxa || j >= P) return;
   const size_t k = (size_t)i * P + j;
   const int x = i + ox, y = j + ox;
   double a = 1.0, b = 1.0, c = 1.0;
@@ -59,7 +61,8 @@ __global__ void fill_kernel(double *p, double v, size_t count)
 void launch_eps_model(double *e0, double *e1, double *e2, int P, int nxa, int ncols, int ox, int n_px, int n_py,
                       bool tm, bool mpi, const mdl_params &m, cudaStream_t st)
 {
-  dim3 b(32, 8), g((unsigned)((ncols + 31) / 32), (unsigned)((nxa + 7) / 8));
+  (void)ncols;
+  dim3 b(32, 8), g((unsigned)((P + 31) / 32), (unsigned)((nxa + 7) / 8));
   eps_model_kernel<<<g, b, 0, st>>>(e0, e1, e2, P, nxa, ncols, ox, n_px, n_py, tm ? 1 : 0, mpi ? 1 : 0, m);
 }
 

@@ -31,8 +31,10 @@ struct fdtd_sim {
   size_t ntff_len = 0;
   std::vector<double> h_shift;   // [360][ncell], kept to rebuild the window tables
   std::vector<int> h_side;       // side of each path cell (0 bottom, 1 right, 2 top, 3 left)
-  // shared-memory window variant (FDTD_OPT_NTFF_MODE 1)
-  int ntff_mode = 1, ntff_chunk = 1024;
+  // NTFF deposit: 0 direct, 1 shared window, 2 time-blocked (default)
+  int ntff_mode = 2, ntff_chunk = 1024, ntff_block = 32;
+  int nb_pending = 0;           // buffered steps not yet deposited (mode 2)
+  double pending_t0 = 0;        // timeE of the first buffered step
   void *d_chunk = nullptr, *d_lo = nullptr;
   int nchunk = 0, win_width = 0;
   bool window_dirty = true;

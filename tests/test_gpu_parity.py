@@ -116,9 +116,12 @@ def test_gpu_clock_outside_step_num_rejected():
     assert sim.status == 0
 
 
-@pytest.mark.parametrize("mode,chunk", [(0, 1024), (1, 64), (1, 1024), (1, 4096)])
-def test_gpu_ntff_variants_agree(mode, chunk):
-    """Direct-atomic and shared-window NTFF deposits agree with the golden rows."""
+@pytest.mark.parametrize("mode,chunk,block", [(0, 1024, 32), (1, 64, 32), (1, 4096, 32), (2, 1024, 1),
+                                              (2, 1024, 7), (2, 1024, 64)])
+def test_gpu_ntff_variants_agree(mode, chunk, block):
+    """Direct-atomic, shared-window and time-blocked NTFF deposits agree with
+    the golden rows (block 7 leaves a partial block and crosses binades of the
+    retarded time inside blocks, which takes the exact per-step path)."""
     m = _engine()
     name = "mpi_tm_discs_30deg"
     c = CASES[name]
@@ -126,6 +129,7 @@ def test_gpu_ntff_variants_agree(mode, chunk):
     sim = m.Simulation(c["solver"], m.FieldInfo(*c["fi"]))
     sim.set_option(m.OPT_NTFF_MODE, mode)
     sim.set_option(m.OPT_NTFF_CHUNK, chunk)
+    sim.set_option(m.OPT_NTFF_BLOCK, block)
     sim.set_eps(*_eps_for(name, c))
     sim.run(c["steps"])
     got = capture([sim.field(w) for w in range(3)], [sim.eps(w) for w in range(3)],
