@@ -157,6 +157,47 @@ int fdtd_profile_read(fdtd_sim *sim, double *ms_out, long long *steps);
 /* Number of kernel launches the engine issued since creation. */
 long long fdtd_launch_count(const fdtd_sim *sim);
 
+/* ---- Allocation-free NTFF step (no counterpart in the reference) ---------
+ * For callers that may not allocate device memory, directly or through this
+ * library: a host application whose memory manager owns every device buffer
+ * of the process, or a loop that must not pay the device-wide
+ * synchronisation cudaMalloc/cudaFree imply.  Such a caller keeps the fields
+ * and the NTFF accumulators in its own device buffers and calls this once per
+ * update(): it adds that step's 360-angle time-domain NTFF contribution of an
+ * MPI UPML solver (mpiTM_UPML.c:849-1037, mpiTE_UPML.c:611-794), the same
+ * arithmetic as the engine's own NTFF kernels.
+ *
+ * No cudaMalloc, cudaFree or allocating library call is made.  The path
+ * samples are staged in one file-scope __device__ array sized for
+ * FDTD_NOALLOC_MAX_PATH path cells (2 MB, held by every GPU that loads the
+ * library until the process exits); a larger path is rejected with
+ * FDTD_E_ARG.  The first call on a device looks the array up and uploads the
+ * 360 direction cosines, so make that first call before any stream capture.
+ * Every call reuses the same array (each call overwrites all of it before
+ * reading), so calls that overlap on the GPU -- on different streams, or from
+ * several host threads -- race; order them on one stream.
+ *
+ * args->e0/e1/h0/h1: device FP64 complex fields in the one-rank layout of the
+ *   MPI solvers: row i, column j at (i*pitch + j), i in [0, N_PX+2), global
+ *   x = i-1 (TM: e0 Ez, h0 Hx, h1 Hy; TE: e0 Ex, e1 Ey, h0 Hz).
+ * args->acc[3]: device accumulators (TM Ux, Uy, Wz; TE Wx, Wy, Uz), each
+ *   pointing at element 0 of its flat 360*array_size complex block and owning
+ *   FDTD_NTFF_GUARD complex elements before and after it (the flat index of
+ *   the reference reaches past the block at corner angles).
+ * args->time: the clock of the update() these fields come from, in
+ *   [0, step_num-1].  stream: cudaStream_t to launch on (NULL: default). */
+#define FDTD_NOALLOC_MAX_PATH 65536
+#define FDTD_NTFF_GUARD 16
+typedef struct fdtd_ntff_step_args {
+  int solver;                /* FDTD_MPI_TM_UPML or FDTD_MPI_TE_UPML           */
+  fdtd_config cfg;           /* the grid, as for fdtd_create                    */
+  const void *e0, *e1, *h0, *h1;
+  int pitch;                 /* complex elements per row, >= N_PY + 2           */
+  double time;
+  void *acc[3];
+} fdtd_ntff_step_args;
+int fdtd_ntff_step_noalloc(const fdtd_ntff_step_args *args, void *stream);
+
 const char *fdtd_last_error(void);
 const char *fdtd_version(void);
 

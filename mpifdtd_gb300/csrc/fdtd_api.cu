@@ -60,6 +60,17 @@ double sigma_axis(double x, int n_pml, int n_inner, int n_full)
 
 }  // namespace
 
+int fdtd::set_error(int code, const char *fmt, ...)
+{
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
 extern "C" const char *fdtd_last_error(void) { return g_err.c_str(); }
 extern "C" const char *fdtd_version(void) { return "mpifdtd_gb300 0.1 (sm_103a)"; }
 

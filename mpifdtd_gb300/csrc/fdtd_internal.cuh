@@ -118,6 +118,9 @@ void launch_ntff_block(const NtffView &n, int nb, double t0, cudaStream_t st);
 
 namespace fdtd {
 
+// Sets the calling thread's fdtd_last_error() message and returns code (fdtd_api.cu).
+int set_error(int code, const char *fmt, ...);
+
 // fdtd_setup.cu
 void launch_eps_model(double *e0, double *e1, double *e2, int P, int nxa, int ncols, int ox, int n_px, int n_py,
                       bool tm, bool mpi, const mdl_params &m, cudaStream_t st);
