@@ -119,6 +119,18 @@ int fdtd_get_ntff(fdtd_sim *sim, int which, double *out_complex);
  * has `guard` cells; the reference writes past its allocation there). */
 int fdtd_get_ntff_guard(fdtd_sim *sim, int which, double *out_complex, int *guard);
 
+/* Far-field spectrum of ntffTM_TimeOutput / ntffTE_TimeOutput
+ * (ntffTM.c:197-275, ntffTE.c:160-238): E_theta (TM) or E_phi (TE) from the
+ * NTFF accumulators, zero-padded 8192-point FFT per angle, |E|^2 at every nm
+ * from 380 to 700.  out: double[321][360], the layout ntff_outputEnormBin
+ * writes (ntff.c:20-33).  step_num > 8192 returns FDTD_E_UNSUPPORTED (the
+ * reference's FFT buffer overflows there, ntffTM.c:214-221). */
+int fdtd_spectrum(fdtd_sim *sim, double *out);
+/* Frequency-domain NTFF of the current fields, ntffTM_Frequency
+ * (ntffTM.c:72-158, R0 = 1e6 * 500 nm in cells); out: 360 complex.  TM only:
+ * the reference's TE version indexes through an unset sub-domain record. */
+int fdtd_frequency(fdtd_sim *sim, double *out_complex);
+
 /* reset() of the solvers (mpiTM_UPML.c:219-232): zero every field; the
  * serial solvers also zero the NTFF arrays (fdtdTM_upml.c:110-113). The
  * engine clock returns to 0. */

@@ -1,0 +1,92 @@
+/*
+ * mpifdtd_upml.h -- the reference's UPML solver entry points, served by the
+ * GB300 engine (libmpifdtd_upml.so on top of libmpifdtd_gb300.so).
+ *
+ * Drop-in for the four solver translation units of rennone/mpiFDTD that
+ * simulator.c binds (simulator.c:134-205): link libmpifdtd_upml.so instead of
+ * mpiTM_UPML.c, mpiTE_UPML.c, fdtdTM_upml.c and fdtdTE_upml.c; simulator.c,
+ * field.c, models.c and the models stay as they are.  The library calls back
+ * into the host program's field_getFieldInfo(), field_getTime(),
+ * field_getRayCoef(), field_getWaveAngle() and models_eps() exactly where the
+ * reference solvers read them, so the host keeps owning time (field_nextStep
+ * after update(), simulator.c:247-251) and the permittivity callback.
+ *
+ * Semantics per entry point (differences from the reference are listed in
+ * INTEGRATION.md):
+ *   init()   allocates the device state, fills the permittivity through
+ *            models_eps() at the solver's staggered points and modes
+ *   update() one time step on the GPU at field_getTime()/field_getRayCoef()
+ *   reset()  zeroes the fields (serial solvers first write the far-field
+ *            spectrum files, as ntffTM_TimeOutput does)
+ *   finish() releases everything (serial solvers write the spectrum first)
+ *   get*()   borrowed host pointers in the reference solver's own layout,
+ *            refreshed from the device on each call after an update()
+ * This header is C only (double complex), like the reference's headers.
+ */
+#ifndef MPIFDTD_UPML_H
+#define MPIFDTD_UPML_H
+#include <complex.h>
+
+/* mpiTM_UPML.h:5-18 */
+extern void (*mpi_fdtdTM_upml_getUpdate(void))(void);
+extern void (*mpi_fdtdTM_upml_getFinish(void))(void);
+extern void (*mpi_fdtdTM_upml_getReset(void))(void);
+extern void (*mpi_fdtdTM_upml_getInit(void))(void);
+extern double complex *mpi_fdtdTM_upml_getHx(void);
+extern double complex *mpi_fdtdTM_upml_getHy(void);
+extern double complex *mpi_fdtdTM_upml_getEz(void);
+extern double *mpi_fdtdTM_upml_getEps(void);
+extern int mpi_fdtdTM_upml_getSubNx(void);
+extern int mpi_fdtdTM_upml_getSubNy(void);
+extern int mpi_fdtdTM_upml_getSubNpx(void);
+extern int mpi_fdtdTM_upml_getSubNpy(void);
+extern int mpi_fdtdTM_upml_getSubNcell(void);
+
+/* mpiTE_UPML.h:5-19 */
+extern void (*mpi_fdtdTE_upml_getUpdate(void))(void);
+extern void (*mpi_fdtdTE_upml_getFinish(void))(void);
+extern void (*mpi_fdtdTE_upml_getReset(void))(void);
+extern void (*mpi_fdtdTE_upml_getInit(void))(void);
+extern double complex *mpi_fdtdTE_upml_getEx(void);
+extern double complex *mpi_fdtdTE_upml_getEy(void);
+extern double complex *mpi_fdtdTE_upml_getHz(void);
+extern int mpi_fdtdTE_upml_getSubNx(void);
+extern int mpi_fdtdTE_upml_getSubNy(void);
+extern int mpi_fdtdTE_upml_getSubNpx(void);
+extern int mpi_fdtdTE_upml_getSubNpy(void);
+extern int mpi_fdtdTE_upml_getSubNcell(void);
+extern double *mpi_fdtdTE_upml_getEps(void);
+
+/* fdtdTM_upml.h:5-14 */
+extern void (*fdtdTM_upml_getUpdate(void))(void);
+extern void (*fdtdTM_upml_getFinish(void))(void);
+extern void (*fdtdTM_upml_getReset(void))(void);
+extern void (*fdtdTM_upml_getInit(void))(void);
+extern double complex *fdtdTM_upml_getHx(void);
+extern double complex *fdtdTM_upml_getHy(void);
+extern double complex *fdtdTM_upml_getEz(void);
+extern double *fdtdTM_upml_getEps(void);
+
+/* fdtdTE_upml.h:5-14 */
+extern void (*fdtdTE_upml_getUpdate(void))(void);
+extern void (*fdtdTE_upml_getFinish(void))(void);
+extern void (*fdtdTE_upml_getInit(void))(void);
+extern void (*fdtdTE_upml_getReset(void))(void);
+extern double complex *fdtdTE_upml_getEx(void);
+extern double complex *fdtdTE_upml_getEy(void);
+extern double complex *fdtdTE_upml_getHz(void);
+extern double *fdtdTE_upml_getEps(void);
+
+/* Extensions (no counterpart in the reference).
+ * The reference reports errors with printf + exit(2) (function.c:27-32,
+ * simulator.c:234-237); the drop-in does the same by default.  Mode 1 makes
+ * the void entry points return instead and keeps the status for
+ * mpifdtd_upml_last_status() (FDTD_OK or an FDTD_E_* code). */
+extern void mpifdtd_upml_set_error_mode(int return_instead_of_exit);
+extern int mpifdtd_upml_last_status(void);
+/* The engine simulation behind a solver (4 MPI TM, 5 MPI TE, 2 TM, 3 TE), or
+ * NULL before init(): lets a host use the extended C ABI of mpifdtd_gb300.h. */
+struct fdtd_sim;
+extern struct fdtd_sim *mpifdtd_upml_engine(int solver);
+
+#endif

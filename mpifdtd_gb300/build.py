@@ -34,7 +34,8 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp
                      f"-I{INCLUDE}"]
 CC_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-Wall", f"-I{INCLUDE}"]
 
-ENGINE_SOURCES = ["fdtd_kernels.cu", "fdtd_api.cu", "fdtd_setup.cu", "ntff_noalloc.cu"]
+ENGINE_SOURCES = ["fdtd_kernels.cu", "fdtd_api.cu", "fdtd_setup.cu", "ntff_noalloc.cu",
+                  "fdtd_farfield.cu"]
 # The model evaluators classify sub-cell samples with comparisons such as
 # px*px + py*py <= r*r (circleModel.c:45-57); a fused multiply-add could flip a
 # sample on the boundary, so that file is compiled without contraction.
@@ -82,15 +83,13 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         list(ex.map(lambda c: _run(c, verbose), jobs))
     if force or jobs or _stale(ENGINE_SO, objs):
         _run([nvcc()] + ARCH + ["-shared", "-o", ENGINE_SO] + objs, verbose)
-    # drop-in layer (C) and the library's own field/models host API
-    upml_src = CSRC / "compat_upml.c"
-    if upml_src.exists() and (force or _stale(UPML_SO, [upml_src] + hdrs + [ENGINE_SO])):
-        _run(["gcc", "-std=gnu99"] + CC_FLAGS + ["-shared", "-o", UPML_SO, upml_src,
-                                                 f"-L{BUILD}", "-lmpifdtd_gb300",
-                                                 f"-Wl,-rpath,{BUILD}", "-lm"], verbose)
-    field_src = CSRC / "field_host.cu"
-    if field_src.exists() and (force or _stale(FIELD_SO, [field_src] + hdrs)):
-        _run([nvcc()] + NVCC_FLAGS + ["-shared", "-o", FIELD_SO, field_src], verbose)
+    # drop-in layer (C) and the library's own field/models host API, both
+    # linked against the engine and finding it next to themselves ($ORIGIN)
+    link = [f"-L{BUILD}", "-lmpifdtd_gb300", "-Wl,-rpath,$ORIGIN", "-lm"]
+    for src, so in ((CSRC / "compat_upml.c", UPML_SO), (CSRC / "field_host.c", FIELD_SO)):
+        if force or _stale(so, [src] + hdrs + [ENGINE_SO]):
+            _run([os.environ.get("CC", "gcc"), "-std=gnu99"] + CC_FLAGS + [f"-I{CSRC}", "-shared", "-o", so, src]
+                 + link, verbose)
     return ENGINE_SO
 
 

@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -296,6 +297,10 @@ static void free_sim(fdtd_sim *s)
   cudaFree(s->d_chunk);
   cudaFree(s->d_lo);
   for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
+  cudaFree(s->d_spec);
+  cudaFree(s->d_dirs);
+  cudaFree(s->d_twiddle);
+  cudaFree(s->d_freq);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
 }
@@ -911,5 +916,96 @@ extern "C" int fdtd_device_field(fdtd_sim *s, int which, void **dptr, int *pitch
   *dptr = s->d_f[slot];
   if (pitch) *pitch = s->pitch;
   if (rows) *rows = s->nxa;
+  return FDTD_OK;
+}
+
+// ---------------------------------------------------------------- far field
+
+static int ensure_farfield(fdtd_sim *s)
+{
+  if (s->d_spec) return FDTD_OK;
+  CK(cudaMalloc(&s->d_spec, sizeof(double) * 321 * 360));
+  CK(cudaMalloc(&s->d_dirs, sizeof(double2) * 2 * 360));
+  CK(cudaMalloc(&s->d_twiddle, sizeof(double2) * (kNfft / 2)));
+  CK(cudaMalloc(&s->d_freq, sizeof(double2) * 360));
+  std::vector<double2> dirs(2 * 360), tw(kNfft / 2);
+  for (int ang = 0; ang < 360; ang++) {
+    // [0..359] the spectrum's phi: ntffTM.c:169-173 ang*(M_PI/180.0) (TM), ntffTE.c:33 ang*M_PI/180.0 (TE)
+    const double phi = s->tm ? ang * (M_PI / 180.0) : ang * M_PI / 180.0;
+    dirs[ang] = make_double2(cos(phi), sin(phi));
+    // [360..719] ntffTM_Frequency's direction (ntffTM.c:89-91)
+    const double rad = ang * M_PI / 180.0;
+    dirs[360 + ang] = make_double2(cos(rad), sin(rad));
+  }
+  for (int k = 0; k < kNfft / 2; k++) {
+    const double arg = 2 * M_PI * k / kNfft;
+    tw[k] = make_double2(cos(arg), sin(arg));
+  }
+  CK(cudaMemcpy(s->d_dirs, dirs.data(), sizeof(double2) * dirs.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->d_twiddle, tw.data(), sizeof(double2) * tw.size(), cudaMemcpyHostToDevice));
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_spectrum(fdtd_sim *s, double *out)
+{
+  if (!s || !out) return fail(FDTD_E_ARG, "null argument");
+  if (s->cfg.step_num > kNfft)
+    return fail(FDTD_E_UNSUPPORTED, "step_num %d > %d: the reference's FFT buffer overflows (ntffTM.c:214-221)",
+                s->cfg.step_num, kNfft);
+  if (int rc = flush_ntff(s)) return rc;
+  if (int rc = ensure_farfield(s)) return rc;
+  SpectrumView v{};
+  for (int a = 0; a < 3; a++) v.acc[a] = (const double2 *)s->d_ntff[a];
+  v.array_size = s->geo.array_size;
+  v.max_time = s->cfg.step_num;
+  v.tm = s->tm ? 1 : 0;
+  v.h_u_nm = s->cfg.h_u_nm;
+  v.dir = (const double2 *)s->d_dirs;
+  v.twiddle = (const double2 *)s->d_twiddle;
+  // ntffTM.c:165 / ntffTE.c:25: 1/(4 pi C) * csqrt(2 pi C / (i w))
+  const std::complex<double> q = std::complex<double>(2 * M_PI * kC, 0.0) / std::complex<double>(0.0, s->geo.omega_s);
+  const std::complex<double> c = (1.0 / (4 * M_PI * kC)) * std::sqrt(q);
+  v.coef = make_double2(c.real(), c.imag());
+  v.out = (double *)s->d_spec;
+  launch_spectrum(v, s->stream);
+  s->launches += 1;
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, s->d_spec, sizeof(double) * 321 * 360, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_frequency(fdtd_sim *s, double *out)
+{
+  if (!s || !out) return fail(FDTD_E_ARG, "null argument");
+  if (!s->tm) return fail(FDTD_E_UNSUPPORTED, "frequency-domain NTFF is provided for TM (ntffTM.c:72-158) only");
+  if (s->f32) return fail(FDTD_E_UNSUPPORTED, "frequency-domain NTFF reads FP64 fields");
+  if (int rc = ensure_farfield(s)) return rc;
+  FrequencyView f{};
+  f.e = (const double2 *)s->d_f[0];
+  f.h[0] = (const double2 *)s->d_f[3];
+  f.h[1] = (const double2 *)s->d_f[4];
+  f.P = s->pitch;
+  f.ox = s->ox;
+  f.lt = s->geo.ntff_left;
+  f.rt = s->geo.ntff_right;
+  f.bm = s->geo.ntff_bottom;
+  f.tp = s->geo.ntff_top;
+  f.cx = s->geo.ntff_cx;
+  f.cy = s->geo.ntff_cy;
+  f.k_s = s->geo.k_s;
+  f.sqrt_hu = sqrt((double)s->cfg.h_u_nm);
+  f.dir = (const double2 *)s->d_dirs + 360;
+  // ntffTM.c:31 R0 = 1e6 * field_toCellUnit(500); ntffTM.c:82 coef
+  const double R0 = 1.0e6 * (500.0 / s->cfg.h_u_nm);
+  const std::complex<double> i_k(0.0, s->geo.k_s);
+  const std::complex<double> c = std::sqrt(i_k / (8 * M_PI * R0)) * std::exp(i_k * R0);
+  f.coef = make_double2(c.real(), c.imag());
+  f.out = (double2 *)s->d_freq;
+  launch_frequency(f, s->stream);
+  s->launches += 1;
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, s->d_freq, sizeof(double2) * 360, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
   return FDTD_OK;
 }

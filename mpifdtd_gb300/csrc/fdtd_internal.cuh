@@ -118,6 +118,27 @@ void launch_ntff_block(const NtffView &n, int nb, double t0, cudaStream_t st);
 
 namespace fdtd {
 
+// fdtd_farfield.cu
+struct SpectrumView {
+  const double2 *acc[3];   // NTFF accumulators incl. guard
+  int array_size, max_time, tm, h_u_nm;
+  const double2 *dir;      // [360] (cos phi, sin phi)
+  const double2 *twiddle;  // [4096] e^{+2 pi i k / 8192}
+  double2 coef;            // 1/(4 pi C) sqrt(2 pi C / (i w))  (ntffTM.c:165)
+  double *out;             // [321][360]
+};
+struct FrequencyView {
+  const double2 *e;        // Ez (global cell (x,y) at array (x-ox)*P + (y-ox))
+  const double2 *h[2];     // Hx, Hy
+  int P, ox, lt, rt, bm, tp;
+  double cx, cy, k_s, sqrt_hu;
+  const double2 *dir;      // [360] (cos, sin)
+  double2 coef;            // csqrt(i k/(8 pi R0)) e^{i k R0}  (ntffTM.c:82)
+  double2 *out;            // [360]
+};
+void launch_spectrum(const SpectrumView &s, cudaStream_t st);
+void launch_frequency(const FrequencyView &f, cudaStream_t st);
+
 // Sets the calling thread's fdtd_last_error() message and returns code (fdtd_api.cu).
 int set_error(int code, const char *fmt, ...);
 

@@ -42,6 +42,8 @@ struct fdtd_sim {
   // engine clock (field.c:21-22 time, ray_coef)
   double time = 0, ray_coef = 0;
   long long launches = 0;
+  // far-field outputs (allocated on first use)
+  void *d_spec = nullptr, *d_dirs = nullptr, *d_twiddle = nullptr, *d_freq = nullptr;
   // per-kernel event timing (fdtd_profile_*): 5 events per step
   bool profiling = false;
   std::vector<cudaEvent_t> ev_pool;

@@ -99,6 +99,8 @@ def load():
         "fdtd_launch_count": (C.c_longlong, [P]),
         "fdtd_get_status": (I, [P, C.POINTER(C.c_uint)]),
         "fdtd_get_stream": (I, [P, C.POINTER(P)]),
+        "fdtd_spectrum": (I, [P, dp]),
+        "fdtd_frequency": (I, [P, dp]),
         "fdtd_profile_enable": (I, [P, I]),
         "fdtd_profile_read": (I, [P, dp, C.POINTER(C.c_longlong)]),
         "fdtd_set_option": (I, [P, I, I]),
@@ -247,6 +249,18 @@ class Simulation:
     def eps_into(self, which: int, host_addr: int, layout: int = LAYOUT_GLOBAL):
         _check(self.lib.fdtd_get_eps(self.h, int(which), int(layout),
                                      C.cast(C.c_void_p(host_addr), C.POINTER(C.c_double))))
+
+    def spectrum(self) -> np.ndarray:
+        """|E|^2 far-field spectrum, double[321][360] (380..700 nm x angle)."""
+        out = np.empty((321, 360), dtype=np.float64)
+        _check(self.lib.fdtd_spectrum(self.h, _dptr(out)))
+        return out
+
+    def frequency(self) -> np.ndarray:
+        """Frequency-domain NTFF of the current fields (360 complex, TM)."""
+        out = np.empty(360, dtype=np.complex128)
+        _check(self.lib.fdtd_frequency(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
 
     def profile(self, on: bool = True):
         """Record CUDA events around every launch class on the engine stream."""

@@ -41,19 +41,32 @@ def run_gpu(name, precision="f64"):
     eps = [sim.eps(w) for w in range(3)]
     ntff = [sim.ntff(w) for w in range(3)]
     out = capture(fields, eps, ntff, sim.array_size, c["kind"], c.get("rows", "all"))
+    extras = c.get("extras", ())
+    if "spectrum" in extras:
+        out["spectrum"] = sim.spectrum()
+    if "frequency" in extras:
+        out["frequency"] = sim.frequency()
     out["meta_time"] = np.array(sim.time)
     return sim, out
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_gpu_fp64_matches_reference_golden(name):
+    """Fields, NTFF accumulators, and where the case has them the far-field
+    spectrum (ntff*_TimeOutput) and frequency NTFF (ntffTM_Frequency)."""
     ref = dict(np.load(GOLDEN / f"{name}.npz"))
     sim, got = run_gpu(name)
     assert float(got["meta_time"]) == float(ref["meta_time"])
     assert sim.array_size == int(ref["meta_array_size"])
-    skip = {"spectrum", "frequency"}
-    bad = compare(got, {k: v for k, v in ref.items() if k not in skip}, TOL)
+    bad = compare(got, ref, TOL)
     assert not bad, f"{name}: {bad}"
+
+
+def test_gpu_spectrum_rejects_more_than_8192_steps():
+    m = _engine()
+    sim = m.Simulation("TM_UPML", m.FieldInfo(300, 300, 5, 8, 100, 0, 9000))
+    with pytest.raises(m.FdtdError):
+        sim.spectrum()
 
 
 MODEL_CASES = ["mpi_tm_circle", "mpi_te_circle", "mpi_tm_morpho", "mpi_te_morpho_eps225", "ser_tm_circle",
