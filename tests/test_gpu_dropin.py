@@ -120,4 +120,8 @@ def test_dropin_serial_reset_writes_reference_spectrum(libs, name, tmp_path):
     assert len(txt) == 321 and txt[0].startswith("380 ")
     a = _array(_fn(upml, pre + ("getEz" if "TM" in pre else "getEx"), C.c_void_p)(), shape, np.complex128)
     assert np.all(a == 0)                                   # reset zeroes the fields
-    _fn(upml, pre + "getFinish", VOIDFN)()()
+    os.chdir(tmp_path)
+    try:
+        _fn(upml, pre + "getFinish", VOIDFN)()()            # finish() writes the spectrum again (reset first)
+    finally:
+        os.chdir(cwd)
