@@ -156,6 +156,7 @@ int fdtd_get_status(fdtd_sim *sim, unsigned int *flags);
 #define FDTD_OPT_NTFF_MODE 1     /* 0, 1 or 2 (default 2)                              */
 #define FDTD_OPT_NTFF_CHUNK 2    /* mode 1: cells of a side per block (64..4096, 1024)  */
 #define FDTD_OPT_NTFF_BLOCK 3    /* mode 2: steps per deposit (1..64, default 32)       */
+#define FDTD_OPT_ROWS 4          /* stencil rows per thread: 1 (default), 2, 4 or 8     */
 int fdtd_set_option(fdtd_sim *sim, int key, int value);
 int fdtd_get_option(fdtd_sim *sim, int key, int *value);
 

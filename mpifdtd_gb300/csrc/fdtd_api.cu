@@ -527,6 +527,10 @@ extern "C" int fdtd_set_option(fdtd_sim *s, int key, int value)
     if (value < 1 || value > kMaxNtffBlock) return fail(FDTD_E_ARG, "NTFF block must be in [1, %d]", kMaxNtffBlock);
     s->ntff_block = value;
     return FDTD_OK;
+  case FDTD_OPT_ROWS:
+    if (value != 1 && value != 2 && value != 4 && value != 8) return fail(FDTD_E_ARG, "rows must be 1, 2, 4 or 8");
+    s->rows = value;
+    return FDTD_OK;
   }
   return fail(FDTD_E_ARG, "unknown option %d", key);
 }
@@ -538,6 +542,7 @@ extern "C" int fdtd_get_option(fdtd_sim *s, int key, int *value)
   case FDTD_OPT_NTFF_MODE: *value = s->ntff_mode; return FDTD_OK;
   case FDTD_OPT_NTFF_CHUNK: *value = s->ntff_chunk; return FDTD_OK;
   case FDTD_OPT_NTFF_BLOCK: *value = s->ntff_block; return FDTD_OK;
+  case FDTD_OPT_ROWS: *value = s->rows; return FDTD_OK;
   }
   return fail(FDTD_E_ARG, "unknown option %d", key);
 }
@@ -568,6 +573,7 @@ static StencilView<R> view_of(fdtd_sim *s)
   v.in_y0 = s->in_y0;
   v.in_y1 = s->in_y1;
   v.inv_mu = (R)s->inv_mu;
+  v.rows = s->rows;
   return v;
 }
 
@@ -979,12 +985,12 @@ extern "C" int fdtd_frequency(fdtd_sim *s, double *out)
 {
   if (!s || !out) return fail(FDTD_E_ARG, "null argument");
   if (!s->tm) return fail(FDTD_E_UNSUPPORTED, "frequency-domain NTFF is provided for TM (ntffTM.c:72-158) only");
-  if (s->f32) return fail(FDTD_E_UNSUPPORTED, "frequency-domain NTFF reads FP64 fields");
   if (int rc = ensure_farfield(s)) return rc;
   FrequencyView f{};
-  f.e = (const double2 *)s->d_f[0];
-  f.h[0] = (const double2 *)s->d_f[3];
-  f.h[1] = (const double2 *)s->d_f[4];
+  f.e = s->d_f[0];
+  f.h[0] = s->d_f[3];
+  f.h[1] = s->d_f[4];
+  f.f32 = s->f32 ? 1 : 0;   // FP32 fields are widened; the transform stays FP64
   f.P = s->pitch;
   f.ox = s->ox;
   f.lt = s->geo.ntff_left;

@@ -81,6 +81,16 @@ __device__ __forceinline__ double2 cexp_i(double ph)
   return make_double2(cs, sn);
 }
 
+// complex sample of an FP64 (double2) or FP32 (float2) field, widened to FP64
+__device__ __forceinline__ double2 load_c(const void *p, long long k, int f32)
+{
+  if (f32) {
+    const float2 v = ((const float2 *)p)[k];
+    return make_double2(v.x, v.y);
+  }
+  return ((const double2 *)p)[k];
+}
+
 __global__ void __launch_bounds__(256) frequency_kernel(FrequencyView f)
 {
   __shared__ double red[6][256];
@@ -98,8 +108,9 @@ __global__ void __launch_bounds__(256) frequency_kernel(FrequencyView f)
     else { side = 3; x = f.lt; y = f.bm + (c - 2 * nb - nr); }
     const long long k = (long long)(x - f.ox) * f.P + (y - f.ox);
     const long long hoff = (side == 0 || side == 2) ? -1 : -(long long)f.P;
-    const double2 ez = f.e[k];
-    const double2 ha = f.h[side == 0 || side == 2 ? 0 : 1][k], hb = f.h[side == 0 || side == 2 ? 0 : 1][k + hoff];
+    const void *hp = f.h[side == 0 || side == 2 ? 0 : 1];
+    const double2 ez = load_c(f.e, k, f.f32);
+    const double2 ha = load_c(hp, k, f.f32), hb = load_c(hp, k + hoff, f.f32);
     const double hr = 0.5 * (ha.x + hb.x), hi = 0.5 * (ha.y + hb.y);
     const double inner = __dadd_rn(__dmul_rn(rx, (double)x - f.cx), __dmul_rn(ry, (double)y - f.cy));
     const double2 e = cexp_i(f.k_s * inner);

@@ -53,6 +53,7 @@ struct StencilView {
   const double2 *ex, *ey;       // CW source phase tables e^{i x kcos}, e^{i y ksin}
   int P, nxa, ni, nj, ox;
   int in_x0, in_x1, in_y0, in_y1;  // interior (all sigma = 0): x in [in_x0,in_x1)
+  int rows;                        // rows per thread of the stencil kernels (1, 2, 4, 8)
   R inv_mu;
 };
 
@@ -128,8 +129,9 @@ struct SpectrumView {
   double *out;             // [321][360]
 };
 struct FrequencyView {
-  const double2 *e;        // Ez (global cell (x,y) at array (x-ox)*P + (y-ox))
-  const double2 *h[2];     // Hx, Hy
+  const void *e;           // Ez (global cell (x,y) at array (x-ox)*P + (y-ox))
+  const void *h[2];        // Hx, Hy
+  int f32;                 // fields are float2 (FP32 mode) instead of double2
   int P, ox, lt, rt, bm, tp;
   double cx, cy, k_s, sqrt_hu;
   const double2 *dir;      // [360] (cos, sin)

@@ -84,166 +84,200 @@ __device__ __forceinline__ bool interior(const StencilView<R> &v, int i, int j)
 }
 
 // ------------------------------------------------------------------ TM
+//
+// Each thread owns one column j and ROWS consecutive rows i (x).  Walking the
+// rows in order lets a thread reuse the neighbour row it loaded for the
+// previous cell (Hy[k-P] of row i is Hy[k] of row i-1; Ez[k+P] of row i is
+// Ez[k] of row i+1) and gives the scheduler ROWS independent cell updates to
+// overlap with the FP64 pipe.
 
 // calcJD + calcE + scatteredWave (mpiTM_UPML.c:431-458, :337-374)
-template <typename R>
+template <typename R, int ROWS>
 __global__ void __launch_bounds__(256) tm_e_kernel(StencilView<R> v, SourceStep s)
 {
   using T = typename Cplx<R>::T;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i < 1 || i > v.ni || j < 1 || j > v.nj) return;
-  const size_t k = (size_t)i * v.P + j;
+  const int i0 = (blockIdx.y * blockDim.y + threadIdx.y) * ROWS + 1;
+  if (j < 1 || j > v.nj || i0 > v.ni) return;
   T *Ez = v.f[0], *Dz = v.f[1], *Jz = v.f[2];
   const T *Hx = v.f[3], *Hy = v.f[4];
-  const T hyk = ldro(Hy + k), hyl = ldro(Hy + k - v.P), hxk = ldro(Hx + k), hxb = ldro(Hx + k - 1);
-  T curl;
-  curl.x = ((hyk.x - hyl.x) - hxk.x) + hxb.x;
-  curl.y = ((hyk.y - hyl.y) - hxk.y) + hxb.y;
-  T dz = Dz[k];
-  if (interior(v, i, j)) {
-    dz = cadd(dz, curl);
-  } else {
-    const Coef4<R> cx = v.tx_i[i], cy = v.ty_i[j];
-    const T jz = Jz[k];
-    T jn;
-    jn.x = cx.a * jz.x + cx.b * curl.x;          // C_JZ Jz + C_JZHXHY curl
-    jn.y = cx.a * jz.y + cx.b * curl.y;
-    dz.x = (cy.a * dz.x + cy.b * jn.x) - cy.b * jz.x;   // C_DZ Dz + C_DZJZ1 Jz' - C_DZJZ0 Jz
-    dz.y = (cy.a * dz.y + cy.b * jn.y) - cy.b * jz.y;
-    Jz[k] = jn;
+  size_t k = (size_t)i0 * v.P + j;
+  T hyl = ldro(Hy + k - v.P);
+#pragma unroll
+  for (int r = 0; r < ROWS; r++, k += v.P) {
+    const int i = i0 + r;
+    if (i > v.ni) break;
+    const T hyk = ldro(Hy + k), hxk = ldro(Hx + k), hxb = ldro(Hx + k - 1);
+    T curl;
+    curl.x = ((hyk.x - hyl.x) - hxk.x) + hxb.x;
+    curl.y = ((hyk.y - hyl.y) - hxk.y) + hxb.y;
+    hyl = hyk;
+    T dz = Dz[k];
+    if (interior(v, i, j)) {
+      dz = cadd(dz, curl);
+    } else {
+      const Coef4<R> cx = v.tx_i[i], cy = v.ty_i[j];
+      const T jz = Jz[k];
+      T jn;
+      jn.x = cx.a * jz.x + cx.b * curl.x;          // C_JZ Jz + C_JZHXHY curl
+      jn.y = cx.a * jz.y + cx.b * curl.y;
+      dz.x = (cy.a * dz.x + cy.b * jn.x) - cy.b * jz.x;   // C_DZ Dz + C_DZJZ1 Jz' - C_DZJZ0 Jz
+      dz.y = (cy.a * dz.y + cy.b * jn.y) - cy.b * jz.y;
+      Jz[k] = jn;
+    }
+    Dz[k] = dz;
+    const R ie = v.inv_eps[0][k];
+    T ez = dz;
+    if (!is_one(ie)) {
+      ez = cscale(dz, ie);
+      apply_source<R>(v, s, i, j, ie, ez);
+    }
+    Ez[k] = ez;
   }
-  Dz[k] = dz;
-  const R ie = v.inv_eps[0][k];
-  T ez = dz;
-  if (!is_one(ie)) {
-    ez = cscale(dz, ie);
-    apply_source<R>(v, s, i, j, ie, ez);
-  }
-  Ez[k] = ez;
 }
 
 // calcMB + calcH (mpiTM_UPML.c:491-530)
-template <typename R>
+template <typename R, int ROWS>
 __global__ void __launch_bounds__(256) tm_h_kernel(StencilView<R> v)
 {
   using T = typename Cplx<R>::T;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i < 1 || i > v.ni || j < 1 || j > v.nj) return;
-  const size_t k = (size_t)i * v.P + j;
+  const int i0 = (blockIdx.y * blockDim.y + threadIdx.y) * ROWS + 1;
+  if (j < 1 || j > v.nj || i0 > v.ni) return;
   const T *Ez = v.f[0];
   T *Hx = v.f[3], *Hy = v.f[4], *Mx = v.f[5], *My = v.f[6];
-  const T ek = ldro(Ez + k), et = ldro(Ez + k + 1), er = ldro(Ez + k + v.P);
-  const T dEx = csub(et, ek);           // Ez[k_top] - Ez[k]
-  const T dEy = csub(ek, er);           // -Ez[k_rht] + Ez[k]
-  T hx = Hx[k], hy = Hy[k];
-  if (interior(v, i, j)) {
-    hx.x -= v.inv_mu * dEx.x; hx.y -= v.inv_mu * dEx.y;
-    hy.x -= v.inv_mu * dEy.x; hy.y -= v.inv_mu * dEy.y;
-  } else {
-    const Coef4<R> cxi = v.tx_i[i], cxh = v.tx_h[i], cyi = v.ty_i[j], cyh = v.ty_h[j];
-    const T mx = Mx[k], my = My[k];
-    T mxn, myn;
-    mxn.x = cyh.a * mx.x - cyh.b * dEx.x;        // C_MX Mx - C_MXEZ/mu0 dE
-    mxn.y = cyh.a * mx.y - cyh.b * dEx.y;
-    hx.x = (hx.x + cxi.c * mxn.x) - cxi.d * mx.x;   // C_BX(=1) H + C_BXMX1 Mx' - C_BXMX0 Mx
-    hx.y = (hx.y + cxi.c * mxn.y) - cxi.d * mx.y;
-    myn.x = my.x - v.inv_mu * dEy.x;              // C_MY(=1) My - C_MYEZ(=1)/mu0 dE
-    myn.y = my.y - v.inv_mu * dEy.y;
-    const R c1 = cyi.c * cxh.b, c0 = cyi.d * cxh.b;  // C_BYMY1, C_BYMY0
-    hy.x = (cxh.a * hy.x + c1 * myn.x) - c0 * my.x;
-    hy.y = (cxh.a * hy.y + c1 * myn.y) - c0 * my.y;
-    Mx[k] = mxn;
-    My[k] = myn;
+  size_t k = (size_t)i0 * v.P + j;
+  T ek = ldro(Ez + k);
+#pragma unroll
+  for (int r = 0; r < ROWS; r++, k += v.P) {
+    const int i = i0 + r;
+    if (i > v.ni) break;
+    const T et = ldro(Ez + k + 1), er = ldro(Ez + k + v.P);
+    const T dEx = csub(et, ek);           // Ez[k_top] - Ez[k]
+    const T dEy = csub(ek, er);           // -Ez[k_rht] + Ez[k]
+    ek = er;
+    T hx = Hx[k], hy = Hy[k];
+    if (interior(v, i, j)) {
+      hx.x -= v.inv_mu * dEx.x; hx.y -= v.inv_mu * dEx.y;
+      hy.x -= v.inv_mu * dEy.x; hy.y -= v.inv_mu * dEy.y;
+    } else {
+      const Coef4<R> cxi = v.tx_i[i], cxh = v.tx_h[i], cyi = v.ty_i[j], cyh = v.ty_h[j];
+      const T mx = Mx[k], my = My[k];
+      T mxn, myn;
+      mxn.x = cyh.a * mx.x - cyh.b * dEx.x;        // C_MX Mx - C_MXEZ/mu0 dE
+      mxn.y = cyh.a * mx.y - cyh.b * dEx.y;
+      hx.x = (hx.x + cxi.c * mxn.x) - cxi.d * mx.x;   // C_BX(=1) H + C_BXMX1 Mx' - C_BXMX0 Mx
+      hx.y = (hx.y + cxi.c * mxn.y) - cxi.d * mx.y;
+      myn.x = my.x - v.inv_mu * dEy.x;              // C_MY(=1) My - C_MYEZ(=1)/mu0 dE
+      myn.y = my.y - v.inv_mu * dEy.y;
+      const R c1 = cyi.c * cxh.b, c0 = cyi.d * cxh.b;  // C_BYMY1, C_BYMY0
+      hy.x = (cxh.a * hy.x + c1 * myn.x) - c0 * my.x;
+      hy.y = (cxh.a * hy.y + c1 * myn.y) - c0 * my.y;
+      Mx[k] = mxn;
+      My[k] = myn;
+    }
+    Hx[k] = hx;
+    Hy[k] = hy;
   }
-  Hx[k] = hx;
-  Hy[k] = hy;
 }
 
 // ------------------------------------------------------------------ TE
 
 // calcJD + calcE + scatteredWave on Ey (mpiTE_UPML.c:337-375, :250-281)
-template <typename R>
+template <typename R, int ROWS>
 __global__ void __launch_bounds__(256) te_e_kernel(StencilView<R> v, SourceStep sx, SourceStep sy)
 {
   using T = typename Cplx<R>::T;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i < 1 || i > v.ni || j < 1 || j > v.nj) return;
-  const size_t k = (size_t)i * v.P + j;
+  const int i0 = (blockIdx.y * blockDim.y + threadIdx.y) * ROWS + 1;
+  if (j < 1 || j > v.nj || i0 > v.ni) return;
   T *Ex = v.f[0], *Ey = v.f[1], *Dx = v.f[2], *Dy = v.f[3], *Jx = v.f[4], *Jy = v.f[5];
   const T *Hz = v.f[6];
-  const T hzk = ldro(Hz + k), hzb = ldro(Hz + k - 1), hzl = ldro(Hz + k - v.P);
-  const T cxv = csub(hzk, hzb);          // Hz[k] - Hz[k_btm]
-  T cyv;                                 // -Hz[k] + Hz[k_lft]
-  cyv.x = -hzk.x + hzl.x;
-  cyv.y = -hzk.y + hzl.y;
-  T dx = Dx[k], dy = Dy[k];
-  if (interior(v, i, j)) {
-    dx = cadd(dx, cxv);
-    dy = cadd(dy, cyv);
-  } else {
-    const Coef4<R> cxh = v.tx_h[i], cxi = v.tx_i[i], cyi = v.ty_i[j], cyh = v.ty_h[j];
-    const T jx = Jx[k], jy = Jy[k];
-    T jxn, jyn;
-    jxn.x = cyi.a * jx.x + cyi.b * cxv.x;         // C_JX Jx + C_JXHZ curl
-    jxn.y = cyi.a * jx.y + cyi.b * cxv.y;
-    dx.x = (dx.x + cxh.a * jxn.x) - cxh.b * jx.x;  // C_DX(=1) Dx + C_DXJX1 Jx' - C_DXJX0 Jx
-    dx.y = (dx.y + cxh.a * jxn.y) - cxh.b * jx.y;
-    jyn = cadd(jy, cyv);                          // C_JY(=1) Jy + C_JYHZ(=1) curl
-    const R c1 = cyh.c * cxi.b, c0 = cyh.d * cxi.b;  // C_DYJY1, C_DYJY0
-    dy.x = (cxi.a * dy.x + c1 * jyn.x) - c0 * jy.x;
-    dy.y = (cxi.a * dy.y + c1 * jyn.y) - c0 * jy.y;
-    Jx[k] = jxn;
-    Jy[k] = jyn;
+  size_t k = (size_t)i0 * v.P + j;
+  T hzl = ldro(Hz + k - v.P);
+#pragma unroll
+  for (int r = 0; r < ROWS; r++, k += v.P) {
+    const int i = i0 + r;
+    if (i > v.ni) break;
+    const T hzk = ldro(Hz + k), hzb = ldro(Hz + k - 1);
+    const T cxv = csub(hzk, hzb);          // Hz[k] - Hz[k_btm]
+    T cyv;                                 // -Hz[k] + Hz[k_lft]
+    cyv.x = -hzk.x + hzl.x;
+    cyv.y = -hzk.y + hzl.y;
+    hzl = hzk;
+    T dx = Dx[k], dy = Dy[k];
+    if (interior(v, i, j)) {
+      dx = cadd(dx, cxv);
+      dy = cadd(dy, cyv);
+    } else {
+      const Coef4<R> cxh = v.tx_h[i], cxi = v.tx_i[i], cyi = v.ty_i[j], cyh = v.ty_h[j];
+      const T jx = Jx[k], jy = Jy[k];
+      T jxn, jyn;
+      jxn.x = cyi.a * jx.x + cyi.b * cxv.x;         // C_JX Jx + C_JXHZ curl
+      jxn.y = cyi.a * jx.y + cyi.b * cxv.y;
+      dx.x = (dx.x + cxh.a * jxn.x) - cxh.b * jx.x;  // C_DX(=1) Dx + C_DXJX1 Jx' - C_DXJX0 Jx
+      dx.y = (dx.y + cxh.a * jxn.y) - cxh.b * jx.y;
+      jyn = cadd(jy, cyv);                          // C_JY(=1) Jy + C_JYHZ(=1) curl
+      const R c1 = cyh.c * cxi.b, c0 = cyh.d * cxi.b;  // C_DYJY1, C_DYJY0
+      dy.x = (cxi.a * dy.x + c1 * jyn.x) - c0 * jy.x;
+      dy.y = (cxi.a * dy.y + c1 * jyn.y) - c0 * jy.y;
+      Jx[k] = jxn;
+      Jy[k] = jyn;
+    }
+    Dx[k] = dx;
+    Dy[k] = dy;
+    const R iex = v.inv_eps[0][k], iey = v.inv_eps[1][k];
+    T ex = dx, ey = dy;
+    if (!is_one(iex)) {
+      ex = cscale(dx, iex);
+      if (sx.kind) apply_source<R>(v, sx, i, j, iex, ex);
+    }
+    if (!is_one(iey)) {
+      ey = cscale(dy, iey);
+      apply_source<R>(v, sy, i, j, iey, ey);
+    }
+    Ex[k] = ex;
+    Ey[k] = ey;
   }
-  Dx[k] = dx;
-  Dy[k] = dy;
-  const R iex = v.inv_eps[0][k], iey = v.inv_eps[1][k];
-  T ex = dx, ey = dy;
-  if (!is_one(iex)) {
-    ex = cscale(dx, iex);
-    if (sx.kind) apply_source<R>(v, sx, i, j, iex, ex);
-  }
-  if (!is_one(iey)) {
-    ey = cscale(dy, iey);
-    apply_source<R>(v, sy, i, j, iey, ey);
-  }
-  Ex[k] = ex;
-  Ey[k] = ey;
 }
 
 // calcMB + calcH (mpiTE_UPML.c:377-399)
-template <typename R>
+template <typename R, int ROWS>
 __global__ void __launch_bounds__(256) te_h_kernel(StencilView<R> v)
 {
   using T = typename Cplx<R>::T;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i < 1 || i > v.ni || j < 1 || j > v.nj) return;
-  const size_t k = (size_t)i * v.P + j;
+  const int i0 = (blockIdx.y * blockDim.y + threadIdx.y) * ROWS + 1;
+  if (j < 1 || j > v.nj || i0 > v.ni) return;
   const T *Ex = v.f[0], *Ey = v.f[1];
   T *Hz = v.f[6], *Mz = v.f[7];
-  const T eyr = ldro(Ey + k + v.P), eyk = ldro(Ey + k), ext = ldro(Ex + k + 1), exk = ldro(Ex + k);
-  T ce;                                  // Ey[k_rht] - Ey[k] - Ex[k_top] + Ex[k]
-  ce.x = ((eyr.x - eyk.x) - ext.x) + exk.x;
-  ce.y = ((eyr.y - eyk.y) - ext.y) + exk.y;
-  T hz = Hz[k];
-  if (interior(v, i, j)) {
-    hz.x -= v.inv_mu * ce.x;
-    hz.y -= v.inv_mu * ce.y;
-  } else {
-    const Coef4<R> cxh = v.tx_h[i], cyh = v.ty_h[j];
-    const T mz = Mz[k];
-    T mzn;
-    mzn.x = cxh.c * mz.x - cxh.d * ce.x;          // C_MZ Mz - C_MZEXEY/mu0 curl
-    mzn.y = cxh.c * mz.y - cxh.d * ce.y;
-    hz.x = (cyh.a * hz.x + cyh.b * mzn.x) - cyh.b * mz.x;   // C_BZ H + C_BZMZ1 Mz' - C_BZMZ0 Mz
-    hz.y = (cyh.a * hz.y + cyh.b * mzn.y) - cyh.b * mz.y;
-    Mz[k] = mzn;
+  size_t k = (size_t)i0 * v.P + j;
+  T eyk = ldro(Ey + k);
+#pragma unroll
+  for (int r = 0; r < ROWS; r++, k += v.P) {
+    const int i = i0 + r;
+    if (i > v.ni) break;
+    const T eyr = ldro(Ey + k + v.P), ext = ldro(Ex + k + 1), exk = ldro(Ex + k);
+    T ce;                                  // Ey[k_rht] - Ey[k] - Ex[k_top] + Ex[k]
+    ce.x = ((eyr.x - eyk.x) - ext.x) + exk.x;
+    ce.y = ((eyr.y - eyk.y) - ext.y) + exk.y;
+    eyk = eyr;
+    T hz = Hz[k];
+    if (interior(v, i, j)) {
+      hz.x -= v.inv_mu * ce.x;
+      hz.y -= v.inv_mu * ce.y;
+    } else {
+      const Coef4<R> cxh = v.tx_h[i], cyh = v.ty_h[j];
+      const T mz = Mz[k];
+      T mzn;
+      mzn.x = cxh.c * mz.x - cxh.d * ce.x;          // C_MZ Mz - C_MZEXEY/mu0 curl
+      mzn.y = cxh.c * mz.y - cxh.d * ce.y;
+      hz.x = (cyh.a * hz.x + cyh.b * mzn.x) - cyh.b * mz.x;   // C_BZ H + C_BZMZ1 Mz' - C_BZMZ0 Mz
+      hz.y = (cyh.a * hz.y + cyh.b * mzn.y) - cyh.b * mz.y;
+      Mz[k] = mzn;
+    }
+    Hz[k] = hz;
   }
-  Hz[k] = hz;
 }
 
 // ------------------------------------------------------------------ NTFF
@@ -451,34 +485,46 @@ __global__ void __launch_bounds__(256) ntff_block_kernel(NtffView n, int nb, dou
 
 // ------------------------------------------------------------------ launchers
 
+static const dim3 kBlock(32, 8);
+
+// columns 1..nj and rows 1..ni, ROWS rows per thread
 template <typename R>
-static dim3 grid_of(const StencilView<R> &v, dim3 b)
+static dim3 grid_of(const StencilView<R> &v, int rows)
 {
-  return dim3((unsigned)((v.nj + 2 + b.x - 1) / b.x), (unsigned)((v.nxa + b.y - 1) / b.y));
+  const int span = (int)kBlock.y * rows;
+  return dim3((unsigned)((v.nj + 1 + kBlock.x - 1) / kBlock.x), (unsigned)((v.ni + span - 1) / span));
 }
 
-static const dim3 kBlock(32, 8);
+// dispatch on the run-time rows-per-thread setting (1, 2, 4 or 8)
+#define ROWS_DISPATCH(KERNEL, ...)                                                                   \
+  switch (v.rows) {                                                                                \
+  case 1: KERNEL<R, 1><<<grid_of(v, 1), kBlock, 0, st>>>(__VA_ARGS__); break;                     \
+  case 2: KERNEL<R, 2><<<grid_of(v, 2), kBlock, 0, st>>>(__VA_ARGS__); break;                     \
+  case 8: KERNEL<R, 8><<<grid_of(v, 8), kBlock, 0, st>>>(__VA_ARGS__); break;                     \
+  default: KERNEL<R, 4><<<grid_of(v, 4), kBlock, 0, st>>>(__VA_ARGS__); break;                    \
+  }
 
 template <typename R>
 void launch_tm_e(const StencilView<R> &v, const SourceStep &s, cudaStream_t st)
 {
-  tm_e_kernel<R><<<grid_of(v, kBlock), kBlock, 0, st>>>(v, s);
+  ROWS_DISPATCH(tm_e_kernel, v, s)
 }
 template <typename R>
 void launch_tm_h(const StencilView<R> &v, cudaStream_t st)
 {
-  tm_h_kernel<R><<<grid_of(v, kBlock), kBlock, 0, st>>>(v);
+  ROWS_DISPATCH(tm_h_kernel, v)
 }
 template <typename R>
 void launch_te_e(const StencilView<R> &v, const SourceStep &sx, const SourceStep &sy, cudaStream_t st)
 {
-  te_e_kernel<R><<<grid_of(v, kBlock), kBlock, 0, st>>>(v, sx, sy);
+  ROWS_DISPATCH(te_e_kernel, v, sx, sy)
 }
 template <typename R>
 void launch_te_h(const StencilView<R> &v, cudaStream_t st)
 {
-  te_h_kernel<R><<<grid_of(v, kBlock), kBlock, 0, st>>>(v);
+  ROWS_DISPATCH(te_h_kernel, v)
 }
+#undef ROWS_DISPATCH
 template <typename R>
 void launch_ntff_gather(const StencilView<R> &v, const NtffView &n, double coef, int slot, cudaStream_t st)
 {

@@ -33,6 +33,7 @@ struct fdtd_sim {
   std::vector<int> h_side;       // side of each path cell (0 bottom, 1 right, 2 top, 3 left)
   // NTFF deposit: 0 direct, 1 shared window, 2 time-blocked (default)
   int ntff_mode = 2, ntff_chunk = 1024, ntff_block = 32;
+  int rows = 1;                 // stencil rows per thread (FDTD_OPT_ROWS)
   int nb_pending = 0;           // buffered steps not yet deposited (mode 2)
   double pending_t0 = 0;        // timeE of the first buffered step
   void *d_chunk = nullptr, *d_lo = nullptr;

@@ -152,6 +152,33 @@ def test_gpu_ntff_variants_agree(mode, chunk, block):
     assert sim.status == 0
 
 
+@pytest.mark.parametrize("rows", [2, 4, 8])
+@pytest.mark.parametrize("name", ["mpi_tm_discs_30deg", "mpi_te_discs_60deg", "ser_tm_circle"])
+def test_gpu_rows_per_thread_variants(name, rows):
+    """Every rows-per-thread setting of the stencil kernels gives the golden fields."""
+    m = _engine()
+    c = CASES[name]
+    ref = dict(np.load(GOLDEN / f"{name}.npz"))
+    sim = m.Simulation(c["solver"], m.FieldInfo(*c["fi"]))
+    sim.set_option(m.OPT_ROWS, rows)
+    sim.set_eps(*_eps_for(name, c))
+    sim.run(c["steps"])
+    for w in range(3):
+        assert rel(sim.field(w), ref[f"field{w}"]) <= TOL, (name, rows, w)
+
+
+def test_gpu_fp32_error_against_fp64():
+    """FP32 fields with FP64 NTFF: field relative L2 and far-field error (dB)
+    against the FP64 engine on the 1044^2 Mie case (config-2 grid, eps 2.25)."""
+    from mpifdtd_gb300.precision import compare_precisions
+    m = _engine()
+    fi = m.FieldInfo(5220, 5220, 5, 10, 500, 0, 4000)
+    rep = compare_precisions("MPI_TM_UPML", fi, (m.MODEL_CIRCLE, [500.0, 2.25]), steps=600)
+    assert rep["field_rel_l2"]["Ez"] < 1e-4, rep
+    assert rep["ntff_rel_l2"] < 1e-4, rep
+    assert rep["farfield_db_max"] < 0.01, rep
+
+
 def test_gpu_vacuum_config1_exact_zero():
     """SURVEY config 1 (276^2, vacuum, 2000 steps): every output stays exactly 0."""
     _, got = run_gpu("mpi_tm_vacuum_c1")
