@@ -157,8 +157,27 @@ int fdtd_get_status(fdtd_sim *sim, unsigned int *flags);
 #define FDTD_OPT_NTFF_CHUNK 2    /* mode 1: cells of a side per block (64..4096, 1024)  */
 #define FDTD_OPT_NTFF_BLOCK 3    /* mode 2: steps per deposit (1..64, default 32)       */
 #define FDTD_OPT_ROWS 4          /* stencil rows per thread: 1 (default), 2, 4 or 8     */
+/* Temporal blocking (MPI solvers, NTFF mode 2): fdtd_run advances K steps per
+ * pass over the fields in HBM (K = 1, 2, 4; 8 in FP32; 0 = off, the default)
+ * in tiles of 32-2K columns x FDTD_OPT_TBLOCK_ROWS rows (0 = automatic).  It
+ * holds a second set of fields on the device, and the fields move between the
+ * two sets, so a pointer from fdtd_device_field is valid until the next
+ * fdtd_run or fdtd_update.  fdtd_update (one step per call) never blocks. */
+#define FDTD_OPT_TBLOCK 5
+#define FDTD_OPT_TBLOCK_ROWS 6
 int fdtd_set_option(fdtd_sim *sim, int key, int value);
 int fdtd_get_option(fdtd_sim *sim, int key, int *value);
+
+/* Autotuner of the temporal blocking: times the one-step kernels and the
+ * blocked kernel at each depth K and tile height on this simulation's own
+ * grid and fields (into the spare field set: the state does not change),
+ * sets FDTD_OPT_TBLOCK / FDTD_OPT_TBLOCK_ROWS to the fastest and returns them
+ * with its stencil time per step in ms (*k_out = 0: one-step kernels won). */
+int fdtd_autotune(fdtd_sim *sim, int *k_out, int *rows_out, double *ms_per_step_out);
+/* The candidates the last fdtd_autotune timed: up to cap triples
+ * (K, rows, ms per step) into out, K = 0 being the one-step kernels; returns
+ * the number of candidates (negative status on error). */
+int fdtd_autotune_report(const fdtd_sim *sim, double *out, int cap);
 
 /* Per-kernel timing with CUDA events recorded on the engine's own stream
  * around every launch class while enabled.  ms_out[4] receives the summed

@@ -283,7 +283,13 @@ static int build_ntff(fdtd_sim *s)
 static void free_sim(fdtd_sim *s)
 {
   if (!s) return;
-  for (int a = 0; a < kMaxSlots; a++) cudaFree(s->d_f[a]);
+  for (int a = 0; a < kMaxSlots; a++) {
+    cudaFree(s->d_f[a]);
+    cudaFree(s->d_f2[a]);
+  }
+  cudaFree(s->d_tbcol);
+  cudaFree(s->d_tbrow);
+  cudaFree(s->d_tiles);
   for (int a = 0; a < 2; a++) { cudaFree(s->d_ieps64[a]); cudaFree(s->d_ieps32[a]); }
   for (int a = 0; a < 3; a++) cudaFree(s->d_eps[a]);
   for (int a = 0; a < 4; a++) { cudaFree(s->d_tab64[a]); cudaFree(s->d_tab32[a]); }
@@ -531,6 +537,18 @@ extern "C" int fdtd_set_option(fdtd_sim *s, int key, int value)
     if (value != 1 && value != 2 && value != 4 && value != 8) return fail(FDTD_E_ARG, "rows must be 1, 2, 4 or 8");
     s->rows = value;
     return FDTD_OK;
+  case FDTD_OPT_TBLOCK:
+    if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8)
+      return fail(FDTD_E_ARG, "temporal blocking depth must be 0, 1, 2, 4 or 8");
+    if (value == 8 && !s->f32) return fail(FDTD_E_ARG, "temporal blocking depth 8 needs FP32 fields");
+    if (value > 0 && !s->mpi)
+      return fail(FDTD_E_UNSUPPORTED, "temporal blocking needs an MPI solver (E then H half-step)");
+    s->tblock = value;
+    return FDTD_OK;
+  case FDTD_OPT_TBLOCK_ROWS:
+    if (value < 0 || value > (1 << 20)) return fail(FDTD_E_ARG, "tile rows must be in [0, 2^20]");
+    s->tb_rows = value;
+    return FDTD_OK;
   }
   return fail(FDTD_E_ARG, "unknown option %d", key);
 }
@@ -543,6 +561,8 @@ extern "C" int fdtd_get_option(fdtd_sim *s, int key, int *value)
   case FDTD_OPT_NTFF_CHUNK: *value = s->ntff_chunk; return FDTD_OK;
   case FDTD_OPT_NTFF_BLOCK: *value = s->ntff_block; return FDTD_OK;
   case FDTD_OPT_ROWS: *value = s->rows; return FDTD_OK;
+  case FDTD_OPT_TBLOCK: *value = s->tblock; return FDTD_OK;
+  case FDTD_OPT_TBLOCK_ROWS: *value = s->tb_rows; return FDTD_OK;
   }
   return fail(FDTD_E_ARG, "unknown option %d", key);
 }
@@ -707,6 +727,250 @@ static int before_step(fdtd_sim *s, double time)
   return FDTD_OK;
 }
 
+// ---------------------------------------------------------------- temporal blocking
+
+// Tile rows when FDTD_OPT_TBLOCK_ROWS is 0: the tallest power of two in
+// [16, 512] that still gives 16 tiles (warps) per SM.
+static int tb_auto_rows(const fdtd_sim *s, int K)
+{
+  const int W = 32 - 2 * K;
+  const long long nstrip = (s->nj + W - 1) / W;
+  int dev = 0, nsm = 152;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev))
+    cudaGetLastError();
+  const long long want = 16LL * nsm;
+  int L = 512;
+  while (L > 16 && nstrip * ((s->ni + L - 1) / L) < want) L >>= 1;
+  return L;
+}
+
+// The spare field set, the NTFF line buffers, and the tiles of depth K and
+// height L: an interior rectangle of strips x segments whose whole cone is
+// PML-free (x = i+ox, y = j+ox inside [in_x0,in_x1) x [in_y0,in_y1)), and the
+// work-list of every other tile.
+static int tb_prepare(fdtd_sim *s, int K, int L)
+{
+  const size_t bytes = (size_t)s->nxa * s->pitch * s->esize;
+  if (!s->d_f2[0])
+    for (int a = 0; a < s->nslots; a++) {
+      CK(cudaMalloc(&s->d_f2[a], bytes));
+      CK(cudaMemsetAsync(s->d_f2[a], 0, bytes, s->stream));
+    }
+  if (!s->d_tbcol) {
+    CK(cudaMalloc(&s->d_tbcol, (size_t)kMaxTBlock * 12 * s->nxa * s->esize));
+    CK(cudaMalloc(&s->d_tbrow, (size_t)kMaxTBlock * 12 * s->pitch * s->esize));
+  }
+  if (s->tb_built_k == K && s->tb_built_l == L) return FDTD_OK;
+  const int W = 32 - 2 * K;
+  const int nstrip = (s->nj + W - 1) / W, nseg = (s->ni + L - 1) / L;
+  if (nseg > 65535) return fail(FDTD_E_ARG, "tile rows %d: more than 65535 segments of %d rows", L, s->ni);
+  const int ilo = s->in_x0 - s->ox, ihi = s->in_x1 - s->ox;  // PML-free array rows [ilo, ihi)
+  const int jlo = s->in_y0 - s->ox, jhi = s->in_y1 - s->ox;  // PML-free array columns
+  auto strip_in = [&](int st) {  // lanes cover columns c .. c+31
+    const int c = 1 + st * W - K;
+    return c >= jlo && c + 32 <= jhi;
+  };
+  auto seg_in = [&](int g) {     // rows r0-K .. r1+K are read
+    const int r0 = 1 + g * L, r1 = std::min(r0 + L, s->ni + 1);
+    return r0 - K >= ilo && r1 + K < ihi;
+  };
+  int s0 = 0, g0 = 0;
+  while (s0 < nstrip && !strip_in(s0)) s0++;
+  int s1 = s0;
+  while (s1 < nstrip && strip_in(s1)) s1++;
+  while (g0 < nseg && !seg_in(g0)) g0++;
+  int g1 = g0;
+  while (g1 < nseg && seg_in(g1)) g1++;
+  if (s1 <= s0 || g1 <= g0) s0 = s1 = g0 = g1 = 0;
+  std::vector<int2> tiles;
+  for (int g = 0; g < nseg; g++)
+    for (int st = 0; st < nstrip; st++)
+      if (!(st >= s0 && st < s1 && g >= g0 && g < g1)) tiles.push_back(make_int2(st, g));
+  if ((int)tiles.size() > s->tiles_cap) {
+    CK(cudaStreamSynchronize(s->stream));
+    cudaFree(s->d_tiles);
+    s->d_tiles = nullptr;
+    s->tiles_cap = 0;
+    CK(cudaMalloc(&s->d_tiles, sizeof(int2) * tiles.size()));
+    s->tiles_cap = (int)tiles.size();
+  }
+  if (!tiles.empty()) {
+    CK(cudaStreamSynchronize(s->stream));  // the previous list may still be in use
+    CK(cudaMemcpy(s->d_tiles, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice));
+  }
+  s->ntiles = (int)tiles.size();
+  s->tb_s0 = s0;
+  s->tb_s1 = s1;
+  s->tb_g0 = g0;
+  s->tb_g1 = g1;
+  s->tb_L = L;
+  s->tb_built_k = K;
+  s->tb_built_l = L;
+  return FDTD_OK;
+}
+
+template <typename R>
+static TBlockView<R> tblock_view(const fdtd_sim *s, bool lines)
+{
+  using T = typename Cplx<R>::T;
+  TBlockView<R> tb{};
+  for (int a = 0; a < kMaxSlots; a++) tb.out[a] = (T *)s->d_f2[a];
+  if (lines) {
+    tb.col = (T *)s->d_tbcol;
+    tb.row = (T *)s->d_tbrow;
+  }
+  const fdtd_geometry &g = s->geo;  // the path's columns / rows and their H neighbours (build_ntff)
+  const int cj[4] = {g.ntff_bottom - 1, g.ntff_bottom, g.ntff_top - 1, g.ntff_top};
+  const int ri[4] = {g.ntff_left - 1, g.ntff_left, g.ntff_right - 1, g.ntff_right};
+  for (int q = 0; q < 4; q++) {
+    tb.cj[q] = cj[q];
+    tb.ri[q] = ri[q];
+  }
+  tb.tiles = (const int2 *)s->d_tiles;
+  tb.ntiles = s->ntiles;
+  tb.s0 = s->tb_s0;
+  tb.s1 = s->tb_s1;
+  tb.g0 = s->tb_g0;
+  tb.g1 = s->tb_g1;
+  tb.L = s->tb_L;
+  return tb;
+}
+
+// K steps of an MPI solver in one blocked launch (same clock, source and NTFF
+// samples as K calls of enqueue_step), then the fields swap sets.
+template <typename R>
+static void enqueue_block(fdtd_sim *s, int K)
+{
+  const StencilView<R> v = view_of<R>(s);
+  const NtffView n = ntff_view(s);
+  cudaStream_t st = s->stream;
+  TBlockView<R> tb = tblock_view<R>(s, true);
+  double t = s->time, rc = s->ray_coef;
+  const double t_first = t;
+  for (int l = 0; l < K; l++) {  // field.c:312-315 per step
+    const double wt = s->geo.omega_s * t;
+    tb.sc[l] = make_double2(rc * cos(wt), -rc * sin(wt));
+    t = t + 1.0;
+    rc = 1.0 - exp(-pow(0.01 * t, 2));
+  }
+  const double coef = 1.0 / (4 * M_PI * kC * 1.0e6);  // mpiTM_UPML.c:852-854
+  mark(s);
+  launch_tblock<R>(v, tb, K, s->tm, st);
+  mark(s);
+  mark(s);
+  launch_line_gather<R>(v, tb, n, coef, K, s->nb_pending, s->tm, st);
+  mark(s);
+  s->launches += (tb.s1 > tb.s0 && tb.g1 > tb.g0 ? 1 : 0) + (tb.ntiles > 0 ? 1 : 0) + 1;
+  if (s->nb_pending == 0) s->pending_t0 = t_first - 1;
+  s->nb_pending += K;
+  if (s->nb_pending == s->ntff_block) {
+    launch_ntff_block(n, s->nb_pending, s->pending_t0, st);
+    s->nb_pending = 0;
+    s->launches += 1;
+  }
+  mark(s);
+  if (s->profiling) s->prof_steps += K;
+  for (int a = 0; a < kMaxSlots; a++) std::swap(s->d_f[a], s->d_f2[a]);
+  s->time = t;
+  s->ray_coef = rc;
+}
+
+template <typename R>
+static int autotune_impl(fdtd_sim *s, int *k_out, int *rows_out, double *ms_out)
+{
+  cudaStream_t st = s->stream;
+  if (int rc = tb_prepare(s, 1, 16)) return rc;  // allocates the spare set
+  cudaEvent_t a = nullptr, b = nullptr;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  auto timed = [&](auto &&fn) -> double {  // ms per call: one warm call, then >= 3 calls and >= ~20 ms
+    fn();
+    cudaEventRecord(a, st);
+    fn();
+    cudaEventRecord(b, st);
+    cudaEventSynchronize(b);
+    float one = 0;
+    cudaEventElapsedTime(&one, a, b);
+    const int reps = std::max(3, std::min(200, (int)(20.0 / std::max(one, 1e-3f))));
+    cudaEventRecord(a, st);
+    for (int q = 0; q < reps; q++) fn();
+    cudaEventRecord(b, st);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms / reps;
+  };
+  // one-step kernels, run in place on a copy of the fields in the spare set
+  const size_t bytes = (size_t)s->nxa * s->pitch * s->esize;
+  for (int q = 0; q < s->nslots; q++) CK(cudaMemcpyAsync(s->d_f2[q], s->d_f[q], bytes, cudaMemcpyDeviceToDevice, st));
+  StencilView<R> vs = view_of<R>(s);
+  for (int q = 0; q < kMaxSlots; q++) vs.f[q] = (typename Cplx<R>::T *)s->d_f2[q];
+  SourceStep cw{};
+  cw.kind = 1;
+  cw.s_re = s->ray_coef;
+  double best = timed([&] {
+    if (s->tm) {
+      launch_tm_e<R>(vs, cw, st);
+      launch_tm_h<R>(vs, st);
+    } else {
+      launch_te_e<R>(vs, SourceStep{}, cw, st);
+      launch_te_h<R>(vs, st);
+    }
+  });
+  int best_k = 0, best_l = 0;
+  s->tune_table.assign({0.0, 0.0, best});
+  const int depths[4] = {1, 2, 4, 8};
+  for (int K : depths) {
+    if (K == 8 && !s->f32) continue;
+    for (int L = 16; L <= 512; L *= 2) {
+      if ((s->ni + L - 1) / L > 65535) continue;
+      if (int rc = tb_prepare(s, K, L)) {
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        return rc;
+      }
+      const StencilView<R> v = view_of<R>(s);  // reads the current set, writes the spare one
+      TBlockView<R> tb = tblock_view<R>(s, false);
+      tb.sc[0] = make_double2(s->ray_coef, 0.0);
+      for (int l = 1; l < K; l++) tb.sc[l] = tb.sc[0];
+      const double ms = timed([&] { launch_tblock<R>(v, tb, K, s->tm, st); }) / K;
+      s->tune_table.insert(s->tune_table.end(), {(double)K, (double)L, ms});
+      if (ms < best) {
+        best = ms;
+        best_k = K;
+        best_l = L;
+      }
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  CK(cudaGetLastError());
+  s->tblock = best_k;
+  s->tb_rows = best_l;
+  if (k_out) *k_out = best_k;
+  if (rows_out) *rows_out = best_l;
+  if (ms_out) *ms_out = best;
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_autotune(fdtd_sim *s, int *k_out, int *rows_out, double *ms_per_step_out)
+{
+  if (!s) return fail(FDTD_E_ARG, "null simulation");
+  if (!s->mpi) return fail(FDTD_E_UNSUPPORTED, "temporal blocking needs an MPI solver (E then H half-step)");
+  if (int rc = flush_ntff(s)) return rc;
+  return s->f32 ? autotune_impl<float>(s, k_out, rows_out, ms_per_step_out)
+                : autotune_impl<double>(s, k_out, rows_out, ms_per_step_out);
+}
+
+extern "C" int fdtd_autotune_report(const fdtd_sim *s, double *out, int cap)
+{
+  if (!s) return -fail(FDTD_E_ARG, "null simulation");
+  const int n = (int)(s->tune_table.size() / 3);
+  if (out)
+    for (int q = 0; q < std::min(n, cap) * 3; q++) out[q] = s->tune_table[q];
+  return n;
+}
+
 extern "C" int fdtd_profile_enable(fdtd_sim *s, int on)
 {
   if (!s) return fail(FDTD_E_ARG, "null simulation");
@@ -774,7 +1038,19 @@ extern "C" int fdtd_run(fdtd_sim *s, int n_steps)
   if (int rc = prepare_step(s)) return rc;
   if (n_steps > 0)
     if (int rc = before_step(s, s->time)) return rc;
+  const int K = s->tblock;
+  const bool blocked = K > 0 && s->mpi && s->ntff_mode == 2 && K <= s->ntff_block && n_steps >= K;
+  if (blocked)
+    if (int rc = tb_prepare(s, K, s->tb_rows > 0 ? s->tb_rows : tb_auto_rows(s, K))) return rc;
   for (int q = 0; q < n_steps; q++) {
+    if (blocked && n_steps - q >= K) {
+      if (s->nb_pending + K > s->ntff_block)
+        if (int rc = flush_ntff(s)) return rc;
+      if (s->f32) enqueue_block<float>(s, K);
+      else enqueue_block<double>(s, K);
+      q += K - 1;
+      continue;
+    }
     const double t = s->time;
     const double rc = s->ray_coef;
     if (s->f32) enqueue_step<float>(s, t, rc);

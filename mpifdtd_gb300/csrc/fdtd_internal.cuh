@@ -113,6 +113,40 @@ void launch_ntff_window(const NtffView &n, const NtffWindow &w, double timeE, do
 // Deposit nb buffered steps (slots 0..nb-1) whose first step has timeE = t0.
 void launch_ntff_block(const NtffView &n, int nb, double t0, cudaStream_t st);
 
+// ---- temporally blocked stencil (fdtd_tblock.cu)
+//
+// K steps of an MPI solver per launch.  A warp owns a tile: a strip of
+// 32 - 2K columns and a segment of L rows (strip s covers columns
+// 1 + s (32-2K) .., segment g rows 1 + g L ..).  The launch reads the field set
+// of StencilView::f and writes the set `out` (ping-pong), plus the E and H
+// samples of the NTFF lines of every level.
+constexpr int kMaxTBlock = 8;
+
+template <typename R>
+struct TBlockView {
+  typename Cplx<R>::T *out[kMaxSlots];  // destination field set
+  // NTFF line samples per level (null: none):
+  //   col[((level*4 + q)*3 + f)*nxa + i]   q-th sampled column cj[q], rows i
+  //   row[((level*4 + q)*3 + f)*P + j]     q-th sampled row ri[q], columns j
+  // f: TM 0 Ez, 1 Hx, 2 Hy ; TE 0 Ex, 1 Ey, 2 Hz
+  typename Cplx<R>::T *col, *row;
+  int cj[4], ri[4];
+  const int2 *tiles;   // (strip, segment) tiles of the general kernel
+  int ntiles;
+  int s0, s1, g0, g1;  // tiles of the interior kernel: strips [s0,s1) x segments [g0,g1)
+  int L;               // rows per segment
+  double2 sc[kMaxTBlock];  // CW source per level: ray_coef e^{-i w t}
+};
+
+// Runs the interior and the general kernel of depth K (1, 2, 4 or 8).
+template <typename R>
+void launch_tblock(const StencilView<R> &v, const TBlockView<R> &tb, int K, bool tm, cudaStream_t st);
+// vals slots slot0 .. slot0+K-1 from the NTFF line samples of a blocked launch
+// (the samples ntff_gather_kernel takes from the fields after each step).
+template <typename R>
+void launch_line_gather(const StencilView<R> &v, const TBlockView<R> &tb, const NtffView &n, double coef, int K,
+                        int slot0, bool tm, cudaStream_t st);
+
 }  // namespace fdtd
 
 #include "models_eval.h"

@@ -34,6 +34,16 @@ struct fdtd_sim {
   // NTFF deposit: 0 direct, 1 shared window, 2 time-blocked (default)
   int ntff_mode = 2, ntff_chunk = 1024, ntff_block = 32;
   int rows = 1;                 // stencil rows per thread (FDTD_OPT_ROWS)
+  // temporal blocking (MPI solvers): K steps per launch, ping-pong field sets
+  int tblock = 0;               // depth K (FDTD_OPT_TBLOCK), 0 = one launch pair per step
+  int tb_rows = 0;              // rows per tile segment (FDTD_OPT_TBLOCK_ROWS), 0 = automatic
+  void *d_f2[fdtd::kMaxSlots] = {};  // the other field set
+  void *d_tbcol = nullptr, *d_tbrow = nullptr;  // NTFF line samples of kMaxTBlock levels
+  void *d_tiles = nullptr;      // int2 (strip, segment) work-list of the general kernel
+  int ntiles = 0, tiles_cap = 0;
+  int tb_s0 = 0, tb_s1 = 0, tb_g0 = 0, tb_g1 = 0, tb_L = 0;
+  int tb_built_k = 0, tb_built_l = 0;
+  std::vector<double> tune_table;  // last fdtd_autotune: (K, rows, ms per step) per candidate
   int nb_pending = 0;           // buffered steps not yet deposited (mode 2)
   double pending_t0 = 0;        // timeE of the first buffered step
   void *d_chunk = nullptr, *d_lo = nullptr;

@@ -22,6 +22,7 @@ F64, F32 = 0, 1
 LAYOUT_GLOBAL, LAYOUT_SOLVER = 0, 1
 MODEL_NONE, MODEL_CIRCLE, MODEL_MORPHO = 0, 1, 3
 OPT_NTFF_MODE, OPT_NTFF_CHUNK, OPT_NTFF_BLOCK, OPT_ROWS = 1, 2, 3, 4
+OPT_TBLOCK, OPT_TBLOCK_ROWS = 5, 6
 
 _ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "bad state", 5: "unsupported"}
 
@@ -105,6 +106,8 @@ def load():
         "fdtd_profile_read": (I, [P, dp, C.POINTER(C.c_longlong)]),
         "fdtd_set_option": (I, [P, I, I]),
         "fdtd_get_option": (I, [P, I, C.POINTER(I)]),
+        "fdtd_autotune": (I, [P, C.POINTER(I), C.POINTER(I), dp]),
+        "fdtd_autotune_report": (I, [P, dp, I]),
         "fdtd_last_error": (C.c_char_p, []),
         "fdtd_version": (C.c_char_p, []),
     }
@@ -281,6 +284,17 @@ class Simulation:
         v = C.c_int()
         _check(self.lib.fdtd_get_option(self.h, int(key), C.byref(v)))
         return v.value
+
+    def autotune(self) -> dict:
+        """Pick the temporal-blocking depth and tile rows on this grid (the
+        fields do not change); returns them with the stencil ms per step."""
+        k, rows, ms = C.c_int(), C.c_int(), C.c_double()
+        _check(self.lib.fdtd_autotune(self.h, C.byref(k), C.byref(rows), C.byref(ms)))
+        n = self.lib.fdtd_autotune_report(self.h, None, 0)
+        table = np.zeros(3 * max(n, 0))
+        self.lib.fdtd_autotune_report(self.h, _dptr(table), n)
+        return {"tblock": k.value, "tblock_rows": rows.value, "stencil_ms_per_step": ms.value,
+                "candidates": [(int(a), int(b), float(c)) for a, b, c in table.reshape(-1, 3)]}
 
     def fill_model(self, model: int, params=()):
         p = np.ascontiguousarray(params, dtype=np.float64)
