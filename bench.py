@@ -19,6 +19,9 @@ e2e   : the same metric through the C ABI with host buffers: the permittivity
         accumulators come back device->host, all inside the timed region.
 roofline : the stencil half-step pair (E + H kernels) against the measured
         HBM copy bandwidth, with the algorithmic 200 B per FP64 TM cell-update.
+variants : the same workload with FP32 fields and FP64 NTFF, temporally
+        blocked (depth and tile rows from fdtd_autotune), and the FP32-vs-FP64
+        error (field relative L2, far-field dB) on the 1044^2 Mie cylinder.
 cpu_baseline / --impl reference : the oracle's C restatement of the reference
         (oracle/fdtd_oracle.c, the reference's own loops) on every host core,
         one independent down-scaled instance per core (the reference's own
@@ -272,6 +275,7 @@ def run_gpu_arm(args):
     # e2e through the C ABI with host buffers
     e2e = None if args.no_e2e else run_e2e(m, sim, args, torch)
     sim.close()
+    variants = None if args.no_variants else run_variants(m, args, torch, cells, t_max / args.steps)
 
     if rank == 0:
         cpu = None
@@ -289,13 +293,59 @@ def run_gpu_arm(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": workload_config(), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "clocks": clk.summary(), "gpu_launches": launches,
-            "hbm_frac": roofline["frac"],
+            "hbm_frac": roofline["frac"], "variants": variants,
         }
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
     return 0
+
+
+def run_variants(m, args, torch, cells, ms_f64):
+    """The same workload with FP32 fields (FP64 NTFF), temporal blocking picked
+    by the engine's autotuner, and the FP32-vs-FP64 error on the 1044^2 Mie
+    cylinder (field relative L2, far-field dB)."""
+    from mpifdtd_gb300.precision import compare_precisions
+    out = {}
+    sim = m.Simulation("MPI_TM_UPML", m.FieldInfo(*FIELD), "f32")
+    sim.fill_model(m.MODEL_MORPHO, morpho_params())
+    stream = torch.cuda.ExternalStream(sim.stream)
+    sim.run(args.warmup)
+    tune = sim.autotune()
+    sim.run(max(args.warmup, 2 * max(1, tune["tblock"])))
+    sim.synchronize()
+    sim.profile(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    sim.run(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    prof = sim.profile_read()
+    sim.profile(False)
+    if sim.status != 0:
+        raise RuntimeError(f"engine status {sim.status:#x}")
+    stencil = (prof["e_half"] + prof["h_half"]) / max(1, prof["steps"])
+    one_step = [c for k, _, c in tune["candidates"] if k == 0][0]
+    b_alg = B_ALG[("tm", "f32")]
+    out["fp32_tm"] = {
+        "value": cells / (ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms, "speedup_vs_fp64": ms_f64 / ms,
+        "tblock": tune["tblock"], "tblock_rows": tune["tblock_rows"], "stencil_ms_per_step": stencil,
+        "stencil_ms_per_step_one_step_kernels": one_step,
+        "stencil_alg_gbs": cells * b_alg / (stencil * 1e-3) / 1e9, "bytes_per_cell_alg": b_alg,
+        "ntff_deposit_ms_per_step": prof["ntff_deposit"] / max(1, prof["steps"]),
+        "note": "algorithmic GB/s above the HBM peak is the temporal blocking: K steps per HBM pass",
+        "autotune": [list(c) for c in tune["candidates"]],
+    }
+    sim.close()
+    fi = m.FieldInfo(5220, 5220, 5, 10, 500, 0, 4000)
+    rep = compare_precisions("MPI_TM_UPML", fi, (m.MODEL_CIRCLE, [500.0, 2.25]), steps=600)
+    out["fp32_error_vs_fp64"] = {"case": "1044^2 Mie cylinder r 500 nm eps 2.25, MPI_TM_UPML, 600 steps",
+                                 "field_rel_l2": rep["field_rel_l2"], "ntff_rel_l2": rep["ntff_rel_l2"],
+                                 "farfield_db_max": rep["farfield_db_max"]}
+    return out
 
 
 def run_e2e(m, sim, args, torch):
@@ -335,6 +385,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-variants", action="store_true", help="skip the FP32 / temporal-blocking line items")
     ap.add_argument("--grid", type=int, default=0,
                     help="interior cells per side for a smaller case of the same workload (profiling)")
     args = ap.parse_args()
