@@ -152,8 +152,10 @@ int fdtd_get_status(fdtd_sim *sim, unsigned int *flags);
  * 1 shared-memory window per side chunk, 2 time-blocked (default): the path
  * samples of FDTD_OPT_NTFF_BLOCK consecutive steps are buffered and each
  * (angle, cell) pair deposits them in one pass.  Buffered steps are deposited
- * before any NTFF read-out, fdtd_synchronize, fdtd_reset or option change. */
-#define FDTD_OPT_NTFF_MODE 1     /* 0, 1 or 2 (default 2)                              */
+ * before any NTFF read-out, fdtd_synchronize, fdtd_reset or option change.
+ * Mode 3 skips the time-domain NTFF (the accumulators stay as they are): for
+ * CW runs whose far field comes from fdtd_frequency at the end. */
+#define FDTD_OPT_NTFF_MODE 1     /* 0, 1, 2 or 3 (default 2)                           */
 #define FDTD_OPT_NTFF_CHUNK 2    /* mode 1: cells of a side per block (64..4096, 1024)  */
 #define FDTD_OPT_NTFF_BLOCK 3    /* mode 2: steps per deposit (1..64, default 32)       */
 #define FDTD_OPT_ROWS 4          /* stencil rows per thread: 1 (default), 2, 4 or 8     */
@@ -185,6 +187,29 @@ int fdtd_autotune_report(const fdtd_sim *sim, double *out, int cap);
  * *steps the number of steps timed.  Reading synchronizes and clears. */
 int fdtd_profile_enable(fdtd_sim *sim, int on);
 int fdtd_profile_read(fdtd_sim *sim, double *ms_out, long long *steps);
+
+/* ---- Batched sweeps (no counterpart in the reference; it runs one process
+ * per structure, main.c:114-138) ---------------------------------------------
+ * n independent instances of one MPI solver, each with its own fdtd_config
+ * (grid, wavelength, step_num; one precision for all), advanced together on
+ * one GPU: a packed work-list of the temporally blocked tiles of every
+ * instance, stepped by persistent kernels captured in one CUDA graph per
+ * K-step block.  Each instance is an fdtd_sim handle owned by the batch
+ * (fdtd_batch_instance): fill its permittivity and read its fields and
+ * fdtd_frequency far field with the single-simulation calls.
+ * fdtd_batch_run advances every instance from time 0 to its own step_num;
+ * the batch does no time-domain NTFF (the instances' accumulators stay zero).
+ * Options: FDTD_OPT_TBLOCK (K = 1, 2, 4 (default), 8 for FP32) and
+ * FDTD_OPT_TBLOCK_ROWS (0 = per-instance automatic). */
+typedef struct fdtd_batch fdtd_batch;
+int fdtd_batch_create(int solver, const fdtd_config *cfgs, int n, fdtd_batch **out);
+int fdtd_batch_destroy(fdtd_batch *batch);
+int fdtd_batch_size(const fdtd_batch *batch);
+int fdtd_batch_instance(fdtd_batch *batch, int index, fdtd_sim **sim);
+int fdtd_batch_set_option(fdtd_batch *batch, int key, int value);
+int fdtd_batch_run(fdtd_batch *batch);
+int fdtd_batch_reset(fdtd_batch *batch);
+long long fdtd_batch_launch_count(const fdtd_batch *batch);
 
 /* Number of kernel launches the engine issued since creation. */
 long long fdtd_launch_count(const fdtd_sim *sim);

@@ -185,6 +185,14 @@ static int build_tables(fdtd_sim *s)
   CK(cudaMemcpy(s->d_ex, ex.data(), ex.size() * sizeof(double2), cudaMemcpyHostToDevice));
   CK(cudaMalloc(&s->d_ey, ey.size() * sizeof(double2)));
   CK(cudaMemcpy(s->d_ey, ey.data(), ey.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  // FP32 copies for the FP32 stencil, which evaluates the source in FP32
+  std::vector<float2> ex32(ex.size()), ey32(ey.size());
+  for (size_t q = 0; q < ex.size(); q++) ex32[q] = make_float2((float)ex[q].x, (float)ex[q].y);
+  for (size_t q = 0; q < ey.size(); q++) ey32[q] = make_float2((float)ey[q].x, (float)ey[q].y);
+  CK(cudaMalloc(&s->d_ex32, ex32.size() * sizeof(float2)));
+  CK(cudaMemcpy(s->d_ex32, ex32.data(), ex32.size() * sizeof(float2), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&s->d_ey32, ey32.size() * sizeof(float2)));
+  CK(cudaMemcpy(s->d_ey32, ey32.data(), ey32.size() * sizeof(float2), cudaMemcpyHostToDevice));
   return FDTD_OK;
 }
 
@@ -295,6 +303,8 @@ static void free_sim(fdtd_sim *s)
   for (int a = 0; a < 4; a++) { cudaFree(s->d_tab64[a]); cudaFree(s->d_tab32[a]); }
   cudaFree(s->d_ex);
   cudaFree(s->d_ey);
+  cudaFree(s->d_ex32);
+  cudaFree(s->d_ey32);
   cudaFree(s->d_cells);
   cudaFree(s->d_shift);
   cudaFree(s->d_vals);
@@ -520,7 +530,7 @@ extern "C" int fdtd_set_option(fdtd_sim *s, int key, int value)
   if (rc) return rc;
   switch (key) {
   case FDTD_OPT_NTFF_MODE:
-    if (value < 0 || value > 2) return fail(FDTD_E_ARG, "NTFF mode must be 0, 1 or 2");
+    if (value < 0 || value > 3) return fail(FDTD_E_ARG, "NTFF mode must be 0, 1, 2 or 3");
     s->ntff_mode = value;
     return FDTD_OK;
   case FDTD_OPT_NTFF_CHUNK:
@@ -581,8 +591,9 @@ static StencilView<R> view_of(fdtd_sim *s)
   v.tx_h = (const Coef4<R> *)tab[1];
   v.ty_i = (const Coef4<R> *)tab[2];
   v.ty_h = (const Coef4<R> *)tab[3];
-  v.ex = (const double2 *)s->d_ex;
-  v.ey = (const double2 *)s->d_ey;
+  using T = typename Cplx<R>::T;
+  v.ex = (const T *)(std::is_same<R, double>::value ? s->d_ex : s->d_ex32);
+  v.ey = (const T *)(std::is_same<R, double>::value ? s->d_ey : s->d_ey32);
   v.P = s->pitch;
   v.nxa = s->nxa;
   v.ni = s->ni;
@@ -596,6 +607,14 @@ static StencilView<R> view_of(fdtd_sim *s)
   v.rows = s->rows;
   return v;
 }
+
+template <typename R>
+StencilView<R> fdtd_view_of(fdtd_sim *s)
+{
+  return view_of<R>(s);
+}
+template StencilView<double> fdtd_view_of<double>(fdtd_sim *);
+template StencilView<float> fdtd_view_of<float>(fdtd_sim *);
 
 static NtffView ntff_view(fdtd_sim *s)
 {
@@ -685,10 +704,17 @@ static void enqueue_step(fdtd_sim *s, double time, double ray_coef)
     launch_te_e<R>(v, sx, sy, st);
   }
   mark(s);
+  s->launches += 2;
+  if (s->ntff_mode == 3) {  // no time-domain NTFF
+    mark(s);
+    mark(s);
+    if (s->profiling) s->prof_steps++;
+    return;
+  }
   const bool blocked = s->ntff_mode == 2;
   launch_ntff_gather<R>(v, n, coef, blocked ? s->nb_pending : 0, st);
   mark(s);
-  s->launches += 3;
+  s->launches += 1;
   if (blocked) {
     if (s->nb_pending++ == 0) s->pending_t0 = time - 1;
     if (s->nb_pending == s->ntff_block) {
@@ -744,10 +770,57 @@ static int tb_auto_rows(const fdtd_sim *s, int K)
   return L;
 }
 
+// Tiles of depth K (strip s: columns 1 + s(32-2K) .., 32 lanes from K columns
+// left of it).  A tile whose cone -- rows r0-K .. r1+K, its 32 lane columns --
+// is PML-free (x = i+ox, y = j+ox inside [in_x0,in_x1) x [in_y0,in_y1)) runs
+// the interior kernel: strips [s0, s1) x rows [ra, rb) in segments of L rows.
+// Everything else is a work-list tile: the row bands above ra and below rb
+// (thin: the PML rows and K more), and the strips outside [s0, s1).
+int fdtd_plan_tiles(const fdtd_sim *s, int K, int L, TilePlan *plan)
+{
+  const int W = 32 - 2 * K;
+  const int nstrip = (s->nj + W - 1) / W;
+  const int ilo = s->in_x0 - s->ox, ihi = s->in_x1 - s->ox;  // PML-free array rows [ilo, ihi)
+  const int jlo = s->in_y0 - s->ox, jhi = s->in_y1 - s->ox;  // PML-free array columns
+  auto strip_in = [&](int st) {
+    const int c = 1 + st * W - K;
+    return c >= jlo && c + 32 <= jhi;
+  };
+  int s0 = 0;
+  while (s0 < nstrip && !strip_in(s0)) s0++;
+  int s1 = s0;
+  while (s1 < nstrip && strip_in(s1)) s1++;
+  int ra = std::max(1, ilo + K), rb = std::min(s->ni + 1, ihi - 1 - K);  // r0 - K >= ilo, r1 + K < ihi
+  if (rb <= ra || s1 <= s0) {
+    ra = rb = 1;
+    s0 = s1 = 0;
+  }
+  const int nseg = rb > ra ? (rb - ra + L - 1) / L : 0;
+  if (nseg > 65535) return fail(FDTD_E_ARG, "tile rows %d: more than 65535 segments of %d rows", L, rb - ra);
+  plan->s0 = s0;
+  plan->s1 = s1;
+  plan->ra = ra;
+  plan->rb = rb;
+  plan->L = L;
+  plan->nseg = nseg;
+  std::vector<int4> &gen = plan->general;
+  gen.clear();
+  auto band = [&](int r_lo, int r_hi) {  // all strips, rows [r_lo, r_hi) in chunks of at most L rows
+    for (int r0 = r_lo; r0 < r_hi; r0 += L)
+      for (int st = 0; st < nstrip; st++) gen.push_back(make_int4(st, r0, std::min(r0 + L, r_hi), 0));
+  };
+  band(1, ra);
+  for (int g = 0; g < nseg; g++) {
+    const int r0 = ra + g * L, r1 = std::min(r0 + L, rb);
+    for (int st = 0; st < nstrip; st++)
+      if (st < s0 || st >= s1) gen.push_back(make_int4(st, r0, r1, 0));
+  }
+  band(rb, s->ni + 1);
+  return FDTD_OK;
+}
+
 // The spare field set, the NTFF line buffers, and the tiles of depth K and
-// height L: an interior rectangle of strips x segments whose whole cone is
-// PML-free (x = i+ox, y = j+ox inside [in_x0,in_x1) x [in_y0,in_y1)), and the
-// work-list of every other tile.
+// height L (fdtd_plan_tiles) on the device.
 static int tb_prepare(fdtd_sim *s, int K, int L)
 {
   const size_t bytes = (size_t)s->nxa * s->pitch * s->esize;
@@ -761,48 +834,27 @@ static int tb_prepare(fdtd_sim *s, int K, int L)
     CK(cudaMalloc(&s->d_tbrow, (size_t)kMaxTBlock * 12 * s->pitch * s->esize));
   }
   if (s->tb_built_k == K && s->tb_built_l == L) return FDTD_OK;
-  const int W = 32 - 2 * K;
-  const int nstrip = (s->nj + W - 1) / W, nseg = (s->ni + L - 1) / L;
-  if (nseg > 65535) return fail(FDTD_E_ARG, "tile rows %d: more than 65535 segments of %d rows", L, s->ni);
-  const int ilo = s->in_x0 - s->ox, ihi = s->in_x1 - s->ox;  // PML-free array rows [ilo, ihi)
-  const int jlo = s->in_y0 - s->ox, jhi = s->in_y1 - s->ox;  // PML-free array columns
-  auto strip_in = [&](int st) {  // lanes cover columns c .. c+31
-    const int c = 1 + st * W - K;
-    return c >= jlo && c + 32 <= jhi;
-  };
-  auto seg_in = [&](int g) {     // rows r0-K .. r1+K are read
-    const int r0 = 1 + g * L, r1 = std::min(r0 + L, s->ni + 1);
-    return r0 - K >= ilo && r1 + K < ihi;
-  };
-  int s0 = 0, g0 = 0;
-  while (s0 < nstrip && !strip_in(s0)) s0++;
-  int s1 = s0;
-  while (s1 < nstrip && strip_in(s1)) s1++;
-  while (g0 < nseg && !seg_in(g0)) g0++;
-  int g1 = g0;
-  while (g1 < nseg && seg_in(g1)) g1++;
-  if (s1 <= s0 || g1 <= g0) s0 = s1 = g0 = g1 = 0;
-  std::vector<int2> tiles;
-  for (int g = 0; g < nseg; g++)
-    for (int st = 0; st < nstrip; st++)
-      if (!(st >= s0 && st < s1 && g >= g0 && g < g1)) tiles.push_back(make_int2(st, g));
+  TilePlan plan;
+  if (int rc = fdtd_plan_tiles(s, K, L, &plan)) return rc;
+  const std::vector<int4> &tiles = plan.general;
   if ((int)tiles.size() > s->tiles_cap) {
     CK(cudaStreamSynchronize(s->stream));
     cudaFree(s->d_tiles);
     s->d_tiles = nullptr;
     s->tiles_cap = 0;
-    CK(cudaMalloc(&s->d_tiles, sizeof(int2) * tiles.size()));
+    CK(cudaMalloc(&s->d_tiles, sizeof(int4) * tiles.size()));
     s->tiles_cap = (int)tiles.size();
   }
   if (!tiles.empty()) {
     CK(cudaStreamSynchronize(s->stream));  // the previous list may still be in use
-    CK(cudaMemcpy(s->d_tiles, tiles.data(), sizeof(int2) * tiles.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(s->d_tiles, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice));
   }
   s->ntiles = (int)tiles.size();
-  s->tb_s0 = s0;
-  s->tb_s1 = s1;
-  s->tb_g0 = g0;
-  s->tb_g1 = g1;
+  s->tb_s0 = plan.s0;
+  s->tb_s1 = plan.s1;
+  s->tb_ra = plan.ra;
+  s->tb_rb = plan.rb;
+  s->tb_nseg = plan.nseg;
   s->tb_L = L;
   s->tb_built_k = K;
   s->tb_built_l = L;
@@ -826,12 +878,13 @@ static TBlockView<R> tblock_view(const fdtd_sim *s, bool lines)
     tb.cj[q] = cj[q];
     tb.ri[q] = ri[q];
   }
-  tb.tiles = (const int2 *)s->d_tiles;
+  tb.tiles = (const int4 *)s->d_tiles;
   tb.ntiles = s->ntiles;
   tb.s0 = s->tb_s0;
   tb.s1 = s->tb_s1;
-  tb.g0 = s->tb_g0;
-  tb.g1 = s->tb_g1;
+  tb.ra = s->tb_ra;
+  tb.rb = s->tb_rb;
+  tb.nseg = s->tb_nseg;
   tb.L = s->tb_L;
   return tb;
 }
@@ -844,7 +897,8 @@ static void enqueue_block(fdtd_sim *s, int K)
   const StencilView<R> v = view_of<R>(s);
   const NtffView n = ntff_view(s);
   cudaStream_t st = s->stream;
-  TBlockView<R> tb = tblock_view<R>(s, true);
+  const bool lines = s->ntff_mode == 2;  // mode 3: no time-domain NTFF
+  TBlockView<R> tb = tblock_view<R>(s, lines);
   double t = s->time, rc = s->ray_coef;
   const double t_first = t;
   for (int l = 0; l < K; l++) {  // field.c:312-315 per step
@@ -858,12 +912,15 @@ static void enqueue_block(fdtd_sim *s, int K)
   launch_tblock<R>(v, tb, K, s->tm, st);
   mark(s);
   mark(s);
-  launch_line_gather<R>(v, tb, n, coef, K, s->nb_pending, s->tm, st);
+  s->launches += (tb.s1 > tb.s0 && tb.nseg > 0 ? 1 : 0) + (tb.ntiles > 0 ? 1 : 0);
+  if (lines) {
+    launch_line_gather<R>(v, tb, n, coef, K, s->nb_pending, s->tm, st);
+    s->launches += 1;
+    if (s->nb_pending == 0) s->pending_t0 = t_first - 1;
+    s->nb_pending += K;
+  }
   mark(s);
-  s->launches += (tb.s1 > tb.s0 && tb.g1 > tb.g0 ? 1 : 0) + (tb.ntiles > 0 ? 1 : 0) + 1;
-  if (s->nb_pending == 0) s->pending_t0 = t_first - 1;
-  s->nb_pending += K;
-  if (s->nb_pending == s->ntff_block) {
+  if (lines && s->nb_pending == s->ntff_block) {
     launch_ntff_block(n, s->nb_pending, s->pending_t0, st);
     s->nb_pending = 0;
     s->launches += 1;
@@ -1039,7 +1096,8 @@ extern "C" int fdtd_run(fdtd_sim *s, int n_steps)
   if (n_steps > 0)
     if (int rc = before_step(s, s->time)) return rc;
   const int K = s->tblock;
-  const bool blocked = K > 0 && s->mpi && s->ntff_mode == 2 && K <= s->ntff_block && n_steps >= K;
+  const bool blocked = K > 0 && s->mpi && (s->ntff_mode == 3 || (s->ntff_mode == 2 && K <= s->ntff_block)) &&
+                       n_steps >= K;
   if (blocked)
     if (int rc = tb_prepare(s, K, s->tb_rows > 0 ? s->tb_rows : tb_auto_rows(s, K))) return rc;
   for (int q = 0; q < n_steps; q++) {

@@ -1,0 +1,431 @@
+// fdtd_batch.cu -- many independent simulations advanced together: a sweep of
+// scatterer / wavelength instances of one MPI solver with uneven grids and
+// step counts (the task parallelism the reference gets from one process per
+// structure, main.c:114-138, on one GPU).
+//
+// Every instance is an ordinary fdtd_sim (own fields, tables and
+// permittivity; the caller fills and reads it through the fdtd_* calls).  The
+// batch adds each instance's spare field set, a device clock, and two packed
+// work-lists of (instance, strip, segment) tiles over all instances -- the
+// PML-free interior tiles and the others -- for the temporally blocked tile
+// code (tblock_tile.cuh).  One K-step block is four launches:
+//   source  : ray_coef e^{-i w t} of every instance at the block's K times
+//   interior: persistent kernel striding over the interior work-list
+//   general : persistent kernel striding over the other tiles (on a second
+//             stream forked and joined inside the graph: runs beside interior)
+//   clock   : t += K, set parity flips
+// captured once in a CUDA graph and replayed until the instance with the
+// largest step_num has finished.  An instance whose step_num ends inside a
+// block freezes its remaining levels; a finished one is skipped, so its
+// fields stay in the set of its last block.  The batch does no time-domain
+// NTFF: the far field of a CW instance is fdtd_frequency (ntffTM_Frequency)
+// of its final fields.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <new>
+#include <vector>
+
+#include "fdtd_internal.cuh"
+#include "fdtd_sim.h"
+#include "stencil_ops.cuh"
+#include "tblock_tile.cuh"
+
+namespace fdtd {
+
+namespace {
+
+struct BatchClock {
+  double t;  // engine time of the block's first step
+  int q;     // blocks run so far (field-set parity)
+  int pad;
+};
+
+// Per instance and per field-set parity p (blocks q with q % 2 == p): the
+// view reading set p and the blocked view writing the other set; the source
+// kernel stores the block's per-level source values into tb[p].sc.
+template <typename R>
+struct BatchInst {
+  StencilView<R> v[2];
+  TBlockView<R> tb[2];
+  int n_steps;
+};
+
+constexpr int kBWarps = 4;
+
+template <typename R>
+__global__ void batch_source_kernel(BatchInst<R> *inst, const double *omega, int n, int K, const BatchClock *clk)
+{
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= n * K) return;
+  const int i = id / K, l = id - i * K;
+  const double t = clk->t + l;
+  const double rc = 1.0 - exp(-pow(0.01 * t, 2.0));  // field.c:312-315
+  double sn, cs;
+  sincos(omega[i] * t, &sn, &cs);
+  inst[i].tb[clk->q & 1].sc[l] = make_double2(rc * cs, -rc * sn);
+}
+
+__global__ void batch_clock_kernel(BatchClock *clk, int K)
+{
+  clk->t += K;
+  clk->q += 1;
+}
+
+template <typename R, int K> constexpr int batch_min_blocks() { return sizeof(R) * K > 16 ? 3 : 4; }
+
+template <typename R, int K, bool AUX, bool TM>
+__global__ void __launch_bounds__(32 * kBWarps, (AUX ? 2 : batch_min_blocks<R, K>()))
+    batch_tile_kernel(const BatchInst<R> *__restrict__ inst, const int4 *__restrict__ tiles, int ntiles,
+                      const BatchClock *__restrict__ clk)
+{
+  const double t = clk->t;
+  const int p = clk->q & 1;
+  const int nw = (int)gridDim.x * kBWarps;
+  for (int w = (int)blockIdx.x * kBWarps + (int)(threadIdx.x >> 5); w < ntiles; w += nw) {
+    const int4 tl = tiles[w];
+    const BatchInst<R> &I = inst[tl.x];
+    const int left = I.n_steps - (int)t;
+    if (left <= 0) continue;  // finished instance (whole warp)
+    const int nlev = left < K ? left : K;
+    if (TM) tile::tm_tile<R, K, AUX>(I.v[p], I.tb[p], tl.y, tl.z, tl.w, nlev);
+    else tile::te_tile<R, K, AUX>(I.v[p], I.tb[p], tl.y, tl.z, tl.w, nlev);
+  }
+}
+
+template <typename R, int K, bool AUX, bool TM>
+int persistent_grid(int ntiles)
+{
+  int dev = 0, nsm = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_tile_kernel<R, K, AUX, TM>, 32 * kBWarps, 0);
+  cudaGetLastError();
+  const int want = (ntiles + kBWarps - 1) / kBWarps;
+  return std::max(1, std::min(want, std::max(1, nsm) * std::max(1, per)));
+}
+
+}  // namespace
+
+}  // namespace fdtd
+
+using namespace fdtd;
+
+struct fdtd_batch {
+  int solver = 0;
+  bool tm = false, f32 = false;
+  int K = 4, L = 0;
+  std::vector<fdtd_sim *> sims;
+  cudaStream_t stream = nullptr, stream2 = nullptr;  // stream2: the work-list kernel, forked in the graph
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  void *d_inst = nullptr, *d_tint = nullptr, *d_tgen = nullptr, *d_clock = nullptr, *d_omega = nullptr;
+  int n_int = 0, n_gen = 0, grid_int = 0, grid_gen = 0;
+  int planned_k = 0, planned_l = -1;
+  std::vector<int> rows;  // tile rows of each instance
+  cudaGraphExec_t graph = nullptr;
+  int graph_blocks = 0;
+  long long launches = 0;
+};
+
+static void batch_free(fdtd_batch *b)
+{
+  if (!b) return;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  for (fdtd_sim *s : b->sims) fdtd_destroy(s);
+  cudaFree(b->d_inst);
+  cudaFree(b->d_tint);
+  cudaFree(b->d_tgen);
+  cudaFree(b->d_clock);
+  cudaFree(b->d_omega);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  if (b->ev_join) cudaEventDestroy(b->ev_join);
+  if (b->stream2) cudaStreamDestroy(b->stream2);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+#define BCK(x)                                                                                     \
+  do {                                                                                             \
+    cudaError_t e_ = (x);                                                                          \
+    if (e_ != cudaSuccess) {                                                                       \
+      cudaGetLastError();                                                                          \
+      return set_error(FDTD_E_CUDA, "%s: %s", #x, cudaGetErrorString(e_));                        \
+    }                                                                                              \
+  } while (0)
+
+extern "C" int fdtd_batch_create(int solver, const fdtd_config *cfgs, int n, fdtd_batch **out)
+{
+  if (!cfgs || !out || n <= 0) return set_error(FDTD_E_ARG, "bad batch arguments");
+  *out = nullptr;
+  if (solver != FDTD_MPI_TM_UPML && solver != FDTD_MPI_TE_UPML)
+    return set_error(FDTD_E_UNSUPPORTED, "a batch runs an MPI solver (E then H half-step)");
+  for (int i = 1; i < n; i++)
+    if (cfgs[i].precision != cfgs[0].precision) return set_error(FDTD_E_ARG, "instances differ in precision");
+  fdtd_batch *b = new (std::nothrow) fdtd_batch();
+  if (!b) return set_error(FDTD_E_NOMEM, "host allocation failed");
+  b->solver = solver;
+  b->tm = solver == FDTD_MPI_TM_UPML;
+  b->f32 = cfgs[0].precision == FDTD_F32;
+  for (int i = 0; i < n; i++) {
+    fdtd_sim *s = nullptr;
+    if (int rc = fdtd_create(solver, &cfgs[i], &s)) {
+      batch_free(b);
+      return rc;
+    }
+    b->sims.push_back(s);
+  }
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    batch_free(b);
+    return set_error(FDTD_E_CUDA, "stream / event creation failed");
+  }
+  *out = b;
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_batch_destroy(fdtd_batch *b)
+{
+  batch_free(b);
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_batch_size(const fdtd_batch *b) { return b ? (int)b->sims.size() : 0; }
+
+extern "C" int fdtd_batch_instance(fdtd_batch *b, int index, fdtd_sim **sim)
+{
+  if (!b || !sim || index < 0 || index >= (int)b->sims.size()) return set_error(FDTD_E_ARG, "bad instance index");
+  *sim = b->sims[index];
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_batch_set_option(fdtd_batch *b, int key, int value)
+{
+  if (!b) return set_error(FDTD_E_ARG, "null batch");
+  switch (key) {
+  case FDTD_OPT_TBLOCK:
+    if (value != 1 && value != 2 && value != 4 && value != 8)
+      return set_error(FDTD_E_ARG, "batch blocking depth must be 1, 2, 4 or 8");
+    if (value == 8 && !b->f32) return set_error(FDTD_E_ARG, "blocking depth 8 needs FP32 fields");
+    b->K = value;
+    return FDTD_OK;
+  case FDTD_OPT_TBLOCK_ROWS:
+    if (value < 0 || value > (1 << 20)) return set_error(FDTD_E_ARG, "tile rows must be in [0, 2^20]");
+    b->L = value;
+    return FDTD_OK;
+  }
+  return set_error(FDTD_E_ARG, "unknown batch option %d", key);
+}
+
+extern "C" long long fdtd_batch_launch_count(const fdtd_batch *b) { return b ? b->launches : 0; }
+
+// rows per interior tile segment of one instance (the work-list over all
+// instances provides the parallelism; the PML bands get their own thin tiles)
+static int batch_rows(const fdtd_batch *b, const fdtd_sim *s)
+{
+  if (b->L > 0) return b->L;
+  return std::max(16, std::min(128, s->ni / 4 + 1));
+}
+
+// Instance descriptors from the current field sets (fdtd_batch_run swaps an
+// instance's sets after a run, so they are rebuilt before every run).
+template <typename R>
+static int batch_descriptors(fdtd_batch *b)
+{
+  const int n = (int)b->sims.size();
+  std::vector<BatchInst<R>> inst(n);
+  for (int i = 0; i < n; i++) {
+    fdtd_sim *s = b->sims[i];
+    BatchInst<R> &I = inst[i];
+    I = BatchInst<R>{};
+    I.v[0] = fdtd_view_of<R>(s);  // reads set A (the current d_f): blocks of even parity
+    I.v[1] = I.v[0];
+    for (int a = 0; a < kMaxSlots; a++) {
+      I.v[1].f[a] = (typename Cplx<R>::T *)s->d_f2[a];
+      I.tb[0].out[a] = I.v[1].f[a];
+      I.tb[1].out[a] = I.v[0].f[a];
+    }
+    for (int p = 0; p < 2; p++) I.tb[p].L = b->rows[i];  // no NTFF lines (col/row null)
+    I.n_steps = s->cfg.step_num;
+  }
+  BCK(cudaMemcpyAsync(b->d_inst, inst.data(), sizeof(BatchInst<R>) * n, cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));  // inst is a host temporary
+  return FDTD_OK;
+}
+
+// Spare field sets, tile work-lists and device buffers for depth K.
+template <typename R>
+static int batch_plan(fdtd_batch *b)
+{
+  const int K = b->K, n = (int)b->sims.size();
+  std::vector<int4> tint, tgen;
+  std::vector<double> omega(n);
+  b->rows.assign(n, 0);
+  for (int i = 0; i < n; i++) {
+    fdtd_sim *s = b->sims[i];
+    const size_t bytes = (size_t)s->nxa * s->pitch * s->esize;
+    if (!s->d_f2[0])
+      for (int a = 0; a < s->nslots; a++) {
+        BCK(cudaMalloc(&s->d_f2[a], bytes));
+        BCK(cudaMemsetAsync(s->d_f2[a], 0, bytes, s->stream));
+      }
+    const int L = batch_rows(b, s);
+    TilePlan plan;
+    if (int rc = fdtd_plan_tiles(s, K, L, &plan)) return rc;
+    for (int g = 0; g < plan.nseg; g++) {
+      const int r0 = plan.ra + g * L, r1 = std::min(r0 + L, plan.rb);
+      for (int st = plan.s0; st < plan.s1; st++) tint.push_back(make_int4(i, st, r0, r1));
+    }
+    for (const int4 &t : plan.general) tgen.push_back(make_int4(i, t.x, t.y, t.z));
+    b->rows[i] = L;
+    omega[i] = s->geo.omega_s;
+  }
+  for (fdtd_sim *s : b->sims) BCK(cudaStreamSynchronize(s->stream));
+  cudaFree(b->d_inst);
+  cudaFree(b->d_tint);
+  cudaFree(b->d_tgen);
+  cudaFree(b->d_omega);
+  b->d_inst = b->d_tint = b->d_tgen = b->d_omega = nullptr;
+  BCK(cudaMalloc(&b->d_inst, sizeof(BatchInst<R>) * n));
+  BCK(cudaMalloc(&b->d_tint, sizeof(int4) * std::max<size_t>(1, tint.size())));
+  BCK(cudaMalloc(&b->d_tgen, sizeof(int4) * std::max<size_t>(1, tgen.size())));
+  if (!tint.empty()) BCK(cudaMemcpy(b->d_tint, tint.data(), sizeof(int4) * tint.size(), cudaMemcpyHostToDevice));
+  if (!tgen.empty()) BCK(cudaMemcpy(b->d_tgen, tgen.data(), sizeof(int4) * tgen.size(), cudaMemcpyHostToDevice));
+  BCK(cudaMalloc(&b->d_omega, sizeof(double) * n));
+  BCK(cudaMemcpy(b->d_omega, omega.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+  if (!b->d_clock) BCK(cudaMalloc(&b->d_clock, sizeof(BatchClock)));
+  b->n_int = (int)tint.size();
+  b->n_gen = (int)tgen.size();
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  b->planned_k = K;
+  b->planned_l = b->L;
+  return FDTD_OK;
+}
+
+template <typename R, int K, bool TM>
+static void batch_block(fdtd_batch *b)
+{
+  cudaStream_t st = b->stream;
+  const int n = (int)b->sims.size();
+  auto *inst = (BatchInst<R> *)b->d_inst;
+  const auto *clk = (BatchClock *)b->d_clock;
+  batch_source_kernel<R><<<(n * K + 127) / 128, 128, 0, st>>>(inst, (const double *)b->d_omega, n, K, clk);
+  // the two tile kernels run side by side (fork onto the second stream, join)
+  cudaEventRecord(b->ev_fork, st);
+  cudaStreamWaitEvent(b->stream2, b->ev_fork, 0);
+  if (b->n_gen > 0)
+    batch_tile_kernel<R, K, true, TM><<<b->grid_gen, 32 * kBWarps, 0, b->stream2>>>(
+        inst, (const int4 *)b->d_tgen, b->n_gen, clk);
+  cudaEventRecord(b->ev_join, b->stream2);
+  if (b->n_int > 0)
+    batch_tile_kernel<R, K, false, TM><<<b->grid_int, 32 * kBWarps, 0, st>>>(inst, (const int4 *)b->d_tint,
+                                                                             b->n_int, clk);
+  cudaStreamWaitEvent(st, b->ev_join, 0);
+  batch_clock_kernel<<<1, 1, 0, st>>>((BatchClock *)b->d_clock, K);
+}
+
+// persistent grid sizes (resident blocks on every SM, at most one warp per tile)
+template <typename R, int K, bool TM>
+static void batch_grids(fdtd_batch *b)
+{
+  b->grid_int = persistent_grid<R, K, false, TM>(b->n_int);
+  b->grid_gen = persistent_grid<R, K, true, TM>(b->n_gen);
+}
+
+template <typename R>
+static void batch_grids_any(fdtd_batch *b)
+{
+  switch (b->K) {
+  case 1: b->tm ? batch_grids<R, 1, true>(b) : batch_grids<R, 1, false>(b); break;
+  case 2: b->tm ? batch_grids<R, 2, true>(b) : batch_grids<R, 2, false>(b); break;
+  case 4: b->tm ? batch_grids<R, 4, true>(b) : batch_grids<R, 4, false>(b); break;
+  default:
+    if (sizeof(R) == 4) b->tm ? batch_grids<R, sizeof(R) == 4 ? 8 : 4, true>(b) : batch_grids<R, sizeof(R) == 4 ? 8 : 4, false>(b);
+    break;
+  }
+}
+
+template <typename R>
+static void batch_block_any(fdtd_batch *b)
+{
+  switch (b->K) {
+  case 1: b->tm ? batch_block<R, 1, true>(b) : batch_block<R, 1, false>(b); break;
+  case 2: b->tm ? batch_block<R, 2, true>(b) : batch_block<R, 2, false>(b); break;
+  case 4: b->tm ? batch_block<R, 4, true>(b) : batch_block<R, 4, false>(b); break;
+  default:  // 8: FP32 only (checked by fdtd_batch_set_option)
+    if (sizeof(R) == 4) b->tm ? batch_block<R, sizeof(R) == 4 ? 8 : 4, true>(b) : batch_block<R, sizeof(R) == 4 ? 8 : 4, false>(b);
+    break;
+  }
+}
+
+// blocks per graph replay
+static const int kGraphBlocks = 4;
+
+extern "C" int fdtd_batch_run(fdtd_batch *b)
+{
+  if (!b) return set_error(FDTD_E_ARG, "null batch");
+  int max_n = 0;
+  for (fdtd_sim *s : b->sims) {
+    if (s->time != 0) return set_error(FDTD_E_STATE, "batch_run starts every instance at time 0 (fdtd_reset)");
+    max_n = std::max(max_n, s->cfg.step_num);
+  }
+  if (b->planned_k != b->K || b->planned_l != b->L) {
+    if (int rc = b->f32 ? batch_plan<float>(b) : batch_plan<double>(b)) return rc;
+    if (b->f32) batch_grids_any<float>(b);
+    else batch_grids_any<double>(b);
+  }
+  for (fdtd_sim *s : b->sims) BCK(cudaStreamSynchronize(s->stream));
+  if (int rc = b->f32 ? batch_descriptors<float>(b) : batch_descriptors<double>(b)) return rc;
+  BatchClock c0{0.0, 0, 0};
+  BCK(cudaMemcpyAsync(b->d_clock, &c0, sizeof c0, cudaMemcpyHostToDevice, b->stream));
+  if (!b->graph) {
+    cudaGraph_t g = nullptr;
+    BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    for (int q = 0; q < kGraphBlocks; q++) {
+      if (b->f32) batch_block_any<float>(b);
+      else batch_block_any<double>(b);
+    }
+    const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+    if (ce != cudaSuccess) {
+      cudaGetLastError();
+      return set_error(FDTD_E_CUDA, "graph capture failed: %s", cudaGetErrorString(ce));
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+      cudaGetLastError();
+      b->graph = nullptr;
+      return set_error(FDTD_E_CUDA, "graph instantiate failed: %s", cudaGetErrorString(ie));
+    }
+    b->graph_blocks = kGraphBlocks;
+  }
+  const int nblocks = (max_n + b->K - 1) / b->K;
+  const int reps = (nblocks + b->graph_blocks - 1) / b->graph_blocks;
+  const int per_block = 2 + (b->n_int > 0) + (b->n_gen > 0);
+  for (int r = 0; r < reps; r++) BCK(cudaGraphLaunch(b->graph, b->stream));
+  b->launches += (long long)reps * b->graph_blocks * per_block;
+  BCK(cudaStreamSynchronize(b->stream));
+  for (fdtd_sim *s : b->sims) {  // the fields of instance i are in the set its last block wrote
+    const int blocks = (s->cfg.step_num + b->K - 1) / b->K;
+    if (blocks & 1)
+      for (int a = 0; a < kMaxSlots; a++) std::swap(s->d_f[a], s->d_f2[a]);
+    s->time = s->cfg.step_num;
+    s->ray_coef = 1.0 - exp(-pow(0.01 * s->time, 2));
+  }
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_batch_reset(fdtd_batch *b)
+{
+  if (!b) return set_error(FDTD_E_ARG, "null batch");
+  for (fdtd_sim *s : b->sims)
+    if (int rc = fdtd_reset(s)) return rc;
+  return FDTD_OK;
+}

@@ -50,7 +50,7 @@ struct StencilView {
   const R *inv_eps[2];          // TM: [0] 1/EPS_EZ ; TE: [0] 1/EPS_EX, [1] 1/EPS_EY
   const Coef4<R> *tx_i, *tx_h;  // indexed by row i (sigma_x at x, x+1/2)
   const Coef4<R> *ty_i, *ty_h;  // indexed by column j (sigma_y at y, y+1/2)
-  const double2 *ex, *ey;       // CW source phase tables e^{i x kcos}, e^{i y ksin}
+  const typename Cplx<R>::T *ex, *ey;  // CW source phase tables e^{i x kcos}, e^{i y ksin} in R
   int P, nxa, ni, nj, ox;
   int in_x0, in_x1, in_y0, in_y1;  // interior (all sigma = 0): x in [in_x0,in_x1)
   int rows;                        // rows per thread of the stencil kernels (1, 2, 4, 8)
@@ -116,9 +116,11 @@ void launch_ntff_block(const NtffView &n, int nb, double t0, cudaStream_t st);
 // ---- temporally blocked stencil (fdtd_tblock.cu)
 //
 // K steps of an MPI solver per launch.  A warp owns a tile: a strip of
-// 32 - 2K columns and a segment of L rows (strip s covers columns
-// 1 + s (32-2K) .., segment g rows 1 + g L ..).  The launch reads the field set
-// of StencilView::f and writes the set `out` (ping-pong), plus the E and H
+// 32 - 2K columns (strip s covers columns 1 + s (32-2K) ..) and a row segment
+// [r0, r1).  Interior tiles (cone free of PML and halo) cover strips [s0, s1)
+// x rows [ra, rb) in segments of L rows; every other tile is an entry
+// (strip, r0, r1) of the work-list.  The launch reads the field set of
+// StencilView::f and writes the set `out` (ping-pong), plus the E and H
 // samples of the NTFF lines of every level.
 constexpr int kMaxTBlock = 8;
 
@@ -131,10 +133,11 @@ struct TBlockView {
   // f: TM 0 Ez, 1 Hx, 2 Hy ; TE 0 Ex, 1 Ey, 2 Hz
   typename Cplx<R>::T *col, *row;
   int cj[4], ri[4];
-  const int2 *tiles;   // (strip, segment) tiles of the general kernel
+  const int4 *tiles;   // (strip, r0, r1, -) tiles of the general kernel
   int ntiles;
-  int s0, s1, g0, g1;  // tiles of the interior kernel: strips [s0,s1) x segments [g0,g1)
-  int L;               // rows per segment
+  int s0, s1;          // interior kernel: strips [s0, s1) x
+  int ra, rb, nseg;    //   rows [ra, rb) in nseg segments of L rows
+  int L;
   double2 sc[kMaxTBlock];  // CW source per level: ray_coef e^{-i w t}
 };
 

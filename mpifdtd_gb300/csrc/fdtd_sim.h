@@ -22,7 +22,8 @@ struct fdtd_sim {
   void *d_f[fdtd::kMaxSlots] = {};
   void *d_ieps64[2] = {}, *d_ieps32[2] = {};
   void *d_tab64[4] = {}, *d_tab32[4] = {};
-  void *d_ex = nullptr, *d_ey = nullptr;
+  void *d_ex = nullptr, *d_ey = nullptr;      // CW phase tables, FP64
+  void *d_ex32 = nullptr, *d_ey32 = nullptr;  // and FP32 copies (FP32 fields)
   // NTFF
   void *d_cells = nullptr, *d_shift = nullptr, *d_vals = nullptr;
   void *d_ntff[3] = {};
@@ -39,9 +40,9 @@ struct fdtd_sim {
   int tb_rows = 0;              // rows per tile segment (FDTD_OPT_TBLOCK_ROWS), 0 = automatic
   void *d_f2[fdtd::kMaxSlots] = {};  // the other field set
   void *d_tbcol = nullptr, *d_tbrow = nullptr;  // NTFF line samples of kMaxTBlock levels
-  void *d_tiles = nullptr;      // int2 (strip, segment) work-list of the general kernel
+  void *d_tiles = nullptr;      // int4 (strip, r0, r1, -) work-list of the general kernel
   int ntiles = 0, tiles_cap = 0;
-  int tb_s0 = 0, tb_s1 = 0, tb_g0 = 0, tb_g1 = 0, tb_L = 0;
+  int tb_s0 = 0, tb_s1 = 0, tb_ra = 1, tb_rb = 1, tb_nseg = 0, tb_L = 0;
   int tb_built_k = 0, tb_built_l = 0;
   std::vector<double> tune_table;  // last fdtd_autotune: (K, rows, ms per step) per candidate
   int nb_pending = 0;           // buffered steps not yet deposited (mode 2)
@@ -62,3 +63,15 @@ struct fdtd_sim {
   long long prof_steps = 0;
 };
 
+// Temporal-blocking tiles of a simulation (fdtd_api.cu): interior strips
+// [s0, s1) x rows [ra, rb) in nseg segments of L rows, and the list of the
+// other tiles (strip, r0, r1, 0).
+struct TilePlan {
+  int s0 = 0, s1 = 0, ra = 1, rb = 1, L = 0, nseg = 0;
+  std::vector<int4> general;
+};
+int fdtd_plan_tiles(const fdtd_sim *s, int K, int L, TilePlan *plan);
+
+// The stencil view of a simulation's current field set (fdtd_api.cu).
+template <typename R>
+fdtd::StencilView<R> fdtd_view_of(fdtd_sim *s);

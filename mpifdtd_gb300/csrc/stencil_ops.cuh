@@ -18,19 +18,23 @@ __device__ __forceinline__ bool is_one(float v) { return __float_as_int(v) == 0x
 
 // CW scattered-wave increment at array cell (i, j): ray_coef (1/eps - 1) e^{i(kr - w t)}
 // (mpiTM_UPML.c:369-370).  kr is split as x*kcos + y*ksin, so e^{ikr} is the
-// product of two 1-D tables; (s_re, s_im) = ray_coef e^{-i w t} comes from the host per step.
+// product of two 1-D tables; (s_re, s_im) = ray_coef e^{-i w t} comes from the
+// host per step.  Evaluated in the field precision R: FP64 for the parity
+// engine; FP32 for FP32 fields (an FP64 evaluation there costs more than the
+// whole FP32 stencil on dielectric cells, GB300's FP64 rate being ~1/56 of FP32).
 template <typename R>
 __device__ __forceinline__ void cw_add(const StencilView<R> &v, double s_re, double s_im, int i, int j, R ie,
                                        typename Cplx<R>::T &e)
 {
-  const double2 ex = v.ex[i], ey = v.ey[j];
-  const double pr = ex.x * ey.x - ex.y * ey.y;
-  const double pi = ex.x * ey.y + ex.y * ey.x;
-  const double amp = (double)ie - 1.0;
-  const double qr = (pr * s_re - pi * s_im) * amp;
-  const double qi = (pr * s_im + pi * s_re) * amp;
-  e.x = (R)((double)e.x + qr);
-  e.y = (R)((double)e.y + qi);
+  const typename Cplx<R>::T ex = v.ex[i], ey = v.ey[j];
+  const R sr = (R)s_re, si = (R)s_im;
+  const R pr = ex.x * ey.x - ex.y * ey.y;
+  const R pi = ex.x * ey.y + ex.y * ey.x;
+  const R amp = ie - (R)1;
+  const R qr = (pr * sr - pi * si) * amp;
+  const R qi = (pr * si + pi * sr) * amp;
+  e.x = e.x + qr;
+  e.y = e.y + qi;
 }
 
 template <typename R>

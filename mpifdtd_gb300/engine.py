@@ -108,6 +108,14 @@ def load():
         "fdtd_get_option": (I, [P, I, C.POINTER(I)]),
         "fdtd_autotune": (I, [P, C.POINTER(I), C.POINTER(I), dp]),
         "fdtd_autotune_report": (I, [P, dp, I]),
+        "fdtd_batch_create": (I, [I, P, I, C.POINTER(P)]),
+        "fdtd_batch_destroy": (I, [P]),
+        "fdtd_batch_size": (I, [P]),
+        "fdtd_batch_instance": (I, [P, I, C.POINTER(P)]),
+        "fdtd_batch_set_option": (I, [P, I, I]),
+        "fdtd_batch_run": (I, [P]),
+        "fdtd_batch_reset": (I, [P]),
+        "fdtd_batch_launch_count": (C.c_longlong, [P]),
         "fdtd_last_error": (C.c_char_p, []),
         "fdtd_version": (C.c_char_p, []),
     }
@@ -144,7 +152,7 @@ def geometry_of(fi: FieldInfo) -> Geometry:
 class Simulation:
     """One GPU simulation of a UPML solver (see include/mpifdtd_gb300.h)."""
 
-    def __init__(self, solver, fi: FieldInfo, precision: int | str = F64):
+    def __init__(self, solver, fi: FieldInfo, precision: int | str = F64, _borrow=None):
         self.lib = load()
         self.solver = SOLVERS[solver] if isinstance(solver, str) else int(solver)
         if isinstance(precision, str):
@@ -152,7 +160,10 @@ class Simulation:
         self.precision = precision
         self.fi = fi
         h = C.c_void_p()
-        _check(self.lib.fdtd_create(self.solver, C.byref(_config(fi, precision)), C.byref(h)))
+        if _borrow is not None:  # an instance owned by a Batch
+            h, self._owner = _borrow
+        else:
+            _check(self.lib.fdtd_create(self.solver, C.byref(_config(fi, precision)), C.byref(h)))
         self.h = h
         self.geo = Geometry()
         _check(self.lib.fdtd_get_geometry(self.h, C.byref(self.geo)))
@@ -160,7 +171,8 @@ class Simulation:
     # -- lifetime
     def close(self):
         if getattr(self, "h", None):
-            self.lib.fdtd_destroy(self.h)
+            if getattr(self, "_owner", None) is None:
+                self.lib.fdtd_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -342,3 +354,59 @@ class Simulation:
         _check(self.lib.fdtd_get_ntff_guard(self.h, int(which), out.ctypes.data_as(C.POINTER(C.c_double)),
                                             C.byref(g)))
         return out[:2 * g.value]
+
+
+class Batch:
+    """Independent instances of one MPI solver advanced together (fdtd_batch_*):
+    a sweep of structures / wavelengths with uneven grids and step counts.
+
+    batch.instances[i] is a Simulation view of instance i (owned by the batch):
+    fill its permittivity before run(), read fields and frequency() after."""
+
+    def __init__(self, solver, fis, precision: int | str = F32):
+        self.lib = load()
+        self.solver = SOLVERS[solver] if isinstance(solver, str) else int(solver)
+        if isinstance(precision, str):
+            precision = {"f64": F64, "f32": F32}[precision]
+        cfgs = (_Config * len(fis))(*[_config(fi, precision) for fi in fis])
+        h = C.c_void_p()
+        _check(self.lib.fdtd_batch_create(self.solver, cfgs, len(fis), C.byref(h)))
+        self.h = h
+        self.instances = []
+        for i, fi in enumerate(fis):
+            sh = C.c_void_p()
+            _check(self.lib.fdtd_batch_instance(self.h, i, C.byref(sh)))
+            self.instances.append(Simulation(self.solver, fi, precision, _borrow=(sh, self)))
+
+    def set_option(self, key: int, value: int):
+        _check(self.lib.fdtd_batch_set_option(self.h, int(key), int(value)))
+
+    def run(self):
+        """Every instance from time 0 to its own step_num."""
+        _check(self.lib.fdtd_batch_run(self.h))
+
+    def reset(self):
+        _check(self.lib.fdtd_batch_reset(self.h))
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.fdtd_batch_launch_count(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            for s in self.instances:
+                s.h = None
+            self.lib.fdtd_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
