@@ -20,8 +20,10 @@ e2e   : the same metric through the C ABI with host buffers: the permittivity
 roofline : the stencil half-step pair (E + H kernels) against the measured
         HBM copy bandwidth, with the algorithmic 200 B per FP64 TM cell-update.
 variants : the same workload with FP32 fields and FP64 NTFF, temporally
-        blocked (depth and tile rows from fdtd_autotune), and the FP32-vs-FP64
-        error (field relative L2, far-field dB) on the 1044^2 Mie cylinder.
+        blocked (depth and tile rows from fdtd_autotune), the FP32-vs-FP64
+        error (field relative L2, far-field dB) on the 1044^2 Mie cylinder, and
+        the batched sweep of 256 Mie cylinders (structures/s, FP32 batched
+        engine against the FP64 engine structure by structure).
 cpu_baseline / --impl reference : the oracle's C restatement of the reference
         (oracle/fdtd_oracle.c, the reference's own loops) on every host core,
         one independent down-scaled instance per core (the reference's own
@@ -345,7 +347,34 @@ def run_variants(m, args, torch, cells, ms_f64):
     out["fp32_error_vs_fp64"] = {"case": "1044^2 Mie cylinder r 500 nm eps 2.25, MPI_TM_UPML, 600 steps",
                                  "field_rel_l2": rep["field_rel_l2"], "ntff_rel_l2": rep["ntff_rel_l2"],
                                  "farfield_db_max": rep["farfield_db_max"]}
+    if not args.no_sweep:
+        out["sweep"] = run_sweep()
     return out
+
+
+def run_sweep():
+    """The batched Mie sweep: 256 seeded cylinders (r 100-800 nm, eps 1.5-4.0,
+    lambda 380-780 nm, 5 nm cells, 236^2..643^2 grids, 12 periods), FP32 fields
+    in one batched engine against the FP64 engine run structure by structure,
+    far field from the FP64 frequency NTFF (360 angles) of each."""
+    from mpifdtd_gb300.sweep import farfield_rel_err, mie_sweep, run_batch, run_sequential
+    cases = mie_sweep(256)
+    cell_steps = sum(c.cells * c.fi.step_num for c in cases)
+    ff32, t32, e2e32, launches = run_batch(cases, "f32", tblock=4)
+    ff64, t64, e2e64 = run_sequential(cases, "f64")
+    err = farfield_rel_err(ff32, ff64)
+    return {
+        "workload": "256 Mie cylinders, MPI_TM_UPML, 12 optical periods each, FP64 frequency NTFF at 360 angles",
+        "unit": "structures/s", "cell_updates": cell_steps,
+        "batched_fp32": {"structures_per_s": len(cases) / t32, "gcell_per_s": cell_steps / t32 / 1e9,
+                         "seconds": t32, "e2e_seconds": e2e32, "gpu_launches": launches,
+                         "tblock": 4, "timing": "wall clock around fdtd_batch_run (synchronous)"},
+        "sequential_fp64": {"structures_per_s": len(cases) / t64, "gcell_per_s": cell_steps / t64 / 1e9,
+                            "seconds": t64, "e2e_seconds": e2e64,
+                            "timing": "wall clock around each fdtd_run + synchronize, summed"},
+        "speedup_fp32_batched_vs_fp64": t64 / t32,
+        "farfield_rel_l2_fp32_vs_fp64": {"max": float(err.max()), "median": float(np.median(err))},
+    }
 
 
 def run_e2e(m, sim, args, torch):
@@ -386,6 +415,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-variants", action="store_true", help="skip the FP32 / temporal-blocking line items")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the batched 256-structure sweep")
     ap.add_argument("--grid", type=int, default=0,
                     help="interior cells per side for a smaller case of the same workload (profiling)")
     args = ap.parse_args()

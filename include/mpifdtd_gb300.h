@@ -61,8 +61,15 @@ typedef struct fdtd_config {
   /* field.h:20-28 FieldInfo, physical sizes in nm */
   int width_nm, height_nm, h_u_nm, pml, lambda_nm, angle_deg, step_num;
   int precision;       /* FDTD_F64 or FDTD_F32                                 */
-  int reserved[8];     /* must be zero                                         */
+  int flags;           /* FDTD_CFG_* bits                                      */
+  int reserved[7];     /* must be zero                                         */
 } fdtd_config;
+
+/* No time-domain NTFF state (accumulators, path tables): for CW runs whose
+ * far field is fdtd_frequency of the final fields, e.g. batch sweeps with
+ * thousands of instances.  NTFF mode is then 3 and fdtd_get_ntff /
+ * fdtd_spectrum return FDTD_E_STATE. */
+#define FDTD_CFG_NO_TIME_NTFF 1
 
 /* Grid and NTFF geometry derived exactly as field_init() does (field.c:89-143). */
 typedef struct fdtd_geometry {

@@ -6,6 +6,8 @@
   (include/mpifdtd_upml.h); needs the host program's field_*/models_* symbols.
 * ``_build/libmpifdtd_field.so``  the library's own implementation of the
   reference's field.h / models.h host API (for programs without field.c).
+* ``_build/libmpifdtd_surrogate.so`` the far-field surrogate's kernels
+  (tcgen05 BF16 GEMM, element-wise forward/backward, Adam), sm_103a.
 
 Translation units compile in parallel; no cmake.  Host code is compiled with
 -ffp-contract=off because it evaluates the reference's one-time formulas
@@ -28,6 +30,8 @@ INCLUDE = ROOT / "include"
 ENGINE_SO = BUILD / "libmpifdtd_gb300.so"
 UPML_SO = BUILD / "libmpifdtd_upml.so"
 FIELD_SO = BUILD / "libmpifdtd_field.so"
+SURROGATE_SO = BUILD / "libmpifdtd_surrogate.so"
+SURROGATE_SOURCES = ["surrogate_gemm.cu", "surrogate_ops.cu"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -73,16 +77,19 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     hdrs = _headers()
     objs = []
     jobs = []
-    for src in ENGINE_SOURCES:
+    sobjs = []
+    for src in ENGINE_SOURCES + SURROGATE_SOURCES:
         s = CSRC / src
         o = BUILD / (s.stem + ".o")
-        objs.append(o)
+        (objs if src in ENGINE_SOURCES else sobjs).append(o)
         if force or _stale(o, [s] + hdrs):
             jobs.append([nvcc()] + NVCC_FLAGS + PER_FILE_FLAGS.get(src, []) + ["-c", s, "-o", o])
     with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         list(ex.map(lambda c: _run(c, verbose), jobs))
-    if force or jobs or _stale(ENGINE_SO, objs):
+    if force or _stale(ENGINE_SO, objs):
         _run([nvcc()] + ARCH + ["-shared", "-o", ENGINE_SO] + objs, verbose)
+    if force or _stale(SURROGATE_SO, sobjs):
+        _run([nvcc()] + ARCH + ["-shared", "-o", SURROGATE_SO] + sobjs, verbose)
     # drop-in layer (C) and the library's own field/models host API, both
     # linked against the engine and finding it next to themselves ($ORIGIN)
     link = [f"-L{BUILD}", "-lmpifdtd_gb300", "-Wl,-rpath,$ORIGIN", "-lm"]

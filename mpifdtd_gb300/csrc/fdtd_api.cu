@@ -199,6 +199,12 @@ static int build_tables(fdtd_sim *s)
 // NTFF path cells in the reference's side order and their per-angle shifts.
 static int build_ntff(fdtd_sim *s)
 {
+  if (s->cfg.flags & FDTD_CFG_NO_TIME_NTFF) {  // status word only
+    s->ntff_mode = 3;
+    CK(cudaMalloc(&s->d_status, sizeof(unsigned int)));
+    CK(cudaMemsetAsync(s->d_status, 0, sizeof(unsigned int), s->stream));
+    return FDTD_OK;
+  }
   const fdtd_geometry &g = s->geo;
   const bool tm = s->tm, mpi = s->mpi;
   const int P = s->pitch;
@@ -330,8 +336,9 @@ extern "C" int fdtd_create(int solver, const fdtd_config *cfg, fdtd_sim **out)
     return fail(FDTD_E_ARG, "solver %d is not a UPML solver (2..5)", solver);
   if (cfg->precision != FDTD_F64 && cfg->precision != FDTD_F32)
     return fail(FDTD_E_ARG, "precision must be FDTD_F64 or FDTD_F32");
-  for (int q = 0; q < 8; q++)
+  for (int q = 0; q < 7; q++)
     if (cfg->reserved[q]) return fail(FDTD_E_ARG, "reserved fields must be zero");
+  if (cfg->flags & ~FDTD_CFG_NO_TIME_NTFF) return fail(FDTD_E_ARG, "unknown config flags %#x", cfg->flags);
   fdtd_geometry geo;
   int rc = fdtd_geometry_of(cfg, &geo);
   if (rc) return rc;
@@ -531,6 +538,8 @@ extern "C" int fdtd_set_option(fdtd_sim *s, int key, int value)
   switch (key) {
   case FDTD_OPT_NTFF_MODE:
     if (value < 0 || value > 3) return fail(FDTD_E_ARG, "NTFF mode must be 0, 1, 2 or 3");
+    if (value != 3 && (s->cfg.flags & FDTD_CFG_NO_TIME_NTFF))
+      return fail(FDTD_E_STATE, "created with FDTD_CFG_NO_TIME_NTFF: NTFF mode stays 3");
     s->ntff_mode = value;
     return FDTD_OK;
   case FDTD_OPT_NTFF_CHUNK:
@@ -1205,6 +1214,7 @@ extern "C" int fdtd_get_eps(fdtd_sim *s, int which, int layout, double *out)
 extern "C" int fdtd_get_ntff(fdtd_sim *s, int which, double *out)
 {
   if (!s || !out) return fail(FDTD_E_ARG, "null argument");
+  if (!s->d_ntff[0]) return fail(FDTD_E_STATE, "no time-domain NTFF (FDTD_CFG_NO_TIME_NTFF)");
   if (which < 0 || which > 2) return fail(FDTD_E_ARG, "ntff index %d out of range", which);
   if (int rc = flush_ntff(s)) return rc;
   CK(cudaStreamSynchronize(s->stream));
@@ -1216,6 +1226,7 @@ extern "C" int fdtd_get_ntff(fdtd_sim *s, int which, double *out)
 extern "C" int fdtd_get_ntff_guard(fdtd_sim *s, int which, double *out, int *guard)
 {
   if (!s || !out) return fail(FDTD_E_ARG, "null argument");
+  if (!s->d_ntff[0]) return fail(FDTD_E_STATE, "no time-domain NTFF (FDTD_CFG_NO_TIME_NTFF)");
   if (which < 0 || which > 2) return fail(FDTD_E_ARG, "ntff index %d out of range", which);
   if (int rc = flush_ntff(s)) return rc;
   CK(cudaStreamSynchronize(s->stream));
@@ -1233,7 +1244,7 @@ extern "C" int fdtd_reset(fdtd_sim *s)
   if (int rc = flush_ntff(s)) return rc;
   const size_t bytes = (size_t)s->nxa * s->pitch * s->esize;
   for (int a = 0; a < s->nslots; a++) CK(cudaMemsetAsync(s->d_f[a], 0, bytes, s->stream));
-  if (!s->mpi)
+  if (!s->mpi && s->d_ntff[0])
     for (int a = 0; a < 3; a++) CK(cudaMemsetAsync(s->d_ntff[a], 0, sizeof(double2) * s->ntff_len, s->stream));
   CK(cudaStreamSynchronize(s->stream));
   s->time = 0;
@@ -1289,6 +1300,7 @@ static int ensure_farfield(fdtd_sim *s)
 extern "C" int fdtd_spectrum(fdtd_sim *s, double *out)
 {
   if (!s || !out) return fail(FDTD_E_ARG, "null argument");
+  if (!s->d_ntff[0]) return fail(FDTD_E_STATE, "no time-domain NTFF (FDTD_CFG_NO_TIME_NTFF)");
   if (s->cfg.step_num > kNfft)
     return fail(FDTD_E_UNSUPPORTED, "step_num %d > %d: the reference's FFT buffer overflows (ntffTM.c:214-221)",
                 s->cfg.step_num, kNfft);

@@ -51,7 +51,7 @@ class FieldInfo:
 
 class _Config(C.Structure):
     _fields_ = [(n, C.c_int) for n in ("width_nm", "height_nm", "h_u_nm", "pml", "lambda_nm",
-                                       "angle_deg", "step_num", "precision")] + [("reserved", C.c_int * 8)]
+                                       "angle_deg", "step_num", "precision", "flags")] + [("reserved", C.c_int * 7)]
 
 
 class Geometry(C.Structure):
@@ -136,10 +136,14 @@ def _dptr(a):
     return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
 
 
-def _config(fi: FieldInfo, precision: int) -> _Config:
+CFG_NO_TIME_NTFF = 1
+
+
+def _config(fi: FieldInfo, precision: int, flags: int = 0) -> _Config:
     c = _Config()
     (c.width_nm, c.height_nm, c.h_u_nm, c.pml, c.lambda_nm, c.angle_deg, c.step_num) = fi.astuple()
     c.precision = precision
+    c.flags = flags
     return c
 
 
@@ -152,7 +156,7 @@ def geometry_of(fi: FieldInfo) -> Geometry:
 class Simulation:
     """One GPU simulation of a UPML solver (see include/mpifdtd_gb300.h)."""
 
-    def __init__(self, solver, fi: FieldInfo, precision: int | str = F64, _borrow=None):
+    def __init__(self, solver, fi: FieldInfo, precision: int | str = F64, _borrow=None, no_time_ntff=False):
         self.lib = load()
         self.solver = SOLVERS[solver] if isinstance(solver, str) else int(solver)
         if isinstance(precision, str):
@@ -163,7 +167,8 @@ class Simulation:
         if _borrow is not None:  # an instance owned by a Batch
             h, self._owner = _borrow
         else:
-            _check(self.lib.fdtd_create(self.solver, C.byref(_config(fi, precision)), C.byref(h)))
+            flags = CFG_NO_TIME_NTFF if no_time_ntff else 0
+            _check(self.lib.fdtd_create(self.solver, C.byref(_config(fi, precision, flags)), C.byref(h)))
         self.h = h
         self.geo = Geometry()
         _check(self.lib.fdtd_get_geometry(self.h, C.byref(self.geo)))
@@ -363,12 +368,13 @@ class Batch:
     batch.instances[i] is a Simulation view of instance i (owned by the batch):
     fill its permittivity before run(), read fields and frequency() after."""
 
-    def __init__(self, solver, fis, precision: int | str = F32):
+    def __init__(self, solver, fis, precision: int | str = F32, no_time_ntff=True):
         self.lib = load()
         self.solver = SOLVERS[solver] if isinstance(solver, str) else int(solver)
         if isinstance(precision, str):
             precision = {"f64": F64, "f32": F32}[precision]
-        cfgs = (_Config * len(fis))(*[_config(fi, precision) for fi in fis])
+        flags = CFG_NO_TIME_NTFF if no_time_ntff else 0
+        cfgs = (_Config * len(fis))(*[_config(fi, precision, flags) for fi in fis])
         h = C.c_void_p()
         _check(self.lib.fdtd_batch_create(self.solver, cfgs, len(fis), C.byref(h)))
         self.h = h
