@@ -18,7 +18,8 @@
 //                      (rows), bias / accumulate / GELU, stores.
 // Every mbarrier wait is bounded: on timeout the kernel sets *err and leaves
 // the loop (results are then invalid and the host reports the error).
-// Shapes: M % 128 == 0, N % BN == 0, K % 64 == 0, lda / ldb % 8 == 0.
+// Batched: grid.z runs independent products (3-D tensor maps), B may be shared.
+// Shapes: M % 128 == 0, N % 64 == 0, K % 64 == 0, leading dims % 8 == 0.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -69,12 +70,13 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, unsign
   return false;
 }
 
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int c0, int c1, uint64_t *bar)
+// 3-D tile (K, rows, batch entry) into shared memory, completing on bar
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int c0, int c1, int c2, uint64_t *bar)
 {
   asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
-      "[%4];" ::"r"(smem_u32(dst)),
-      "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_u32(dst)),
+      "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
       : "memory");
 }
 
@@ -136,6 +138,7 @@ __device__ __forceinline__ float gelu(float x)
 
 struct Epilogue {
   void *c;            // output
+  long long c_bstride;  // elements between batch entries of C (and pre)
   int ldc;
   int c_bf16;         // 1: BF16 output, 0: FP32
   int accumulate;     // add into C (FP32 output only)
@@ -147,7 +150,7 @@ struct Epilogue {
 template <int BN>
 __global__ void __launch_bounds__(128, 1)
     gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, Epilogue ep,
-                        int K, unsigned *err)
+                        int K, int b_batched, unsigned *err)
 {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -159,7 +162,7 @@ __global__ void __launch_bounds__(128, 1)
   uint64_t *done = empty + STAGES;
   uint32_t *tmem_slot = (uint32_t *)(done + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN, z = blockIdx.z;
   const int nk = K / BK;
 
   if (threadIdx.x == 0) {
@@ -185,8 +188,8 @@ __global__ void __launch_bounds__(128, 1)
       const int s = kb % STAGES;
       if (kb >= STAGES && !mbar_wait(&empty[s], ((kb / STAGES) - 1) & 1, err, 1u)) break;
       mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
-      tma_load_2d(sA + s * A_BYTES, &tA, kb * BK, m0, &full[s]);
-      tma_load_2d(sB + s * B_BYTES, &tB, kb * BK, n0, &full[s]);
+      tma_load_3d(sA + s * A_BYTES, &tA, kb * BK, m0, z, &full[s]);
+      tma_load_3d(sB + s * B_BYTES, &tB, kb * BK, n0, b_batched ? z : 0, &full[s]);
     }
   } else if (threadIdx.x == 32) {  // MMA issuer
     constexpr uint32_t idesc = idesc_bf16(BM, BN);
@@ -220,9 +223,9 @@ __global__ void __launch_bounds__(128, 1)
 #pragma unroll
         for (int q = 0; q < 32; q++) v[q] += ep.bias[col + q];
       if (ep.c_bf16) {
-        __nv_bfloat16 *out = (__nv_bfloat16 *)ep.c + (size_t)row * ep.ldc + col;
+        __nv_bfloat16 *out = (__nv_bfloat16 *)ep.c + z * ep.c_bstride + (size_t)row * ep.ldc + col;
         if (ep.pre) {
-          float *pp = ep.pre + (size_t)row * ep.ldc + col;
+          float *pp = ep.pre + z * ep.c_bstride + (size_t)row * ep.ldc + col;
 #pragma unroll
           for (int q = 0; q < 32; q += 4) *(float4 *)(pp + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
         }
@@ -237,11 +240,12 @@ __global__ void __launch_bounds__(128, 1)
           *(uint4 *)(out + q) = *(const uint4 *)h;
         }
       } else {
-        float *out = (float *)ep.c + (size_t)row * ep.ldc + col;
+        float *out = (float *)ep.c + z * ep.c_bstride + (size_t)row * ep.ldc + col;
         if (ep.pre)
 #pragma unroll
           for (int q = 0; q < 32; q += 4)
-            *(float4 *)(ep.pre + (size_t)row * ep.ldc + col + q) = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+            *(float4 *)(ep.pre + z * ep.c_bstride + (size_t)row * ep.ldc + col + q) =
+                make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
         if (ep.act == 1)
 #pragma unroll
           for (int q = 0; q < 32; q++) v[q] = gelu(v[q]);
@@ -292,14 +296,16 @@ static int encoder()
   return 0;
 }
 
-// rows x K BF16 row-major matrix (ld elements between rows), boxes of box_rows x 64, 128-byte swizzle
-static int make_map(CUtensorMap *map, const void *ptr, int rows, int K, int ld, int box_rows)
+// batch x rows x K BF16 row-major matrices (ld elements between rows, bstride
+// between batch entries), boxes of box_rows x 64, 128-byte swizzle
+static int make_map(CUtensorMap *map, const void *ptr, int rows, int K, int ld, int box_rows, int batch,
+                    long long bstride)
 {
-  const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
-  const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
-  const cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
-  const cuuint32_t estr[2] = {1, 1};
-  const CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims, strides, box,
+  const cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, (cuuint64_t)batch};
+  const cuuint64_t strides[2] = {(cuuint64_t)ld * 2, (cuuint64_t)(batch > 1 ? bstride : (long long)ld * rows) * 2};
+  const cuuint32_t box[3] = {(cuuint32_t)BK, (cuuint32_t)box_rows, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void *>(ptr), dims, strides, box,
                               estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? 0 : set_err(1, "cuTensorMapEncodeTiled rejected the operand");
@@ -317,23 +323,33 @@ using namespace sg;
 
 extern "C" const char *sg_last_error(void) { return g_err; }
 
-// C = A . B^T (+bias) (+C) (GELU).  c_bf16: BF16 output; pre: optional FP32
-// copy of the pre-activation (same ldc).  err: device word, OR-ed with 1/2/4
-// when a wait timed out.  stream: cudaStream_t.
-extern "C" int sg_gemm_bf16_tn(const void *A, int lda, const void *B, int ldb, void *C, int ldc, int M, int N, int K,
-                               int c_bf16, int accumulate, const float *bias, int act, float *pre, unsigned *err,
-                               void *stream)
+// C[z] = A[z] . B[z]^T (+bias) (+C[z]) (GELU) for z < batch.  c_bf16: BF16
+// output; pre: optional FP32 copy of the pre-activation (same layout as C).
+// *_bstride: elements between batch entries (0 for an operand shared by all).
+// err: device word, OR-ed with 1/2/4 when a wait timed out.  stream: cudaStream_t.
+extern "C" int sg_gemm_bf16_tn_batched(const void *A, int lda, long long a_bstride, const void *B, int ldb,
+                                       long long b_bstride, void *C, int ldc, long long c_bstride, int M, int N,
+                                       int K, int batch, int c_bf16, int accumulate, const float *bias, int act,
+                                       float *pre, unsigned *err, void *stream)
 {
   if (!A || !B || !C || !err) return set_err(1, "null pointer");
   if (M <= 0 || N <= 0 || K <= 0 || M % BM || K % BK || N % 64) return set_err(1, "shape: M%128, N%64, K%64");
-  if (lda % 8 || ldb % 8 || ldc % 8 || ((uintptr_t)A & 15) || ((uintptr_t)B & 15)) return set_err(1, "alignment");
+  if (batch < 1 || batch > 65535) return set_err(1, "batch must be in [1, 65535]");
+  if (lda % 8 || ldb % 8 || ldc % 8 || a_bstride % 8 || b_bstride % 8 || c_bstride % 8 || ((uintptr_t)A & 15) ||
+      ((uintptr_t)B & 15) || ((uintptr_t)C & 15))
+    return set_err(1, "alignment");
   if (c_bf16 && accumulate) return set_err(1, "accumulate needs FP32 output");
   if (int rc = encoder()) return rc;
   const bool wide = N % 128 == 0;
   CUtensorMap ta, tb;
-  if (make_map(&ta, A, M, K, lda, BM) || make_map(&tb, B, N, K, ldb, wide ? 128 : 64)) return 1;
-  Epilogue ep{C, ldc, c_bf16, accumulate, bias, act, pre};
+  // B may be shared by every batch entry (b_bstride 0: a one-entry map always read at z = 0)
+  if (a_bstride == 0 && batch > 1) return set_err(1, "A must have a batch stride");
+  if (make_map(&ta, A, M, K, lda, BM, batch, a_bstride) ||
+      make_map(&tb, B, N, K, ldb, wide ? 128 : 64, b_bstride ? batch : 1, b_bstride))
+    return 1;
+  Epilogue ep{C, c_bstride, ldc, c_bf16, accumulate, bias, act, pre};
   cudaStream_t st = (cudaStream_t)stream;
+  const dim3 grid((unsigned)(N / (wide ? 128 : 64)), (unsigned)(M / BM), (unsigned)batch);
   if (wide) {
     static bool cfg = false;
     if (!cfg) {
@@ -341,7 +357,7 @@ extern "C" int sg_gemm_bf16_tn(const void *A, int lda, const void *B, int ldb, v
                            (int)smem_bytes<128>());
       cfg = true;
     }
-    gemm_bf16_tn_kernel<128><<<dim3(N / 128, M / BM), 128, smem_bytes<128>(), st>>>(ta, tb, ep, K, err);
+    gemm_bf16_tn_kernel<128><<<grid, 128, smem_bytes<128>(), st>>>(ta, tb, ep, K, b_bstride ? 1 : 0, err);
   } else {
     static bool cfg = false;
     if (!cfg) {
@@ -349,9 +365,17 @@ extern "C" int sg_gemm_bf16_tn(const void *A, int lda, const void *B, int ldb, v
                            (int)smem_bytes<64>());
       cfg = true;
     }
-    gemm_bf16_tn_kernel<64><<<dim3(N / 64, M / BM), 128, smem_bytes<64>(), st>>>(ta, tb, ep, K, err);
+    gemm_bf16_tn_kernel<64><<<grid, 128, smem_bytes<64>(), st>>>(ta, tb, ep, K, b_bstride ? 1 : 0, err);
   }
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_err(2, cudaGetErrorString(e));
   return 0;
+}
+
+extern "C" int sg_gemm_bf16_tn(const void *A, int lda, const void *B, int ldb, void *C, int ldc, int M, int N, int K,
+                               int c_bf16, int accumulate, const float *bias, int act, float *pre, unsigned *err,
+                               void *stream)
+{
+  return sg_gemm_bf16_tn_batched(A, lda, 0, B, ldb, 0, C, ldc, 0, M, N, K, 1, c_bf16, accumulate, bias, act, pre,
+                                 err, stream);
 }

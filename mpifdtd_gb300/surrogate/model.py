@@ -1,0 +1,242 @@
+"""Far-field surrogate: a Fourier neural operator from a permittivity map to
+the 31 x 360 far-field intensity spectrum, trained and run by the library's
+own kernels (tcgen05 BF16 GEMM with FP32 accumulation, element-wise kernels,
+Adam).  torch supplies device memory and the stream only.
+
+Architecture (B structures, C = 64 channels, 32 x 32 grid, Q = 256 modes):
+  x      = 8 x 8 mean pool of the 256 x 256 map                [B, 1024]
+  h0     = x wl + bl                                            [B, C, 1024]
+  layer l = 0..3 (spectral mixing):
+    F    = h D^T      truncated 2-D DFT (modes kx -8..7, ky 0..15, cos/sin
+                      rows of D, fixed)                         [B*C, 512]
+    Fm   = permute(F)                                           [Q, B, 2C]
+    Y[q] = Fm[q] M_l[q]^T   per-mode real 2C x 2C mixing        [Q, B, 2C]
+    Hs   = permute(Y) E^T   inverse transform (fixed E)         [B*C, 1024]
+    z    = Hs + wp_l h + bp_l ;  h = GELU(z) (no GELU after the last layer)
+  flat   = 4 x 4 mean pool of h                                 [B, C*64]
+  u      = GELU(flat W1^T + b1)                                 [B, 512]
+  out    = u W2^T + b2                                          [B, 11264]
+The first 31*360 outputs are the standardised log10 intensity (per output
+element mean / std of the training targets); the rest is padding that makes
+the output width a multiple of the GEMM tile.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import kernels as K
+
+C = 64
+NS = 1024
+Q = 256
+NL = 4
+H1 = 512
+NT = 31 * 360
+NOUT = 11264
+FLOOR = 1e-30
+
+
+def basis():
+    """Forward DFT rows D [2Q, 1024] and inverse E [1024, 2Q] (float64)."""
+    xs, ys = np.meshgrid(np.arange(32), np.arange(32), indexing="ij")
+    xs, ys = xs.ravel(), ys.ravel()
+    D = np.zeros((2 * Q, NS))
+    E = np.zeros((NS, 2 * Q))
+    q = 0
+    for kx in range(-8, 8):
+        for ky in range(16):
+            th = 2 * math.pi * (kx * xs + ky * ys) / 32
+            w = 1.0 if ky == 0 else 2.0
+            D[2 * q] = np.cos(th) / 32
+            D[2 * q + 1] = np.sin(th) / 32
+            E[:, 2 * q] = w * np.cos(th) / 32
+            E[:, 2 * q + 1] = w * np.sin(th) / 32
+            q += 1
+    return D, E
+
+
+def init_params(seed=1234):
+    """FP32 parameters (numpy), the layout the GPU model and the CPU oracle share."""
+    rng = np.random.default_rng(seed)
+    p = {"wl": rng.normal(0, 1, C), "bl": np.zeros(C)}
+    for l in range(NL):
+        p[f"M{l}"] = rng.normal(0, 0.5 / math.sqrt(2 * C), (Q, 2 * C, 2 * C))
+        p[f"wp{l}"] = rng.normal(0, 1 / math.sqrt(C), (C, C))
+        p[f"bp{l}"] = np.zeros(C)
+    p["W1"] = rng.normal(0, 1 / math.sqrt(C * 64), (H1, C * 64))
+    p["b1"] = np.zeros(H1)
+    p["W2"] = rng.normal(0, 1 / math.sqrt(H1), (NOUT, H1))
+    p["b2"] = np.zeros(NOUT)
+    return {k: v.astype(np.float32) for k, v in p.items()}
+
+
+class FNO:
+    def __init__(self, params=None, seed=1234):
+        import torch
+        self.torch = torch
+        dev = "cuda"
+        p = params if params is not None else init_params(seed)
+        self.p = {k: torch.tensor(v, device=dev, dtype=torch.float32) for k, v in p.items()}
+        # BF16 copies of the GEMM weights (mode mixing M0..M3, head W1, W2), refreshed by adam_step
+        self.bf = {k: self.p[k].to(torch.bfloat16) for k in [f"M{l}" for l in range(NL)] + ["W1", "W2"]}
+        D, E = basis()
+        self.D = torch.tensor(D, device=dev, dtype=torch.bfloat16)        # [512, 1024]
+        self.E = torch.tensor(E, device=dev, dtype=torch.bfloat16)        # [1024, 512]
+        self.Dt = torch.tensor(D.T.copy(), device=dev, dtype=torch.bfloat16)  # [1024, 512]
+        self.Et = torch.tensor(E.T.copy(), device=dev, dtype=torch.bfloat16)  # [512, 1024]
+        self.mu = torch.zeros(NT, device=dev)
+        self.sd = torch.ones(NT, device=dev)
+        self.adam = None
+        self.t = 0
+
+    # ------------------------------------------------------------ helpers
+    def _e(self, shape, dtype=None):
+        return self.torch.empty(shape, device="cuda", dtype=dtype or self.torch.float32)
+
+    def pool(self, maps_u8):
+        """uint8 maps [B, 256, 256] (device) -> x [B, 1024]."""
+        B = maps_u8.shape[0]
+        x = self._e((B, NS))
+        K.op("sg_pool_map", maps_u8, x, B)
+        return x
+
+    # ------------------------------------------------------------ forward
+    def forward(self, x, save=False):
+        """x [B, 1024] FP32 (B % 128 == 0) -> out [B, NOUT] FP32."""
+        t = self.torch
+        B = x.shape[0]
+        assert B % 128 == 0
+        bf = t.bfloat16
+        h = self._e((B, C, NS), bf)
+        K.op("sg_lift", x, self.p["wl"], self.p["bl"], h, B, C)
+        acts = {"x": x, "h": [], "Fm": [], "z": []}
+        F = self._e((B * C, 2 * Q), bf)
+        Fm = self._e((Q, B, 2 * C), bf)
+        Y = self._e((Q, B, 2 * C), bf)
+        Yt = self._e((B * C, 2 * Q), bf)
+        Hs = self._e((B * C, NS))
+        for l in range(NL):
+            K.gemm(h.view(B * C, NS), self.D, F)
+            K.op("sg_mode_permute", F, Fm, B, C, Q, 0)
+            K.gemm(Fm, self.bf[f"M{l}"], Y)
+            K.op("sg_mode_permute", Y, Yt, B, C, Q, 1)
+            K.gemm(Yt, self.E, Hs)
+            z = self._e((B, C, NS))
+            hn = self._e((B, C, NS), bf)
+            K.op("sg_pointwise_fwd", h, Hs, self.p[f"wp{l}"], self.p[f"bp{l}"], z, hn, B, C, 1 if l < NL - 1 else 0)
+            if save:
+                acts["h"].append(h)
+                acts["Fm"].append(Fm.clone())
+                acts["z"].append(z)
+            h = hn
+        flat = self._e((B, C * 64), bf)
+        K.op("sg_head_pool", h, flat, B, C)
+        u = self._e((B, H1), bf)
+        pre1 = self._e((B, H1))
+        K.gemm(flat, self.bf["W1"], u, bias=self.p["b1"], act=1, pre=pre1)
+        out = self._e((B, NOUT))
+        K.gemm(u, self.bf["W2"], out, bias=self.p["b2"])
+        if save:
+            acts.update(flat=flat, u=u, pre1=pre1)
+            self.acts = acts
+        return out
+
+    # ------------------------------------------------------------ backward
+    def loss_and_grads(self, x, y):
+        """Mean squared error against standardised targets y [B, NT]; returns
+        (per-row loss [B], grads dict of FP32 tensors shaped like the params)."""
+        t = self.torch
+        bf = t.bfloat16
+        B = x.shape[0]
+        out = self.forward(x, save=True)
+        a = self.acts
+        dout = self._e((B, NOUT), bf)
+        loss = self._e((B,))
+        K.op("sg_mse", out, y, dout, loss, B, NOUT, NT)
+        g = {}
+        g["W2"] = self._e((NOUT, H1))
+        K.gemm(K.transpose(dout), K.transpose(a["u"]), g["W2"])
+        g["b2"] = self._e((NOUT,))
+        K.op("sg_colsum", dout, g["b2"], B, NOUT)
+        du = self._e((B, H1))
+        K.gemm(dout, K.transpose(self.bf["W2"]), du)
+        dpre1 = self._e((B, H1), bf)
+        K.op("sg_gelu_bwd", du, a["pre1"], dpre1, B * H1)
+        g["W1"] = self._e((H1, C * 64))
+        K.gemm(K.transpose(dpre1), K.transpose(a["flat"]), g["W1"])
+        g["b1"] = self._e((H1,))
+        K.op("sg_colsum", dpre1, g["b1"], B, H1)
+        dflat = self._e((B, C * 64))
+        K.gemm(dpre1, K.transpose(self.bf["W1"]), dflat)
+        dh = self._e((B, C, NS))
+        K.op("sg_head_unpool", dflat, dh, B, C)
+        dz = self._e((B, C, NS))
+        dz_bf = self._e((B, C, NS), bf)
+        dYt = self._e((B * C, 2 * Q), bf)
+        dY = self._e((Q, B, 2 * C), bf)
+        dFm = self._e((Q, B, 2 * C), bf)
+        dF = self._e((B * C, 2 * Q), bf)
+        dspec = self._e((B * C, NS))
+        for l in reversed(range(NL)):
+            K.op("sg_act_bwd", dh, a["z"][l], dz, dz_bf, B * C * NS, 1 if l < NL - 1 else 0)
+            g[f"wp{l}"] = self._e((C, C))
+            g[f"bp{l}"] = self._e((C,))
+            K.op("sg_pointwise_bwd_w", dz, a["h"][l], g[f"wp{l}"], g[f"bp{l}"], B, C)
+            K.gemm(dz_bf.view(B * C, NS), self.Et, dYt)
+            K.op("sg_mode_permute", dYt, dY, B, C, Q, 0)
+            g[f"M{l}"] = self._e((Q, 2 * C, 2 * C))
+            K.gemm(K.transpose(dY), K.transpose(a["Fm"][l]), g[f"M{l}"])
+            K.gemm(dY, K.transpose(self.bf[f"M{l}"]), dFm)
+            K.op("sg_mode_permute", dFm, dF, B, C, Q, 1)
+            K.gemm(dF, self.Dt, dspec)
+            dh_prev = self._e((B, C, NS))
+            K.op("sg_pointwise_bwd_x", dz, self.p[f"wp{l}"], dspec, dh_prev, B, C)
+            dh = dh_prev
+        g["wl"] = self._e((C,))
+        g["bl"] = self._e((C,))
+        K.op("sg_lift_bwd", a["x"], dh, g["wl"], g["bl"], B, C)
+        self.acts = None
+        return loss, g
+
+    # ------------------------------------------------------------ optimizer
+    def adam_step(self, g, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8, wd=0.0):
+        t = self.torch
+        if self.adam is None:
+            self.adam = {k: (t.zeros_like(v), t.zeros_like(v)) for k, v in self.p.items()}
+        self.t += 1
+        c1, c2 = 1 - b1 ** self.t, 1 - b2 ** self.t
+        for k, w in self.p.items():
+            m, v = self.adam[k]
+            K.op("sg_adam", w, g[k], m, v, self.bf.get(k), w.numel(), lr, b1, b2, eps, c1, c2, wd)
+
+    # ------------------------------------------------------------ targets
+    def set_normalisation(self, intensity):
+        """Per-element mean / std of log10 intensity over training targets [N, NT]."""
+        t = self.torch
+        lg = t.log10(intensity.reshape(-1, NT).double() + FLOOR)
+        self.mu = lg.mean(0).float()
+        self.sd = (lg.std(0) + 1e-3).float()
+
+    def encode(self, intensity):
+        t = self.torch
+        return ((t.log10(intensity.reshape(-1, NT) + FLOOR) - self.mu) / self.sd).float().contiguous()
+
+    def decode(self, out):
+        return 10.0 ** (out[:, :NT] * self.sd + self.mu) - FLOOR
+
+    def predict(self, maps_u8, batch=4096):
+        """Far-field intensity [N, 31, 360] of uint8 maps on the device."""
+        t = self.torch
+        res = []
+        n = maps_u8.shape[0]
+        for s in range(0, n, batch):
+            part = maps_u8[s:s + batch]
+            m = part.shape[0]
+            pad = (-m) % 128
+            if pad:
+                part = t.cat([part, part[:1].expand(pad, -1, -1)])
+            out = self.forward(self.pool(part.contiguous()))
+            res.append(self.decode(out[:m]))
+        return t.cat(res).reshape(n, 31, 360)

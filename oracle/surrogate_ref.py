@@ -1,0 +1,104 @@
+"""CPU restatement of the far-field surrogate's forward and backward passes.
+
+Test infrastructure only (the gradient oracle of the GPU kernels): the same
+model as mpifdtd_gb300/surrogate/model.py in float64 numpy, with values
+rounded to BF16 at the points where the GPU stores BF16 (GEMM operands and
+BF16 outputs), so that GPU-vs-oracle differences are FP32 summation order and
+the occasional tie of a BF16 rounding, not the BF16 format itself.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+C, NS, Q, NL, H1, NT, NOUT = 64, 1024, 256, 4, 512, 31 * 360, 11264
+
+
+def bf16(a):
+    """Round to the nearest BF16 value (ties to even), returned as float64."""
+    a32 = np.ascontiguousarray(a, dtype=np.float32)
+    u = a32.view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000).astype(np.uint32)
+    return r.view(np.float32).astype(np.float64)
+
+
+def gelu(x):
+    k0, k1 = 0.7978845608, 0.044715
+    return 0.5 * x * (1 + np.tanh(k0 * (x + k1 * x ** 3)))
+
+
+def gelu_grad(x):
+    k0, k1 = 0.7978845608, 0.044715
+    t = np.tanh(k0 * (x + k1 * x ** 3))
+    return 0.5 * (1 + t) + 0.5 * x * (1 - t * t) * k0 * (1 + 3 * k1 * x * x)
+
+
+def pool_map(maps):
+    b = maps.shape[0]
+    return (maps > 0).reshape(b, 32, 8, 32, 8).mean(axis=(2, 4)).reshape(b, NS).astype(np.float64)
+
+
+def to_modes(F, B):   # [B*C, 2Q] -> [Q, B, 2C] with [q][b][r*C + c] = F[b*C + c][2q + r]
+    return F.reshape(B, C, Q, 2).transpose(2, 0, 3, 1).reshape(Q, B, 2 * C)
+
+
+def from_modes(Y, B):  # inverse of to_modes
+    return Y.reshape(Q, B, 2, C).transpose(1, 3, 0, 2).reshape(B * C, 2 * Q)
+
+
+def head_pool(h, B):
+    return h.reshape(B, C, 8, 4, 8, 4).mean(axis=(3, 5)).reshape(B, C * 64)
+
+
+def head_unpool(d, B):
+    return np.repeat(np.repeat(d.reshape(B, C, 8, 8), 4, axis=2), 4, axis=3).reshape(B, C, NS) / 16
+
+
+def loss_and_grads(p, x, y, D, E):
+    """p: float32 params (model.init_params layout), x [B, 1024], y [B, NT].
+    Returns (per-row loss [B], grads dict)."""
+    p = {k: np.asarray(v, np.float64) for k, v in p.items()}
+    B = x.shape[0]
+    Db, Eb = bf16(D), bf16(E)
+    Mb = [bf16(p[f"M{l}"]) for l in range(NL)]
+    W1b, W2b = bf16(p["W1"]), bf16(p["W2"])
+    h = bf16(x[:, None, :] * p["wl"][None, :, None] + p["bl"][None, :, None])
+    hs, Fms, zs = [], [], []
+    for l in range(NL):
+        F = bf16(h.reshape(B * C, NS) @ Db.T)
+        Fm = to_modes(F, B)
+        Y = bf16(np.einsum("qbk,qnk->qbn", Fm, Mb[l]))
+        Hs = from_modes(Y, B) @ Eb.T
+        z = Hs.reshape(B, C, NS) + np.einsum("ck,bks->bcs", p[f"wp{l}"], h) + p[f"bp{l}"][None, :, None]
+        hs.append(h)
+        Fms.append(Fm)
+        zs.append(z)
+        h = bf16(gelu(z) if l < NL - 1 else z)
+    flat = bf16(head_pool(h, B))
+    pre1 = flat @ W1b.T + p["b1"]
+    u = bf16(gelu(pre1))
+    out = u @ W2b.T + p["b2"]
+    d = out[:, :NT] - y
+    loss = (d * d).mean(axis=1)
+    dout = np.zeros((B, NOUT))
+    dout[:, :NT] = 2 * d / (B * NT)
+    dout = bf16(dout)
+    g = {"W2": dout.T @ u, "b2": dout.sum(0)}
+    du = dout @ W2b
+    dpre1 = bf16(du * gelu_grad(pre1))
+    g["W1"] = dpre1.T @ flat
+    g["b1"] = dpre1.sum(0)
+    dflat = dpre1 @ W1b
+    dh = head_unpool(dflat, B)
+    for l in reversed(range(NL)):
+        dz = dh * (gelu_grad(zs[l]) if l < NL - 1 else 1.0)
+        g[f"wp{l}"] = np.einsum("bcs,bks->ck", dz, hs[l])
+        g[f"bp{l}"] = dz.sum(axis=(0, 2))
+        dYt = bf16(bf16(dz).reshape(B * C, NS) @ Eb)
+        dY = to_modes(dYt, B)
+        g[f"M{l}"] = np.einsum("qbn,qbk->qnk", dY, Fms[l])
+        dFm = bf16(np.einsum("qbn,qnk->qbk", dY, Mb[l]))
+        dspec = from_modes(dFm, B) @ Db
+        dh = np.einsum("ck,bcs->bks", p[f"wp{l}"], dz) + dspec.reshape(B, C, NS)
+    g["wl"] = (dh * x[:, None, :]).sum(axis=(0, 2))
+    g["bl"] = dh.sum(axis=(0, 2))
+    return loss, g

@@ -58,3 +58,22 @@ def test_gemm_strided_operand_views():
     torch.cuda.synchronize()
     ref = a.float() @ b.float().t()
     assert float((out - ref).norm() / ref.norm()) < 1e-5
+
+
+@pytest.mark.parametrize("shared_b", [False, True])
+def test_gemm_batched(shared_b):
+    """grid.z products (3-D tensor maps), B per entry or shared."""
+    import torch
+    from mpifdtd_gb300.surrogate import kernels as K
+    g = torch.Generator(device="cuda").manual_seed(11)
+    z, m, n, k = 37, 128, 128, 128
+    a = torch.randn(z, m, k, device="cuda", generator=g).to(torch.bfloat16)
+    b = torch.randn(n, k, device="cuda", generator=g).to(torch.bfloat16) if shared_b else \
+        torch.randn(z, n, k, device="cuda", generator=g).to(torch.bfloat16)
+    out = torch.empty(z, m, n, device="cuda", dtype=torch.bfloat16)
+    K.gemm(a, b, out)
+    torch.cuda.synchronize()
+    assert int(K.err_word().item()) == 0
+    bt = b.float().t() if shared_b else b.float().transpose(1, 2)
+    ref = a.float() @ bt
+    assert float((out.float() - ref).norm() / ref.norm()) < 1e-2
