@@ -23,7 +23,10 @@ variants : the same workload with FP32 fields and FP64 NTFF, temporally
         blocked (depth and tile rows from fdtd_autotune), the FP32-vs-FP64
         error (field relative L2, far-field dB) on the 1044^2 Mie cylinder, and
         the batched sweep of 256 Mie cylinders (structures/s, FP32 batched
-        engine against the FP64 engine structure by structure).
+        engine against the FP64 engine structure by structure), and the
+        learned far-field surrogate (trained here on FDTD data from the
+        batched engine; held-out error, structures/s with and without the
+        1 % FDTD audit, against the batched FDTD engine).
 cpu_baseline / --impl reference : the oracle's C restatement of the reference
         (oracle/fdtd_oracle.c, the reference's own loops) on every host core,
         one independent down-scaled instance per core (the reference's own
@@ -349,6 +352,55 @@ def run_variants(m, args, torch, cells, ms_f64):
                                  "farfield_db_max": rep["farfield_db_max"]}
     if not args.no_sweep:
         out["sweep"] = run_sweep()
+    if not args.no_surrogate:
+        out["surrogate"] = run_surrogate()
+    return out
+
+
+def run_surrogate(n_train=1024, n_val=128, steps=2000):
+    """The learned far-field surrogate against the batched FDTD engine.
+
+    Data: seeded random lamella maps (256^2, eps {1, 2.43}), each simulated
+    by the batched FP32 engine at 31 wavelengths (400..700 nm) to the
+    360-angle far-field intensity.  The network (Fourier neural operator,
+    tcgen05 BF16 kernels) trains on n_train maps plus their mirror images and
+    is evaluated on n_val held-out maps (relative L2 error of the 31 x 360
+    intensity per structure).  Screening: the network predicts, 1 % of each
+    screening batch is audited by FDTD, a batch whose audit exceeds the
+    tolerance is re-simulated by FDTD (measured, fallback included)."""
+    import numpy as np
+    from mpifdtd_gb300.surrogate import screen as S
+    from mpifdtd_gb300.surrogate.data import Generator, make_maps
+    from mpifdtd_gb300.surrogate.model import FNO
+    gen = Generator(group=64)
+    maps, inten, sec = S.generate(n_train + n_val, 20261203 + 4, gen)
+    fdtd_rate = (n_train + n_val) / sec
+    net = FNO(seed=1)
+    t_train = S.train(net, maps[:n_train], inten[:n_train], steps=steps, batch=128, lr=1e-3)
+    ev = S.evaluate(net, maps[n_train:], inten[n_train:], inten[:n_train])
+    rate = S.inference_rate(net)
+    out = {
+        "unit": "structures/s (31 wavelengths x 360 angles each)",
+        "fdtd_batched_fp32": {"structures_per_s": fdtd_rate, "seconds": sec, "structures": n_train + n_val},
+        "training": {"maps": n_train, "with_mirror_images": 2 * n_train, "steps": steps, "batch": 128,
+                     "seconds": t_train},
+        "heldout_rel_l2": ev,
+        "network_structures_per_s": rate, "network_vs_fdtd": rate / fdtd_rate,
+    }
+    # the screening path at the 2 % tolerance (fallback measured), and the cost
+    # of the 1 % audit alone (a tolerance no audit exceeds: the throughput the
+    # pipeline keeps when its audits pass)
+    for key, tol, n in (("screen_tol_0.02", 0.02, 256), ("screen_audit_only", float("inf"), 4096)):
+        screen_maps = make_maps(n, 20261203 + 40)
+        k = max(1, int(np.ceil(0.01 * n)))
+        audit_gen = Generator(group=k)
+        _, st = S.screen(net, screen_maps, gen, audit_frac=0.01, tol=tol, batch=4096, audit_gen=audit_gen)
+        audit_gen.close()
+        out[key] = {"structures": n, "tolerance": tol if tol != float("inf") else None,
+                    "structures_per_s": st["structures_per_s"], "vs_fdtd": st["structures_per_s"] / fdtd_rate,
+                    "fallback_batches": st["fallback_batches"], "batches": st["batches"],
+                    "audit_rel_l2": st["audit_errors"]}
+    gen.close()
     return out
 
 
@@ -416,6 +468,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-variants", action="store_true", help="skip the FP32 / temporal-blocking line items")
     ap.add_argument("--no-sweep", action="store_true", help="skip the batched 256-structure sweep")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate line item")
     ap.add_argument("--grid", type=int, default=0,
                     help="interior cells per side for a smaller case of the same workload (profiling)")
     args = ap.parse_args()

@@ -212,19 +212,33 @@ class FNO:
             K.op("sg_adam", w, g[k], m, v, self.bf.get(k), w.numel(), lr, b1, b2, eps, c1, c2, wd)
 
     # ------------------------------------------------------------ targets
-    def set_normalisation(self, intensity):
-        """Per-element mean / std of log10 intensity over training targets [N, NT]."""
+    # target "lin" (default): intensity / (mean intensity of its wavelength over
+    # the training set), so the loss weighs the strong lobes as the relative L2
+    # error of the far field does; "log": per-element standardised log10 intensity.
+    def set_normalisation(self, intensity, target="lin"):
         t = self.torch
-        lg = t.log10(intensity.reshape(-1, NT).double() + FLOOR)
-        self.mu = lg.mean(0).float()
-        self.sd = (lg.std(0) + 1e-3).float()
+        self.target = target
+        I = intensity.reshape(-1, 31, 360).double()
+        if target == "log":
+            lg = t.log10(I.reshape(-1, NT) + FLOOR)
+            self.mu = lg.mean(0).float()
+            self.sd = (lg.std(0) + 1e-3).float()
+        else:
+            scale = I.mean(dim=(0, 2))  # per wavelength
+            self.mu = t.zeros(NT, device="cuda")
+            self.sd = scale[:, None].expand(31, 360).reshape(NT).float().contiguous()
 
     def encode(self, intensity):
         t = self.torch
-        return ((t.log10(intensity.reshape(-1, NT) + FLOOR) - self.mu) / self.sd).float().contiguous()
+        I = intensity.reshape(-1, NT)
+        if getattr(self, "target", "lin") == "log":
+            return ((t.log10(I + FLOOR) - self.mu) / self.sd).float().contiguous()
+        return (I / self.sd).float().contiguous()
 
     def decode(self, out):
-        return 10.0 ** (out[:, :NT] * self.sd + self.mu) - FLOOR
+        if getattr(self, "target", "lin") == "log":
+            return 10.0 ** (out[:, :NT] * self.sd + self.mu) - FLOOR
+        return out[:, :NT] * self.sd
 
     def predict(self, maps_u8, batch=4096):
         """Far-field intensity [N, 31, 360] of uint8 maps on the device."""

@@ -1,0 +1,132 @@
+"""Training, evaluation and audited screening of the far-field surrogate.
+
+screen() is the sweep path with the network: predict every structure, audit
+a fraction of them with the batched FDTD engine, and fall back to FDTD for a
+whole screening batch when an audited structure's relative far-field error is
+above the tolerance.  The error of a structure is the relative L2 norm of its
+31 x 360 far-field intensity against FDTD.
+"""
+from __future__ import annotations
+
+import math
+import time
+
+import numpy as np
+
+from .data import Generator, make_maps
+from .model import FNO
+
+
+def rel_err(pred, ref):
+    """Per-structure relative L2 error of [N, 31, 360] intensities."""
+    p = np.asarray(pred, np.float64).reshape(len(pred), -1)
+    r = np.asarray(ref, np.float64).reshape(len(ref), -1)
+    return np.linalg.norm(p - r, axis=1) / np.linalg.norm(r, axis=1)
+
+
+def generate(n, seed, gen: Generator):
+    """n maps and their FDTD far fields; returns (maps, intensity, seconds)."""
+    maps = make_maps(n, seed)
+    t = gen.seconds
+    inten = gen.far_field(maps)
+    return maps, inten, gen.seconds - t
+
+
+def mirror(maps, inten):
+    """The mirror image of each structure in y and its far field: with the
+    plane wave along x, y -> -y maps the far-field angle phi to -phi."""
+    ang = (360 - np.arange(360)) % 360
+    return maps[:, :, ::-1].copy(), np.asarray(inten)[:, :, ang].copy()
+
+
+def train(net: FNO, maps, inten, steps=400, batch=128, lr=1e-3, seed=0, log=None, target="lin", augment=True,
+          wd=0.0):
+    """Adam (cosine-decayed learning rate) on minibatches of normalised far
+    fields, the training set doubled by its mirror images; returns seconds."""
+    import torch
+    if augment:
+        mm, mi = mirror(maps, inten)
+        maps = np.concatenate([maps, mm])
+        inten = np.concatenate([inten, mi])
+    target_mode = target
+    dev_maps = torch.tensor(maps, device="cuda")
+    target = torch.tensor(inten, device="cuda")
+    net.set_normalisation(target, target=target_mode)
+    y_all = net.encode(target)
+    x_all = net.pool(dev_maps)
+    n = len(maps)
+    rng = np.random.default_rng(seed)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for it in range(steps):
+        idx = torch.tensor(rng.choice(n, batch, replace=n < batch), device="cuda")
+        frac = it / max(1, steps - 1)
+        step_lr = lr * 0.5 * (1 + math.cos(math.pi * frac))  # cosine decay
+        loss, g = net.loss_and_grads(x_all[idx].contiguous(), y_all[idx].contiguous())
+        net.adam_step(g, lr=step_lr, wd=wd)
+        if log is not None and (it % 100 == 0 or it == steps - 1):
+            log(it, float(loss.mean()))
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0
+
+
+def evaluate(net: FNO, maps, inten, train_inten=None):
+    """Errors of the network and of the network-free baseline (the mean
+    far field of the training set, the best constant prediction)."""
+    import torch
+    pred = net.predict(torch.tensor(maps, device="cuda")).cpu().numpy()
+    err = rel_err(pred, inten)
+    out = {"median": float(np.median(err)), "p90": float(np.percentile(err, 90)),
+           "within_2pct": float(np.mean(err <= 0.02)), "n": int(len(err))}
+    if train_inten is not None:
+        base = np.broadcast_to(np.asarray(train_inten).mean(0), inten.shape)
+        be = rel_err(base, inten)
+        out["baseline_mean_far_field"] = {"median": float(np.median(be)), "p90": float(np.percentile(be, 90)),
+                                          "within_2pct": float(np.mean(be <= 0.02))}
+    return out
+
+
+def inference_rate(net: FNO, n=16384, batch=4096, seed=99):
+    """Structures per second of the network alone (maps already on the GPU)."""
+    import torch
+    maps = torch.tensor(make_maps(min(n, 512), seed), device="cuda")
+    reps = (n + len(maps) - 1) // len(maps)
+    maps = maps.repeat(reps, 1, 1)[:n].contiguous()
+    net.predict(maps[:batch], batch=batch)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    net.predict(maps, batch=batch)
+    torch.cuda.synchronize()
+    return n / (time.perf_counter() - t0)
+
+
+def screen(net: FNO, maps, gen: Generator, audit_frac=0.01, tol=0.02, batch=4096, seed=7, audit_gen=None):
+    """Audited surrogate screening.  Per screening batch: predict all, run
+    FDTD on ceil(audit_frac * batch) random structures (audit_gen: a
+    generator sized for the audit), and if any of them is off by more than
+    tol, replace the batch by FDTD (gen).  Returns (intensity, stats)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    audit_gen = audit_gen or gen
+    out = np.zeros((len(maps), 31, 360), np.float32)
+    stats = {"batches": 0, "fallback_batches": 0, "audited": 0, "audit_errors": [], "seconds": 0.0}
+    t0 = time.perf_counter()
+    for s in range(0, len(maps), batch):
+        part = maps[s:s + batch]
+        pred = net.predict(torch.tensor(part, device="cuda")).cpu().numpy()
+        k = max(1, int(math.ceil(audit_frac * len(part))))
+        pick = rng.choice(len(part), k, replace=False)
+        ref = audit_gen.far_field(part[pick])
+        e = rel_err(pred[pick], ref)
+        stats["batches"] += 1
+        stats["audited"] += k
+        stats["audit_errors"] += [float(v) for v in e]
+        if (e > tol).any():
+            stats["fallback_batches"] += 1
+            pred = gen.far_field(part)
+        else:
+            pred[pick] = ref
+        out[s:s + len(part)] = pred
+    stats["seconds"] = time.perf_counter() - t0
+    stats["structures_per_s"] = len(maps) / stats["seconds"]
+    return out, stats
