@@ -286,7 +286,7 @@ def run_gpu_arm(args):
         cpu = None
         if not args.no_cpu_baseline:
             threads = host_threads()
-            steps = 60
+            steps = 150
             v, dt, n = cpu_sample_run(steps, threads)
             cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": f"{threads} independent {SAMPLE_FIELD[0] // 2}x{SAMPLE_FIELD[1] // 2} instances of "

@@ -1,0 +1,91 @@
+"""Fixed cases for kernel profiling and timing (the commands under profiles/).
+
+    python -m mpifdtd_gb300.profile_case tblock --grid 4096 --k 4 --rows 128 --steps 16 [--precision f32]
+    python -m mpifdtd_gb300.profile_case gemm --m 8192 --n 8192 --kdim 8192
+    python -m mpifdtd_gb300.profile_case all ...    (both, the blocked case first)
+
+tblock: the morpho ridge on a (grid + 32)^2 MPI_TM_UPML grid with temporal
+blocking depth k and tile rows fixed (no autotuning), steps timed with CUDA
+events on the engine's stream.  gemm: C = A B^T in BF16 with FP32 output on
+the surrogate's tcgen05 kernel, timed with CUDA events.  One JSON line each.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+
+def tblock(a):
+    import torch
+
+    import mpifdtd_gb300 as m
+    side = (a.grid + 32) * 2
+    sim = m.Simulation("MPI_TM_UPML", m.FieldInfo(side, side, 2, 16, 500, 0, 20000), a.precision)
+    sim.fill_model(m.MODEL_MORPHO, [600.0, 80.0, 90.0, 8.0, 50.0, 0.0, 2.43, 0.0])
+    sim.set_option(m.OPT_TBLOCK, a.k)
+    sim.set_option(m.OPT_TBLOCK_ROWS, a.rows)
+    sim.run(max(a.k, 4))
+    sim.synchronize()
+    st = torch.cuda.ExternalStream(sim.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sim.profile(True)
+    e0.record(st)
+    sim.run(a.steps)
+    e1.record(st)
+    e1.synchronize()
+    p = sim.profile_read()
+    ms = e0.elapsed_time(e1) / a.steps
+    cells = sim.n_px * sim.n_py
+    stencil = (p["e_half"] + p["h_half"]) / p["steps"]
+    b_alg = 100 if a.precision == "f32" else 200
+    print(json.dumps({"case": "tblock", "grid": [sim.n_px, sim.n_py], "precision": a.precision, "k": a.k,
+                      "rows": a.rows, "steps": a.steps, "ms_per_step": ms, "gcell_per_s": cells / ms / 1e6,
+                      "stencil_ms_per_step": stencil, "stencil_alg_gbs": cells * b_alg / stencil / 1e6,
+                      "ntff_deposit_ms_per_step": p["ntff_deposit"] / p["steps"]}), flush=True)
+    sim.close()
+
+
+def gemm(a):
+    import torch
+
+    from mpifdtd_gb300.surrogate import kernels as K
+    g = torch.Generator(device="cuda").manual_seed(1)
+    A = torch.randn(a.m, a.kdim, device="cuda", generator=g).to(torch.bfloat16)
+    B = torch.randn(a.n, a.kdim, device="cuda", generator=g).to(torch.bfloat16)
+    C = torch.empty(a.m, a.n, device="cuda")
+    for _ in range(3):
+        K.gemm(A, B, C)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 10
+    e0.record()
+    for _ in range(reps):
+        K.gemm(A, B, C)
+    e1.record()
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    flops = 2.0 * a.m * a.n * a.kdim
+    print(json.dumps({"case": "gemm", "m": a.m, "n": a.n, "k": a.kdim, "ms": ms, "tflops": flops / ms / 1e9,
+                      "err_word": int(K.err_word().item())}), flush=True)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(prog="python -m mpifdtd_gb300.profile_case")
+    ap.add_argument("case", choices=["tblock", "gemm", "all"])
+    ap.add_argument("--grid", type=int, default=4096)
+    ap.add_argument("--k", type=int, default=4)
+    ap.add_argument("--rows", type=int, default=128)
+    ap.add_argument("--steps", type=int, default=16)
+    ap.add_argument("--precision", default="f32", choices=["f32", "f64"])
+    ap.add_argument("--m", type=int, default=8192)
+    ap.add_argument("--n", type=int, default=8192)
+    ap.add_argument("--kdim", type=int, default=8192)
+    a = ap.parse_args(argv)
+    if a.case in ("tblock", "all"):
+        tblock(a)
+    if a.case in ("gemm", "all"):
+        gemm(a)
+
+
+if __name__ == "__main__":
+    main()

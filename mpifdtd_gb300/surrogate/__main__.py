@@ -1,0 +1,50 @@
+"""Train and evaluate the far-field surrogate on data from the batched engine.
+
+    python -m mpifdtd_gb300.surrogate --train 4096 --val 256 --steps 3000
+
+Prints one JSON object: FDTD data-generation rate, training time, held-out
+errors (network and network-free baseline), network throughput and the
+audited screening of the held-out maps at the given tolerance."""
+from __future__ import annotations
+
+import argparse
+import json
+import sys
+
+import numpy as np
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(prog="python -m mpifdtd_gb300.surrogate")
+    ap.add_argument("--train", type=int, default=1024)
+    ap.add_argument("--val", type=int, default=256)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--batch", type=int, default=128)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--seed", type=int, default=20261207)
+    ap.add_argument("--tol", type=float, default=0.02)
+    a = ap.parse_args(argv)
+    from .data import Generator
+    from .model import FNO
+    from . import screen as S
+    gen = Generator(group=64)
+    maps, inten, sec = S.generate(a.train + a.val, a.seed, gen)
+    net = FNO(seed=1)
+    t_train = S.train(net, maps[:a.train], inten[:a.train], steps=a.steps, batch=a.batch, lr=a.lr)
+    ev = S.evaluate(net, maps[a.train:], inten[a.train:], inten[:a.train])
+    rate = S.inference_rate(net)
+    k = max(1, int(np.ceil(0.01 * a.val)))
+    audit = Generator(group=k)
+    _, st = S.screen(net, maps[a.train:], gen, audit_frac=0.01, tol=a.tol, batch=a.val, audit_gen=audit)
+    out = {"maps": a.train + a.val, "fdtd_structures_per_s": (a.train + a.val) / sec,
+           "train": {"maps": a.train, "with_mirror_images": 2 * a.train, "steps": a.steps, "seconds": t_train},
+           "heldout_rel_l2": ev, "network_structures_per_s": rate,
+           "screen": {k2: v for k2, v in st.items()}}
+    json.dump(out, sys.stdout)
+    print()
+    audit.close()
+    gen.close()
+
+
+if __name__ == "__main__":
+    main()
