@@ -284,6 +284,7 @@ static int build_ntff(fdtd_sim *s)
   s->h_side.swap(side);
   s->window_dirty = true;
   CK(cudaMalloc(&s->d_vals, sizeof(double2) * 2 * (size_t)n * kMaxNtffBlock));
+  CK(cudaMalloc(&s->d_dg, sizeof(double4) * 2 * (size_t)n * (kMaxNtffBlock + 2)));
   s->ntff_len = (size_t)360 * g.array_size + 2 * kGuard;
   for (int a = 0; a < 3; a++) {
     CK(cudaMalloc(&s->d_ntff[a], sizeof(double2) * s->ntff_len));
@@ -314,6 +315,7 @@ static void free_sim(fdtd_sim *s)
   cudaFree(s->d_cells);
   cudaFree(s->d_shift);
   cudaFree(s->d_vals);
+  cudaFree(s->d_dg);
   for (int a = 0; a < 3; a++) cudaFree(s->d_ntff[a]);
   cudaFree(s->d_status);
   cudaFree(s->d_chunk);
@@ -632,6 +634,7 @@ static NtffView ntff_view(fdtd_sim *s)
   n.shift = (const double *)s->d_shift;
   n.cells = (const SurfCell *)s->d_cells;
   n.vals = (double2 *)s->d_vals;
+  n.dg = (double4 *)s->d_dg;
   n.ncell = s->ncell;
   n.array_size = s->geo.array_size;
   n.len = (long long)s->ntff_len;
@@ -729,7 +732,7 @@ static void enqueue_step(fdtd_sim *s, double time, double ray_coef)
     if (s->nb_pending == s->ntff_block) {
       launch_ntff_block(n, s->nb_pending, s->pending_t0, st);
       s->nb_pending = 0;
-      s->launches += 1;
+      s->launches += 2;  // differences + deposit
     }
   } else if (s->ntff_mode == 1) {
     NtffWindow w{(const int2 *)s->d_chunk, (const int2 *)s->d_lo, s->nchunk, s->win_width};
@@ -749,7 +752,7 @@ static int flush_ntff(fdtd_sim *s)
   if (s->nb_pending == 0) return FDTD_OK;
   launch_ntff_block(ntff_view(s), s->nb_pending, s->pending_t0, s->stream);
   s->nb_pending = 0;
-  s->launches += 1;
+  s->launches += 2;  // differences + deposit
   CK(cudaGetLastError());
   return FDTD_OK;
 }
@@ -932,7 +935,7 @@ static void enqueue_block(fdtd_sim *s, int K)
   if (lines && s->nb_pending == s->ntff_block) {
     launch_ntff_block(n, s->nb_pending, s->pending_t0, st);
     s->nb_pending = 0;
-    s->launches += 1;
+    s->launches += 2;  // differences + deposit
   }
   mark(s);
   if (s->profiling) s->prof_steps += K;

@@ -78,6 +78,7 @@ struct NtffView {
   const double *shift;    // [360][ncell] retarded-time shift per (angle, cell)
   const SurfCell *cells;
   double2 *vals;          // [slot][2][ncell] surface values (E then H) of buffered steps
+  double4 *dg;            // [j][2][ncell] (d_j, e_j): differences of the buffered values (block deposit)
   int ncell, array_size;
   long long len;          // elements of each accumulator incl. guards
   unsigned int *status;   // device status word (kStatus* bits)

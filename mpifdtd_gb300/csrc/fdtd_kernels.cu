@@ -336,10 +336,13 @@ __global__ void __launch_bounds__(256) ntff_window_kernel(NtffView n, NtffWindow
 // rounding gives fl(timeE + sh) = timeE + R(sh) for every step whose t and
 // t + 1/2 stay inside one binade (timeE is then a multiple of the ulp), so
 // m = floor(t + 1/2) advances by exactly one per step and a = 1/2 + t - m is
-// the same every step.  Each step then completes one bin:
-//   bin m-1 : A + v b   (flushed)     bin m : v (a-b) - P     bin m+1 : -v a
-// carried in registers (A, P).  A block whose t range crosses a binade, or a
-// non-integer clock, takes the exact per-step path (deposit()).
+// the same every step.  Bin m0 + j - 1 (j = 0 .. nb+1) then collects
+//   b v_j + (a - b) v_{j-1} - a v_{j-2} = d_j - a e_j,
+//   d_j = v_j - v_{j-1},  e_j = d_j - d_{j-1}   (v outside 0..nb-1 is zero),
+// i.e. one complex FMA per bin on differences that ntff_diff_kernel computes
+// once per path cell for all 360 angles (the first bin, d_0 - a e_0 =
+// fma(-a, v_0, v_0), rounds exactly as v_0 b).  A block whose t range crosses a
+// binade, or a non-integer clock, takes the exact per-step path (deposit()).
 __device__ __forceinline__ int binade(double x) { return (int)((__double_as_longlong(x) >> 52) & 0x7ff); }
 
 __device__ __forceinline__ void red_c(const NtffView &n, double2 *acc, long long at, double2 v)
@@ -352,8 +355,24 @@ __device__ __forceinline__ void red_c(const NtffView &n, double2 *acc, long long
   atomicAdd(&acc[at].y, v.y);
 }
 
+// (d_j, e_j) of every path cell and field, j = 0 .. nb+1
+__global__ void ntff_diff_kernel(NtffView n, int nb)
+{
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int f = blockIdx.y;  // 0: E samples, 1: H samples
+  if (c >= n.ncell) return;
+  double2 vp = make_double2(0.0, 0.0), dp = make_double2(0.0, 0.0);
+  for (int j = 0; j <= nb + 1; j++) {
+    const double2 v = j < nb ? n.vals[(size_t)j * 2 * n.ncell + (size_t)f * n.ncell + c] : make_double2(0.0, 0.0);
+    const double2 d = make_double2(v.x - vp.x, v.y - vp.y);
+    n.dg[((size_t)j * 2 + f) * n.ncell + c] = make_double4(d.x, d.y, d.x - dp.x, d.y - dp.y);
+    vp = v;
+    dp = d;
+  }
+}
+
 __device__ __forceinline__ void block_field(const NtffView &n, double2 *acc, long long row, const double2 *vals,
-                                            int nb, double base, double sh, bool t0_integer)
+                                            const double4 *dg, int nb, double base, double sh, bool t0_integer)
 {
   const double tf = base + sh;
   const double ul = (base + (double)(nb - 1) + sh) + 0.5;
@@ -361,38 +380,32 @@ __device__ __forceinline__ void block_field(const NtffView &n, double2 *acc, lon
   if (t0_integer && tf >= 1.0 && e == binade(ul) && e <= 1023 + 50) {
     const double uf = tf + 0.5;
     const double mf = floor(uf);
-    const double a = uf - mf, b = 1.0 - a, ab = a - b;
+    const double a = uf - mf;
     const long long m0 = row + (long long)mf;
-    double2 A = make_double2(0.0, 0.0), P = make_double2(0.0, 0.0);
-    for (int s = 0; s < nb; s++) {
-      const double2 v = vals[(size_t)s * 2 * n.ncell];
-      double2 f;
-      f.x = fma(v.x, b, A.x);
-      f.y = fma(v.y, b, A.y);
-      red_c(n, acc, m0 + s - 1, f);
-      A.x = fma(v.x, ab, -P.x);
-      A.y = fma(v.y, ab, -P.y);
-      P.x = v.x * a;
-      P.y = v.y * a;
+    for (int j = 0; j <= nb + 1; j++) {
+      const double4 q = dg[(size_t)j * 2 * n.ncell];
+      const double2 f = make_double2(fma(-a, q.z, q.x), fma(-a, q.w, q.y));
+      if (f.x != 0.0 || f.y != 0.0) red_c(n, acc, m0 + j - 1, f);
     }
-    red_c(n, acc, m0 + nb - 1, A);
-    red_c(n, acc, m0 + nb, make_double2(-P.x, -P.y));
     return;
   }
   for (int s = 0; s < nb; s++) deposit(n, acc, row, (base + (double)s) + sh, vals[(size_t)s * 2 * n.ncell]);
 }
 
+// blockIdx.x = angle (fastest, so the 360 blocks of one cell chunk find its
+// differences in L2), blockIdx.y = chunk of 256 path cells
 __global__ void __launch_bounds__(256) ntff_block_kernel(NtffView n, int nb, double t0)
 {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  const int ang = blockIdx.y;
+  const int ang = blockIdx.x;
+  const int c = blockIdx.y * blockDim.x + threadIdx.x;
   if (c >= n.ncell) return;
   const double sh = n.shift[(size_t)ang * n.ncell + c];
   const unsigned char uw = (unsigned char)n.cells[c].uid_wid;
   const long long row = (long long)kGuard + (long long)ang * n.array_size;
   const bool integer_clock = t0 == floor(t0);
-  block_field(n, n.acc[uw & 15], row, n.vals + c, nb, t0, sh, integer_clock);              // E, timeE
-  block_field(n, n.acc[uw >> 4], row, n.vals + n.ncell + c, nb, t0 + 0.5, sh, integer_clock);  // H, timeH
+  block_field(n, n.acc[uw & 15], row, n.vals + c, n.dg + c, nb, t0, sh, integer_clock);  // E, timeE
+  block_field(n, n.acc[uw >> 4], row, n.vals + n.ncell + c, n.dg + n.ncell + c, nb, t0 + 0.5, sh,
+              integer_clock);  // H, timeH
 }
 
 // ------------------------------------------------------------------ launchers
@@ -444,8 +457,9 @@ void launch_ntff_gather(const StencilView<R> &v, const NtffView &n, double coef,
 }
 void launch_ntff_block(const NtffView &n, int nb, double t0, cudaStream_t st)
 {
-  dim3 g((unsigned)((n.ncell + 255) / 256), 360);
-  ntff_block_kernel<<<g, 256, 0, st>>>(n, nb, t0);
+  const unsigned chunks = (unsigned)((n.ncell + 255) / 256);
+  ntff_diff_kernel<<<dim3(chunks, 2), 256, 0, st>>>(n, nb);
+  ntff_block_kernel<<<dim3(360, chunks), 256, 0, st>>>(n, nb, t0);
 }
 void launch_ntff_accumulate(const NtffView &n, double timeE, double timeH, cudaStream_t st)
 {

@@ -25,7 +25,7 @@ struct fdtd_sim {
   void *d_ex = nullptr, *d_ey = nullptr;      // CW phase tables, FP64
   void *d_ex32 = nullptr, *d_ey32 = nullptr;  // and FP32 copies (FP32 fields)
   // NTFF
-  void *d_cells = nullptr, *d_shift = nullptr, *d_vals = nullptr;
+  void *d_cells = nullptr, *d_shift = nullptr, *d_vals = nullptr, *d_dg = nullptr;
   void *d_ntff[3] = {};
   unsigned int *d_status = nullptr;
   int ncell = 0;
