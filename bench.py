@@ -204,6 +204,24 @@ def run_reference_arm(args):
     return 0
 
 
+# ---------------------------------------------------------------- replicas
+
+def max_over_ranks(ms, ws, device):
+    """The slowest rank's time (ms); every rank gets it."""
+    if ws <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(units_per_rank, ws, t_max_ms):
+    """Whole-job throughput in G units/s: every rank's units over the slowest rank's time."""
+    return units_per_rank * ws / (t_max_ms * 1e-3) / 1e9
+
+
 # ---------------------------------------------------------------- GPU arm
 
 def run_gpu_arm(args):
@@ -254,13 +272,8 @@ def run_gpu_arm(args):
     launches = sim.launches - launches0
     if sim.status != 0:
         raise RuntimeError(f"engine status {sim.status:#x}")
-    t_max = ms
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = cells * args.steps * ws / (t_max * 1e-3) / 1e9
+    t_max = max_over_ranks(ms, ws, "cuda")
+    value = job_value(cells * args.steps, ws, t_max)
 
     # roofline of the stencil pair (E + H half-step kernels)
     peak, peak_src = measured_peak_hbm()

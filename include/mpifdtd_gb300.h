@@ -138,6 +138,20 @@ int fdtd_spectrum(fdtd_sim *sim, double *out);
  * the reference's TE version indexes through an unset sub-domain record. */
 int fdtd_frequency(fdtd_sim *sim, double *out_complex);
 
+/* Running-DFT NTFF (no counterpart in the reference): accumulates, from the
+ * time-blocked NTFF ring (mode 2), sum_t v(t) e^{i w t} of every path sample at
+ * the two 8192-point FFT bins around each wavelength, and at the end forms
+ * the far field of ntff*_TimeOutput at those bins without the 360 x arraySize
+ * accumulators or the FFT.  Call before the first step.  The time-domain
+ * spectrum transforms only the first step_num bins of each angle's series
+ * (ntffTM.c:214-221); the DFT sums every deposit, so the two agree once the
+ * pulse has left the NTFF box.
+ * fdtd_dft_far_field: out[360][2*nlam] complex (lower, upper bin per wavelength).
+ * fdtd_dft_spectrum: out[nlam][360], |E|^2 interpolated as the spectrum is. */
+int fdtd_dft_enable(fdtd_sim *sim, int nlam, const int *lambda_nm);
+int fdtd_dft_far_field(fdtd_sim *sim, double *out_complex);
+int fdtd_dft_spectrum(fdtd_sim *sim, double *out);
+
 /* reset() of the solvers (mpiTM_UPML.c:219-232): zero every field; the
  * serial solvers also zero the NTFF arrays (fdtdTM_upml.c:110-113). The
  * engine clock returns to 0. */

@@ -316,6 +316,10 @@ static void free_sim(fdtd_sim *s)
   cudaFree(s->d_shift);
   cudaFree(s->d_vals);
   cudaFree(s->d_dg);
+  cudaFree(s->d_dft_omega);
+  cudaFree(s->d_dft_P);
+  cudaFree(s->d_dft_S);
+  cudaFree(s->d_dft_X);
   for (int a = 0; a < 3; a++) cudaFree(s->d_ntff[a]);
   cudaFree(s->d_status);
   cudaFree(s->d_chunk);
@@ -661,6 +665,30 @@ static SourceStep pulse_step(const fdtd_sim *s, double time, double gap_x, doubl
   return p;
 }
 
+static DftView dft_view(const fdtd_sim *s)
+{
+  DftView d{};
+  d.omega = (const double *)s->d_dft_omega;
+  d.nfreq = 2 * (int)s->dft_lam.size();
+  d.phasor = (double2 *)s->d_dft_P;
+  d.S = (double2 *)s->d_dft_S;
+  return d;
+}
+
+// Deposits the buffered steps of the time-blocked NTFF (and feeds the running
+// DFT first, while the ring still holds them).
+static void deposit_pending(fdtd_sim *s, const NtffView &n, cudaStream_t st)
+{
+  if (s->nb_pending == 0) return;
+  if (s->d_dft_S) {
+    launch_dft_accumulate(n, dft_view(s), s->nb_pending, s->pending_t0, st);
+    s->launches += 2;
+  }
+  launch_ntff_block(n, s->nb_pending, s->pending_t0, st);
+  s->nb_pending = 0;
+  s->launches += 2;  // differences + deposit
+}
+
 // Records the next profiling event of the step (5 per step) when enabled.
 static void mark(fdtd_sim *s)
 {
@@ -730,9 +758,7 @@ static void enqueue_step(fdtd_sim *s, double time, double ray_coef)
   if (blocked) {
     if (s->nb_pending++ == 0) s->pending_t0 = time - 1;
     if (s->nb_pending == s->ntff_block) {
-      launch_ntff_block(n, s->nb_pending, s->pending_t0, st);
-      s->nb_pending = 0;
-      s->launches += 2;  // differences + deposit
+      deposit_pending(s, n, st);
     }
   } else if (s->ntff_mode == 1) {
     NtffWindow w{(const int2 *)s->d_chunk, (const int2 *)s->d_lo, s->nchunk, s->win_width};
@@ -750,9 +776,7 @@ static void enqueue_step(fdtd_sim *s, double time, double ray_coef)
 static int flush_ntff(fdtd_sim *s)
 {
   if (s->nb_pending == 0) return FDTD_OK;
-  launch_ntff_block(ntff_view(s), s->nb_pending, s->pending_t0, s->stream);
-  s->nb_pending = 0;
-  s->launches += 2;  // differences + deposit
+  deposit_pending(s, ntff_view(s), s->stream);
   CK(cudaGetLastError());
   return FDTD_OK;
 }
@@ -933,9 +957,7 @@ static void enqueue_block(fdtd_sim *s, int K)
   }
   mark(s);
   if (lines && s->nb_pending == s->ntff_block) {
-    launch_ntff_block(n, s->nb_pending, s->pending_t0, st);
-    s->nb_pending = 0;
-    s->launches += 2;  // differences + deposit
+    deposit_pending(s, n, st);
   }
   mark(s);
   if (s->profiling) s->prof_steps += K;
@@ -1247,6 +1269,8 @@ extern "C" int fdtd_reset(fdtd_sim *s)
   if (int rc = flush_ntff(s)) return rc;
   const size_t bytes = (size_t)s->nxa * s->pitch * s->esize;
   for (int a = 0; a < s->nslots; a++) CK(cudaMemsetAsync(s->d_f[a], 0, bytes, s->stream));
+  if (s->d_dft_S)
+    CK(cudaMemsetAsync(s->d_dft_S, 0, sizeof(double2) * 2 * (size_t)s->ncell * 2 * s->dft_lam.size(), s->stream));
   if (!s->mpi && s->d_ntff[0])
     for (int a = 0; a < 3; a++) CK(cudaMemsetAsync(s->d_ntff[a], 0, sizeof(double2) * s->ntff_len, s->stream));
   CK(cudaStreamSynchronize(s->stream));
@@ -1327,6 +1351,84 @@ extern "C" int fdtd_spectrum(fdtd_sim *s, double *out)
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(out, s->d_spec, sizeof(double) * 321 * 360, cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
+  return FDTD_OK;
+}
+
+// ---------------------------------------------------------------- running DFT
+
+static std::complex<double> spectrum_coef(const fdtd_sim *s)
+{
+  // ntffTM.c:165 / ntffTE.c:25: 1/(4 pi C) * csqrt(2 pi C / (i w))
+  const std::complex<double> q = std::complex<double>(2 * M_PI * kC, 0.0) / std::complex<double>(0.0, s->geo.omega_s);
+  return (1.0 / (4 * M_PI * kC)) * std::sqrt(q);
+}
+
+extern "C" int fdtd_dft_enable(fdtd_sim *s, int nlam, const int *lambda_nm)
+{
+  if (!s || nlam <= 0 || !lambda_nm) return fail(FDTD_E_ARG, "bad wavelength list");
+  if (!s->d_ntff[0]) return fail(FDTD_E_STATE, "no NTFF path (FDTD_CFG_NO_TIME_NTFF)");
+  if (s->ntff_mode != 2) return fail(FDTD_E_STATE, "the running DFT reads the time-blocked NTFF ring (mode 2)");
+  if (int rc = flush_ntff(s)) return rc;
+  std::vector<double> omega;
+  s->dft_lam.assign(lambda_nm, lambda_nm + nlam);
+  s->dft_frac.clear();
+  for (int l : s->dft_lam) {
+    if (l <= 0) return fail(FDTD_E_ARG, "wavelength %d nm", l);
+    const double p = kC * s->cfg.h_u_nm * kNfft / l;  // the spectrum's fractional bin (ntffTM.c:227)
+    const double idx = floor(p);
+    s->dft_frac.push_back(p - idx);
+    omega.push_back(2 * M_PI * idx / kNfft);
+    omega.push_back(2 * M_PI * (idx + 1) / kNfft);
+  }
+  const int nfreq = (int)omega.size();
+  cudaFree(s->d_dft_omega);
+  cudaFree(s->d_dft_P);
+  cudaFree(s->d_dft_S);
+  cudaFree(s->d_dft_X);
+  s->d_dft_omega = s->d_dft_P = s->d_dft_S = s->d_dft_X = nullptr;
+  CK(cudaMalloc(&s->d_dft_omega, sizeof(double) * nfreq));
+  CK(cudaMemcpy(s->d_dft_omega, omega.data(), sizeof(double) * nfreq, cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&s->d_dft_P, sizeof(double2) * (size_t)kMaxNtffBlock * nfreq));
+  CK(cudaMalloc(&s->d_dft_S, sizeof(double2) * 2 * (size_t)s->ncell * nfreq));
+  CK(cudaMemsetAsync(s->d_dft_S, 0, sizeof(double2) * 2 * (size_t)s->ncell * nfreq, s->stream));
+  CK(cudaMalloc(&s->d_dft_X, sizeof(double2) * 360 * (size_t)nfreq));
+  return FDTD_OK;
+}
+
+// X[360][2 nlam]: the far-field component's Fourier sum at the two bins of each wavelength
+extern "C" int fdtd_dft_far_field(fdtd_sim *s, double *out_complex)
+{
+  if (!s || !out_complex) return fail(FDTD_E_ARG, "null argument");
+  if (!s->d_dft_S) return fail(FDTD_E_STATE, "running DFT not enabled (fdtd_dft_enable)");
+  if (int rc = flush_ntff(s)) return rc;
+  if (int rc = ensure_farfield(s)) return rc;
+  const std::complex<double> c = spectrum_coef(s);
+  const DftView d = dft_view(s);
+  launch_dft_farfield(ntff_view(s), d, s->tm ? 1 : 0, (const double2 *)s->d_dirs, make_double2(c.real(), c.imag()),
+                      (double2 *)s->d_dft_X, s->stream);
+  s->launches += 1;
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out_complex, s->d_dft_X, sizeof(double2) * 360 * (size_t)d.nfreq, cudaMemcpyDeviceToHost,
+                     s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return FDTD_OK;
+}
+
+// out[nlam][360]: |E|^2 per wavelength, the spectrum's interpolation between the two bins
+extern "C" int fdtd_dft_spectrum(fdtd_sim *s, double *out)
+{
+  if (!s || !out) return fail(FDTD_E_ARG, "null argument");
+  const int nlam = (int)s->dft_lam.size();
+  std::vector<double2> X(360 * (size_t)2 * nlam);
+  if (int rc = fdtd_dft_far_field(s, (double *)X.data())) return rc;
+  for (int l = 0; l < nlam; l++) {
+    const double p = s->dft_frac[l];
+    for (int ang = 0; ang < 360; ang++) {
+      const double2 a = X[(size_t)ang * 2 * nlam + 2 * l], b = X[(size_t)ang * 2 * nlam + 2 * l + 1];
+      const double na = a.x * a.x + a.y * a.y, nb = b.x * b.x + b.y * b.y;
+      out[(size_t)l * 360 + ang] = ((1 - p) * na + p * nb) / kNfft;
+    }
+  }
   return FDTD_OK;
 }
 

@@ -1,0 +1,110 @@
+// fdtd_dft.cu -- running-DFT NTFF: the far field at chosen frequencies
+// accumulated during the run instead of the 360 x arraySize time-domain
+// accumulators and their FFT (ntffTM.c:197-275, ntffTE.c:160-238).
+//
+// The time-domain NTFF deposits path value v_c(t) of step t at t + sh(a, c)
+// with the three taps (b, a - b, -a) around m0 = floor(t + sh + 1/2)
+// (mpiTM_UPML.c:840-847, ntffTM.c:279-288).  For integer t, m0 = t + M and
+// a = sh + 1/2 - M are the same every step, so the Fourier sum of one angle's
+// series at frequency w (radians per step, the FFT's e^{+i w m}) factorises:
+//   X_a(w) = sum_c g_a(c) e^{i w M} (b e^{-i w} + (a - b) - a e^{i w}) S_c(w),
+//   S_c(w) = sum_t v_c(t) e^{i w t}
+// with g_a(c) the weight of the cell's accumulator in E_theta (TM) or E_phi
+// (TE) at angle a (ntffTM.c:174-194, ntffTE.c:20-55).  H samples sit at
+// t + 1/2: their M and a come from sh + 1/2.  S_c(w) is accumulated from the
+// buffered path samples of the time-blocked NTFF (every flush of the ring);
+// the far field sums over the path once, at the end.
+#include <cuda_runtime.h>
+
+#include "fdtd_internal.cuh"
+
+namespace fdtd {
+
+namespace {
+
+// P[s][k] = e^{i w_k (t0 + s)}
+__global__ void dft_phasor_kernel(const double *omega, int nfreq, int nb, double t0, double2 *P)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb * nfreq) return;
+  const int s = i / nfreq, k = i % nfreq;
+  double sn, cs;
+  sincos(omega[k] * (t0 + s), &sn, &cs);
+  P[i] = make_double2(cs, sn);
+}
+
+// S[f][c][k] += sum_s vals[s][f][c] P[s][k]; grid (ncell, ceil(nfreq/256), 2)
+__global__ void dft_accumulate_kernel(NtffView n, const double2 *P, double2 *S, int nfreq, int nb)
+{
+  const int c = blockIdx.x, f = blockIdx.z;
+  const int k = blockIdx.y * blockDim.x + threadIdx.x;
+  if (k >= nfreq) return;
+  double2 acc = S[((size_t)f * n.ncell + c) * nfreq + k];
+  for (int s = 0; s < nb; s++) {
+    const double2 v = n.vals[(size_t)s * 2 * n.ncell + (size_t)f * n.ncell + c];
+    const double2 p = P[(size_t)s * nfreq + k];
+    acc.x = fma(v.x, p.x, fma(-v.y, p.y, acc.x));
+    acc.y = fma(v.x, p.y, fma(v.y, p.x, acc.y));
+  }
+  S[((size_t)f * n.ncell + c) * nfreq + k] = acc;
+}
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b)
+{
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// X[a][k] = coef sum_{c, f} g e^{i w M} kappa S ; one block per angle, threads over k
+__global__ void dft_farfield_kernel(NtffView n, const double2 *S, const double *omega, int nfreq, int tm,
+                                    const double2 *dir, double2 coef, double2 *X)
+{
+  const int ang = blockIdx.x;
+  const double2 d = dir[ang];
+  const double px = -d.y, py = d.x, sz = -1.0;
+  // weight of accumulators 0, 1, 2 in the angle's far-field component (spectrum_kernel's combination)
+  double g[3];
+  if (tm) { g[0] = -px; g[1] = -py; g[2] = -kZ0 * sz; }
+  else { g[0] = -kZ0 * px; g[1] = -kZ0 * py; g[2] = sz; }
+  for (int k = threadIdx.x; k < nfreq; k += blockDim.x) {
+    const double w = omega[k];
+    double sw, cw;
+    sincos(w, &sw, &cw);
+    double2 sum = make_double2(0.0, 0.0);
+    for (int c = 0; c < n.ncell; c++) {
+      const double sh = n.shift[(size_t)ang * n.ncell + c];
+      const unsigned char uw = (unsigned char)n.cells[c].uid_wid;
+      for (int f = 0; f < 2; f++) {
+        const double u = (f == 0 ? sh : sh + 0.5) + 0.5;
+        const double M = floor(u);
+        const double a = u - M, b = 1.0 - a;
+        // kappa = b e^{-iw} + (a - b) - a e^{iw}
+        const double2 kap = make_double2(b * cw + (a - b) - a * cw, -b * sw - a * sw);
+        double sm, cm;
+        sincos(w * M, &sm, &cm);
+        const double2 t = cmul(cmul(make_double2(cm, sm), kap), S[((size_t)f * n.ncell + c) * nfreq + k]);
+        const double gw = g[f == 0 ? (uw & 15) : (uw >> 4)];
+        sum.x += gw * t.x;
+        sum.y += gw * t.y;
+      }
+    }
+    X[(size_t)ang * nfreq + k] = cmul(coef, sum);
+  }
+}
+
+}  // namespace
+
+void launch_dft_accumulate(const NtffView &n, const DftView &d, int nb, double t0, cudaStream_t st)
+{
+  if (nb <= 0 || d.nfreq <= 0) return;
+  dft_phasor_kernel<<<(nb * d.nfreq + 255) / 256, 256, 0, st>>>(d.omega, d.nfreq, nb, t0, d.phasor);
+  dft_accumulate_kernel<<<dim3((unsigned)n.ncell, (unsigned)((d.nfreq + 255) / 256), 2), 256, 0, st>>>(
+      n, d.phasor, d.S, d.nfreq, nb);
+}
+
+void launch_dft_farfield(const NtffView &n, const DftView &d, int tm, const double2 *dir, double2 coef, double2 *X,
+                         cudaStream_t st)
+{
+  dft_farfield_kernel<<<360, 128, 0, st>>>(n, d.S, d.omega, d.nfreq, tm, dir, coef, X);
+}
+
+}  // namespace fdtd

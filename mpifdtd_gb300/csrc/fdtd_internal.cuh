@@ -177,6 +177,17 @@ struct FrequencyView {
   double2 *out;            // [360]
 };
 void launch_spectrum(const SpectrumView &s, cudaStream_t st);
+
+// fdtd_dft.cu: running DFT of the buffered path samples at nfreq frequencies
+struct DftView {
+  const double *omega;  // [nfreq] radians per step
+  int nfreq;
+  double2 *phasor;      // [kMaxNtffBlock][nfreq] scratch
+  double2 *S;           // [2][ncell][nfreq] sum_t v_c(t) e^{i w t} (E samples, H samples)
+};
+void launch_dft_accumulate(const NtffView &n, const DftView &d, int nb, double t0, cudaStream_t st);
+void launch_dft_farfield(const NtffView &n, const DftView &d, int tm, const double2 *dir, double2 coef, double2 *X,
+                         cudaStream_t st);
 void launch_frequency(const FrequencyView &f, cudaStream_t st);
 
 // Sets the calling thread's fdtd_last_error() message and returns code (fdtd_api.cu).

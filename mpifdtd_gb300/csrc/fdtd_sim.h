@@ -54,6 +54,10 @@ struct fdtd_sim {
   // engine clock (field.c:21-22 time, ray_coef)
   double time = 0, ray_coef = 0;
   long long launches = 0;
+  // running-DFT NTFF (fdtd_dft_enable): two FFT bins per wavelength
+  std::vector<int> dft_lam;
+  std::vector<double> dft_frac;  // interpolation weight of the upper bin per wavelength
+  void *d_dft_omega = nullptr, *d_dft_P = nullptr, *d_dft_S = nullptr, *d_dft_X = nullptr;
   // far-field outputs (allocated on first use)
   void *d_spec = nullptr, *d_dirs = nullptr, *d_twiddle = nullptr, *d_freq = nullptr;
   // per-kernel event timing (fdtd_profile_*): 5 events per step

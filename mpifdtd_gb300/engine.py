@@ -108,6 +108,9 @@ def load():
         "fdtd_get_option": (I, [P, I, C.POINTER(I)]),
         "fdtd_autotune": (I, [P, C.POINTER(I), C.POINTER(I), dp]),
         "fdtd_autotune_report": (I, [P, dp, I]),
+        "fdtd_dft_enable": (I, [P, I, C.POINTER(I)]),
+        "fdtd_dft_far_field": (I, [P, dp]),
+        "fdtd_dft_spectrum": (I, [P, dp]),
         "fdtd_batch_create": (I, [I, P, I, C.POINTER(P)]),
         "fdtd_batch_destroy": (I, [P]),
         "fdtd_batch_size": (I, [P]),
@@ -301,6 +304,23 @@ class Simulation:
         v = C.c_int()
         _check(self.lib.fdtd_get_option(self.h, int(key), C.byref(v)))
         return v.value
+
+    def dft_enable(self, lambdas_nm):
+        """Running-DFT NTFF at these wavelengths (nm); call before the first step."""
+        lam = np.ascontiguousarray(lambdas_nm, dtype=np.int32)
+        self._dft_n = int(lam.size)
+        _check(self.lib.fdtd_dft_enable(self.h, self._dft_n, lam.ctypes.data_as(C.POINTER(C.c_int))))
+
+    def dft_far_field(self) -> np.ndarray:
+        out = np.empty((360, 2 * self._dft_n), dtype=np.complex128)
+        _check(self.lib.fdtd_dft_far_field(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def dft_spectrum(self) -> np.ndarray:
+        """|E|^2 [n_lambda, 360] from the running DFT (the spectrum's interpolation)."""
+        out = np.empty((self._dft_n, 360))
+        _check(self.lib.fdtd_dft_spectrum(self.h, _dptr(out)))
+        return out
 
     def autotune(self) -> dict:
         """Pick the temporal-blocking depth and tile rows on this grid (the
