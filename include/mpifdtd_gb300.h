@@ -188,18 +188,19 @@ int fdtd_get_status(fdtd_sim *sim, unsigned int *flags);
  * fdtd_run or fdtd_update.  fdtd_update (one step per call) never blocks. */
 #define FDTD_OPT_TBLOCK 5
 #define FDTD_OPT_TBLOCK_ROWS 6
+#define FDTD_OPT_TBLOCK_COLS 7   /* columns per lane of a tile: 1 (default), 2 (FP32, K = 2 or 4) */
 int fdtd_set_option(fdtd_sim *sim, int key, int value);
 int fdtd_get_option(fdtd_sim *sim, int key, int *value);
 
 /* Autotuner of the temporal blocking: times the one-step kernels and the
  * blocked kernel at each depth K and tile height on this simulation's own
  * grid and fields (into the spare field set: the state does not change),
- * sets FDTD_OPT_TBLOCK / FDTD_OPT_TBLOCK_ROWS to the fastest and returns them
+ * sets FDTD_OPT_TBLOCK / _ROWS / _COLS to the fastest, returns K and rows
  * with its stencil time per step in ms (*k_out = 0: one-step kernels won). */
 int fdtd_autotune(fdtd_sim *sim, int *k_out, int *rows_out, double *ms_per_step_out);
-/* The candidates the last fdtd_autotune timed: up to cap triples
- * (K, rows, ms per step) into out, K = 0 being the one-step kernels; returns
- * the number of candidates (negative status on error). */
+/* The candidates the last fdtd_autotune timed: up to cap quadruples
+ * (K, rows, columns per lane, ms per step) into out, K = 0 being the one-step
+ * kernels; returns the number of candidates (negative status on error). */
 int fdtd_autotune_report(const fdtd_sim *sim, double *out, int cap);
 
 /* Per-kernel timing with CUDA events recorded on the engine's own stream

@@ -574,6 +574,11 @@ extern "C" int fdtd_set_option(fdtd_sim *s, int key, int value)
     if (value < 0 || value > (1 << 20)) return fail(FDTD_E_ARG, "tile rows must be in [0, 2^20]");
     s->tb_rows = value;
     return FDTD_OK;
+  case FDTD_OPT_TBLOCK_COLS:
+    if (value != 1 && value != 2) return fail(FDTD_E_ARG, "columns per lane must be 1 or 2");
+    if (value == 2 && !s->f32) return fail(FDTD_E_ARG, "two columns per lane need FP32 fields");
+    s->tb_cols = value;
+    return FDTD_OK;
   }
   return fail(FDTD_E_ARG, "unknown option %d", key);
 }
@@ -588,6 +593,7 @@ extern "C" int fdtd_get_option(fdtd_sim *s, int key, int *value)
   case FDTD_OPT_ROWS: *value = s->rows; return FDTD_OK;
   case FDTD_OPT_TBLOCK: *value = s->tblock; return FDTD_OK;
   case FDTD_OPT_TBLOCK_ROWS: *value = s->tb_rows; return FDTD_OK;
+  case FDTD_OPT_TBLOCK_COLS: *value = s->tb_cols; return FDTD_OK;
   }
   return fail(FDTD_E_ARG, "unknown option %d", key);
 }
@@ -791,11 +797,14 @@ static int before_step(fdtd_sim *s, double time)
 
 // ---------------------------------------------------------------- temporal blocking
 
+// Columns per lane for depth K: two (FP32, K = 2 or 4) when FDTD_OPT_TBLOCK_COLS asks for them.
+static int tb_cols_for(const fdtd_sim *s, int K) { return s->tb_cols == 2 && s->f32 && (K == 2 || K == 4) ? 2 : 1; }
+
 // Tile rows when FDTD_OPT_TBLOCK_ROWS is 0: the tallest power of two in
 // [16, 512] that still gives 16 tiles (warps) per SM.
-static int tb_auto_rows(const fdtd_sim *s, int K)
+static int tb_auto_rows(const fdtd_sim *s, int K, int cpl)
 {
-  const int W = 32 - 2 * K;
+  const int W = 32 * cpl - 2 * K;
   const long long nstrip = (s->nj + W - 1) / W;
   int dev = 0, nsm = 152;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev))
@@ -806,21 +815,22 @@ static int tb_auto_rows(const fdtd_sim *s, int K)
   return L;
 }
 
-// Tiles of depth K (strip s: columns 1 + s(32-2K) .., 32 lanes from K columns
-// left of it).  A tile whose cone -- rows r0-K .. r1+K, its 32 lane columns --
+// Tiles of depth K with cpl columns per lane (strip s owns columns
+// o + s W .. o + s W + W - 1, W = 32 cpl - 2K; its lanes start K columns left).  A tile whose cone -- rows r0-K .. r1+K, its 32 lane columns --
 // is PML-free (x = i+ox, y = j+ox inside [in_x0,in_x1) x [in_y0,in_y1)) runs
 // the interior kernel: strips [s0, s1) x rows [ra, rb) in segments of L rows.
 // Everything else is a work-list tile: the row bands above ra and below rb
 // (thin: the PML rows and K more), and the strips outside [s0, s1).
-int fdtd_plan_tiles(const fdtd_sim *s, int K, int L, TilePlan *plan)
+int fdtd_plan_tiles(const fdtd_sim *s, int K, int L, int cpl, TilePlan *plan)
 {
-  const int W = 32 - 2 * K;
-  const int nstrip = (s->nj + W - 1) / W;
+  const int W = 32 * cpl - 2 * K;
+  const int o = cpl == 1 ? 1 : (K & 1);  // first owned column (tblock_tile.cuh origin())
+  const int nstrip = (s->nj + 1 - o + W - 1) / W;  // owned columns o .. o + nstrip W - 1 cover 1..nj
   const int ilo = s->in_x0 - s->ox, ihi = s->in_x1 - s->ox;  // PML-free array rows [ilo, ihi)
   const int jlo = s->in_y0 - s->ox, jhi = s->in_y1 - s->ox;  // PML-free array columns
-  auto strip_in = [&](int st) {
-    const int c = 1 + st * W - K;
-    return c >= jlo && c + 32 <= jhi;
+  auto strip_in = [&](int st) {  // the lanes' 32 cpl columns
+    const int c = o + st * W - K;
+    return c >= jlo && c + 32 * cpl <= jhi;
   };
   int s0 = 0;
   while (s0 < nstrip && !strip_in(s0)) s0++;
@@ -857,7 +867,7 @@ int fdtd_plan_tiles(const fdtd_sim *s, int K, int L, TilePlan *plan)
 
 // The spare field set, the NTFF line buffers, and the tiles of depth K and
 // height L (fdtd_plan_tiles) on the device.
-static int tb_prepare(fdtd_sim *s, int K, int L)
+static int tb_prepare(fdtd_sim *s, int K, int L, int cpl)
 {
   const size_t bytes = (size_t)s->nxa * s->pitch * s->esize;
   if (!s->d_f2[0])
@@ -869,9 +879,9 @@ static int tb_prepare(fdtd_sim *s, int K, int L)
     CK(cudaMalloc(&s->d_tbcol, (size_t)kMaxTBlock * 12 * s->nxa * s->esize));
     CK(cudaMalloc(&s->d_tbrow, (size_t)kMaxTBlock * 12 * s->pitch * s->esize));
   }
-  if (s->tb_built_k == K && s->tb_built_l == L) return FDTD_OK;
+  if (s->tb_built_k == K && s->tb_built_l == L && s->tb_built_c == cpl) return FDTD_OK;
   TilePlan plan;
-  if (int rc = fdtd_plan_tiles(s, K, L, &plan)) return rc;
+  if (int rc = fdtd_plan_tiles(s, K, L, cpl, &plan)) return rc;
   const std::vector<int4> &tiles = plan.general;
   if ((int)tiles.size() > s->tiles_cap) {
     CK(cudaStreamSynchronize(s->stream));
@@ -894,6 +904,7 @@ static int tb_prepare(fdtd_sim *s, int K, int L)
   s->tb_L = L;
   s->tb_built_k = K;
   s->tb_built_l = L;
+  s->tb_built_c = cpl;
   return FDTD_OK;
 }
 
@@ -922,6 +933,7 @@ static TBlockView<R> tblock_view(const fdtd_sim *s, bool lines)
   tb.rb = s->tb_rb;
   tb.nseg = s->tb_nseg;
   tb.L = s->tb_L;
+  tb.cpl = s->tb_built_c;
   return tb;
 }
 
@@ -970,7 +982,7 @@ template <typename R>
 static int autotune_impl(fdtd_sim *s, int *k_out, int *rows_out, double *ms_out)
 {
   cudaStream_t st = s->stream;
-  if (int rc = tb_prepare(s, 1, 16)) return rc;  // allocates the spare set
+  if (int rc = tb_prepare(s, 1, 16, 1)) return rc;  // allocates the spare set
   cudaEvent_t a = nullptr, b = nullptr;
   CK(cudaEventCreate(&a));
   CK(cudaEventCreate(&b));
@@ -1008,14 +1020,16 @@ static int autotune_impl(fdtd_sim *s, int *k_out, int *rows_out, double *ms_out)
       launch_te_h<R>(vs, st);
     }
   });
-  int best_k = 0, best_l = 0;
-  s->tune_table.assign({0.0, 0.0, best});
+  int best_k = 0, best_l = 0, best_c = 1;
+  s->tune_table.assign({0.0, 0.0, 1.0, best});
   const int depths[4] = {1, 2, 4, 8};
   for (int K : depths) {
     if (K == 8 && !s->f32) continue;
+    for (int cpl = 1; cpl <= 2; cpl++) {
+    if (cpl == 2 && !(s->f32 && (K == 2 || K == 4))) continue;
     for (int L = 16; L <= 512; L *= 2) {
       if ((s->ni + L - 1) / L > 65535) continue;
-      if (int rc = tb_prepare(s, K, L)) {
+      if (int rc = tb_prepare(s, K, L, cpl)) {
         cudaEventDestroy(a);
         cudaEventDestroy(b);
         return rc;
@@ -1025,12 +1039,14 @@ static int autotune_impl(fdtd_sim *s, int *k_out, int *rows_out, double *ms_out)
       tb.sc[0] = make_double2(s->ray_coef, 0.0);
       for (int l = 1; l < K; l++) tb.sc[l] = tb.sc[0];
       const double ms = timed([&] { launch_tblock<R>(v, tb, K, s->tm, st); }) / K;
-      s->tune_table.insert(s->tune_table.end(), {(double)K, (double)L, ms});
+      s->tune_table.insert(s->tune_table.end(), {(double)K, (double)L, (double)cpl, ms});
       if (ms < best) {
         best = ms;
         best_k = K;
         best_l = L;
+        best_c = cpl;
       }
+    }
     }
   }
   cudaEventDestroy(a);
@@ -1038,6 +1054,7 @@ static int autotune_impl(fdtd_sim *s, int *k_out, int *rows_out, double *ms_out)
   CK(cudaGetLastError());
   s->tblock = best_k;
   s->tb_rows = best_l;
+  s->tb_cols = best_c;
   if (k_out) *k_out = best_k;
   if (rows_out) *rows_out = best_l;
   if (ms_out) *ms_out = best;
@@ -1056,9 +1073,9 @@ extern "C" int fdtd_autotune(fdtd_sim *s, int *k_out, int *rows_out, double *ms_
 extern "C" int fdtd_autotune_report(const fdtd_sim *s, double *out, int cap)
 {
   if (!s) return -fail(FDTD_E_ARG, "null simulation");
-  const int n = (int)(s->tune_table.size() / 3);
+  const int n = (int)(s->tune_table.size() / 4);
   if (out)
-    for (int q = 0; q < std::min(n, cap) * 3; q++) out[q] = s->tune_table[q];
+    for (int q = 0; q < std::min(n, cap) * 4; q++) out[q] = s->tune_table[q];
   return n;
 }
 
@@ -1133,7 +1150,9 @@ extern "C" int fdtd_run(fdtd_sim *s, int n_steps)
   const bool blocked = K > 0 && s->mpi && (s->ntff_mode == 3 || (s->ntff_mode == 2 && K <= s->ntff_block)) &&
                        n_steps >= K;
   if (blocked)
-    if (int rc = tb_prepare(s, K, s->tb_rows > 0 ? s->tb_rows : tb_auto_rows(s, K))) return rc;
+    if (int rc = tb_prepare(s, K, s->tb_rows > 0 ? s->tb_rows : tb_auto_rows(s, K, tb_cols_for(s, K)),
+                            tb_cols_for(s, K)))
+      return rc;
   for (int q = 0; q < n_steps; q++) {
     if (blocked && n_steps - q >= K) {
       if (s->nb_pending + K > s->ntff_block)

@@ -73,10 +73,15 @@ __global__ void batch_clock_kernel(BatchClock *clk, int K)
   clk->q += 1;
 }
 
-template <typename R, int K> constexpr int batch_min_blocks() { return sizeof(R) * K > 16 ? 3 : 4; }
+// resident blocks per SM of the interior tile kernel (see interior_min_blocks in fdtd_tblock.cu)
+template <typename R, int K, bool TM, int CPL> constexpr int batch_min_blocks()
+{
+  return CPL == 2 ? (K > 2 ? 3 : 4)
+                  : sizeof(R) == 8 ? (K > 2 ? 3 : 4) : (K >= 8 ? 3 : K == 4 ? (TM ? 4 : 5) : 6);
+}
 
-template <typename R, int K, bool AUX, bool TM>
-__global__ void __launch_bounds__(32 * kBWarps, (AUX ? 2 : batch_min_blocks<R, K>()))
+template <typename R, int K, bool AUX, bool TM, int CPL>
+__global__ void __launch_bounds__(32 * kBWarps, (AUX ? 2 : batch_min_blocks<R, K, TM, CPL>()))
     batch_tile_kernel(const BatchInst<R> *__restrict__ inst, const int4 *__restrict__ tiles, int ntiles,
                       const BatchClock *__restrict__ clk)
 {
@@ -89,18 +94,18 @@ __global__ void __launch_bounds__(32 * kBWarps, (AUX ? 2 : batch_min_blocks<R, K
     const int left = I.n_steps - (int)t;
     if (left <= 0) continue;  // finished instance (whole warp)
     const int nlev = left < K ? left : K;
-    if (TM) tile::tm_tile<R, K, AUX>(I.v[p], I.tb[p], tl.y, tl.z, tl.w, nlev);
-    else tile::te_tile<R, K, AUX>(I.v[p], I.tb[p], tl.y, tl.z, tl.w, nlev);
+    if (TM) tile::tm_tile<R, K, AUX, CPL>(I.v[p], I.tb[p], tl.y, tl.z, tl.w, nlev);
+    else tile::te_tile<R, K, AUX, CPL>(I.v[p], I.tb[p], tl.y, tl.z, tl.w, nlev);
   }
 }
 
-template <typename R, int K, bool AUX, bool TM>
+template <typename R, int K, bool AUX, bool TM, int CPL>
 int persistent_grid(int ntiles)
 {
   int dev = 0, nsm = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_tile_kernel<R, K, AUX, TM>, 32 * kBWarps, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_tile_kernel<R, K, AUX, TM, CPL>, 32 * kBWarps, 0);
   cudaGetLastError();
   const int want = (ntiles + kBWarps - 1) / kBWarps;
   return std::max(1, std::min(want, std::max(1, nsm) * std::max(1, per)));
@@ -115,13 +120,13 @@ using namespace fdtd;
 struct fdtd_batch {
   int solver = 0;
   bool tm = false, f32 = false;
-  int K = 4, L = 0;
+  int K = 4, L = 0, cols = 1;
   std::vector<fdtd_sim *> sims;
   cudaStream_t stream = nullptr, stream2 = nullptr;  // stream2: the work-list kernel, forked in the graph
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   void *d_inst = nullptr, *d_tint = nullptr, *d_tgen = nullptr, *d_clock = nullptr, *d_omega = nullptr;
   int n_int = 0, n_gen = 0, grid_int = 0, grid_gen = 0;
-  int planned_k = 0, planned_l = -1;
+  int planned_k = 0, planned_l = -1, planned_c = 0;
   std::vector<int> rows;  // tile rows of each instance
   cudaGraphExec_t graph = nullptr;
   int graph_blocks = 0;
@@ -217,11 +222,19 @@ extern "C" int fdtd_batch_set_option(fdtd_batch *b, int key, int value)
     if (value < 0 || value > (1 << 20)) return set_error(FDTD_E_ARG, "tile rows must be in [0, 2^20]");
     b->L = value;
     return FDTD_OK;
+  case FDTD_OPT_TBLOCK_COLS:
+    if (value != 1 && value != 2) return set_error(FDTD_E_ARG, "columns per lane must be 1 or 2");
+    if (value == 2 && !b->f32) return set_error(FDTD_E_ARG, "two columns per lane need FP32 fields");
+    b->cols = value;
+    return FDTD_OK;
   }
   return set_error(FDTD_E_ARG, "unknown batch option %d", key);
 }
 
 extern "C" long long fdtd_batch_launch_count(const fdtd_batch *b) { return b ? b->launches : 0; }
+
+// columns per lane: two (FP32, K = 2 or 4) when asked for
+static int batch_cols(const fdtd_batch *b) { return b->cols == 2 && b->f32 && (b->K == 2 || b->K == 4) ? 2 : 1; }
 
 // rows per interior tile segment of one instance (the work-list over all
 // instances provides the parallelism; the PML bands get their own thin tiles)
@@ -275,7 +288,7 @@ static int batch_plan(fdtd_batch *b)
       }
     const int L = batch_rows(b, s);
     TilePlan plan;
-    if (int rc = fdtd_plan_tiles(s, K, L, &plan)) return rc;
+    if (int rc = fdtd_plan_tiles(s, K, L, batch_cols(b), &plan)) return rc;
     for (int g = 0; g < plan.nseg; g++) {
       const int r0 = plan.ra + g * L, r1 = std::min(r0 + L, plan.rb);
       for (int st = plan.s0; st < plan.s1; st++) tint.push_back(make_int4(i, st, r0, r1));
@@ -306,10 +319,11 @@ static int batch_plan(fdtd_batch *b)
   }
   b->planned_k = K;
   b->planned_l = b->L;
+  b->planned_c = batch_cols(b);
   return FDTD_OK;
 }
 
-template <typename R, int K, bool TM>
+template <typename R, int K, bool TM, int CPL>
 static void batch_block(fdtd_batch *b)
 {
   cudaStream_t st = b->stream;
@@ -321,46 +335,58 @@ static void batch_block(fdtd_batch *b)
   cudaEventRecord(b->ev_fork, st);
   cudaStreamWaitEvent(b->stream2, b->ev_fork, 0);
   if (b->n_gen > 0)
-    batch_tile_kernel<R, K, true, TM><<<b->grid_gen, 32 * kBWarps, 0, b->stream2>>>(
+    batch_tile_kernel<R, K, true, TM, CPL><<<b->grid_gen, 32 * kBWarps, 0, b->stream2>>>(
         inst, (const int4 *)b->d_tgen, b->n_gen, clk);
   cudaEventRecord(b->ev_join, b->stream2);
   if (b->n_int > 0)
-    batch_tile_kernel<R, K, false, TM><<<b->grid_int, 32 * kBWarps, 0, st>>>(inst, (const int4 *)b->d_tint,
+    batch_tile_kernel<R, K, false, TM, CPL><<<b->grid_int, 32 * kBWarps, 0, st>>>(inst, (const int4 *)b->d_tint,
                                                                              b->n_int, clk);
   cudaStreamWaitEvent(st, b->ev_join, 0);
   batch_clock_kernel<<<1, 1, 0, st>>>((BatchClock *)b->d_clock, K);
 }
 
 // persistent grid sizes (resident blocks on every SM, at most one warp per tile)
-template <typename R, int K, bool TM>
+template <typename R, int K, bool TM, int CPL>
 static void batch_grids(fdtd_batch *b)
 {
-  b->grid_int = persistent_grid<R, K, false, TM>(b->n_int);
-  b->grid_gen = persistent_grid<R, K, true, TM>(b->n_gen);
+  b->grid_int = persistent_grid<R, K, false, TM, CPL>(b->n_int);
+  b->grid_gen = persistent_grid<R, K, true, TM, CPL>(b->n_gen);
 }
 
-template <typename R>
-static void batch_grids_any(fdtd_batch *b)
+// dispatch on (K, columns per lane, TM) of the batch
+template <typename R, bool GRIDS>
+static void batch_dispatch(fdtd_batch *b)
 {
-  switch (b->K) {
-  case 1: b->tm ? batch_grids<R, 1, true>(b) : batch_grids<R, 1, false>(b); break;
-  case 2: b->tm ? batch_grids<R, 2, true>(b) : batch_grids<R, 2, false>(b); break;
-  case 4: b->tm ? batch_grids<R, 4, true>(b) : batch_grids<R, 4, false>(b); break;
-  default:
-    if (sizeof(R) == 4) b->tm ? batch_grids<R, sizeof(R) == 4 ? 8 : 4, true>(b) : batch_grids<R, sizeof(R) == 4 ? 8 : 4, false>(b);
-    break;
+  constexpr bool f32 = sizeof(R) == 4;
+  const bool tm = b->tm;
+  if (f32 && batch_cols(b) == 2) {
+    if (b->K == 2) {
+      if (GRIDS) tm ? batch_grids<R, 2, true, f32 ? 2 : 1>(b) : batch_grids<R, 2, false, f32 ? 2 : 1>(b);
+      else tm ? batch_block<R, 2, true, f32 ? 2 : 1>(b) : batch_block<R, 2, false, f32 ? 2 : 1>(b);
+    } else {
+      if (GRIDS) tm ? batch_grids<R, 4, true, f32 ? 2 : 1>(b) : batch_grids<R, 4, false, f32 ? 2 : 1>(b);
+      else tm ? batch_block<R, 4, true, f32 ? 2 : 1>(b) : batch_block<R, 4, false, f32 ? 2 : 1>(b);
+    }
+    return;
   }
-}
-
-template <typename R>
-static void batch_block_any(fdtd_batch *b)
-{
   switch (b->K) {
-  case 1: b->tm ? batch_block<R, 1, true>(b) : batch_block<R, 1, false>(b); break;
-  case 2: b->tm ? batch_block<R, 2, true>(b) : batch_block<R, 2, false>(b); break;
-  case 4: b->tm ? batch_block<R, 4, true>(b) : batch_block<R, 4, false>(b); break;
+  case 1:
+    if (GRIDS) tm ? batch_grids<R, 1, true, 1>(b) : batch_grids<R, 1, false, 1>(b);
+    else tm ? batch_block<R, 1, true, 1>(b) : batch_block<R, 1, false, 1>(b);
+    break;
+  case 2:
+    if (GRIDS) tm ? batch_grids<R, 2, true, 1>(b) : batch_grids<R, 2, false, 1>(b);
+    else tm ? batch_block<R, 2, true, 1>(b) : batch_block<R, 2, false, 1>(b);
+    break;
+  case 4:
+    if (GRIDS) tm ? batch_grids<R, 4, true, 1>(b) : batch_grids<R, 4, false, 1>(b);
+    else tm ? batch_block<R, 4, true, 1>(b) : batch_block<R, 4, false, 1>(b);
+    break;
   default:  // 8: FP32 only (checked by fdtd_batch_set_option)
-    if (sizeof(R) == 4) b->tm ? batch_block<R, sizeof(R) == 4 ? 8 : 4, true>(b) : batch_block<R, sizeof(R) == 4 ? 8 : 4, false>(b);
+    if (f32) {
+      if (GRIDS) tm ? batch_grids<R, f32 ? 8 : 4, true, 1>(b) : batch_grids<R, f32 ? 8 : 4, false, 1>(b);
+      else tm ? batch_block<R, f32 ? 8 : 4, true, 1>(b) : batch_block<R, f32 ? 8 : 4, false, 1>(b);
+    }
     break;
   }
 }
@@ -376,10 +402,10 @@ extern "C" int fdtd_batch_run(fdtd_batch *b)
     if (s->time != 0) return set_error(FDTD_E_STATE, "batch_run starts every instance at time 0 (fdtd_reset)");
     max_n = std::max(max_n, s->cfg.step_num);
   }
-  if (b->planned_k != b->K || b->planned_l != b->L) {
+  if (b->planned_k != b->K || b->planned_l != b->L || b->planned_c != batch_cols(b)) {
     if (int rc = b->f32 ? batch_plan<float>(b) : batch_plan<double>(b)) return rc;
-    if (b->f32) batch_grids_any<float>(b);
-    else batch_grids_any<double>(b);
+    if (b->f32) batch_dispatch<float, true>(b);
+    else batch_dispatch<double, true>(b);
   }
   for (fdtd_sim *s : b->sims) BCK(cudaStreamSynchronize(s->stream));
   if (int rc = b->f32 ? batch_descriptors<float>(b) : batch_descriptors<double>(b)) return rc;
@@ -389,8 +415,8 @@ extern "C" int fdtd_batch_run(fdtd_batch *b)
     cudaGraph_t g = nullptr;
     BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     for (int q = 0; q < kGraphBlocks; q++) {
-      if (b->f32) batch_block_any<float>(b);
-      else batch_block_any<double>(b);
+      if (b->f32) batch_dispatch<float, false>(b);
+      else batch_dispatch<double, false>(b);
     }
     const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
     if (ce != cudaSuccess) {

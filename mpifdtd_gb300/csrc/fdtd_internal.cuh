@@ -117,8 +117,9 @@ void launch_ntff_block(const NtffView &n, int nb, double t0, cudaStream_t st);
 // ---- temporally blocked stencil (fdtd_tblock.cu)
 //
 // K steps of an MPI solver per launch.  A warp owns a tile: a strip of
-// 32 - 2K columns (strip s covers columns 1 + s (32-2K) ..) and a row segment
-// [r0, r1).  Interior tiles (cone free of PML and halo) cover strips [s0, s1)
+// W = 32 cpl - 2K columns (cpl columns per lane; strip s owns columns
+// o + s W .. o + s W + W - 1, o = 1 for cpl 1 and K mod 2 for cpl 2) and a row
+// segment [r0, r1).  Interior tiles (cone free of PML and halo) cover strips [s0, s1)
 // x rows [ra, rb) in segments of L rows; every other tile is an entry
 // (strip, r0, r1) of the work-list.  The launch reads the field set of
 // StencilView::f and writes the set `out` (ping-pong), plus the E and H
@@ -139,6 +140,7 @@ struct TBlockView {
   int s0, s1;          // interior kernel: strips [s0, s1) x
   int ra, rb, nseg;    //   rows [ra, rb) in nseg segments of L rows
   int L;
+  int cpl;             // columns per lane: 1, or 2 (FP32, K = 2 or 4)
   double2 sc[kMaxTBlock];  // CW source per level: ray_coef e^{-i w t}
 };
 

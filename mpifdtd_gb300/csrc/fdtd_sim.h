@@ -43,8 +43,9 @@ struct fdtd_sim {
   void *d_tiles = nullptr;      // int4 (strip, r0, r1, -) work-list of the general kernel
   int ntiles = 0, tiles_cap = 0;
   int tb_s0 = 0, tb_s1 = 0, tb_ra = 1, tb_rb = 1, tb_nseg = 0, tb_L = 0;
-  int tb_built_k = 0, tb_built_l = 0;
-  std::vector<double> tune_table;  // last fdtd_autotune: (K, rows, ms per step) per candidate
+  int tb_cols = 1;               // columns per lane (FDTD_OPT_TBLOCK_COLS)
+  int tb_built_k = 0, tb_built_l = 0, tb_built_c = 0;
+  std::vector<double> tune_table;  // last fdtd_autotune: (K, rows, columns per lane, ms per step) per candidate
   int nb_pending = 0;           // buffered steps not yet deposited (mode 2)
   double pending_t0 = 0;        // timeE of the first buffered step
   void *d_chunk = nullptr, *d_lo = nullptr;
@@ -67,14 +68,14 @@ struct fdtd_sim {
   long long prof_steps = 0;
 };
 
-// Temporal-blocking tiles of a simulation (fdtd_api.cu): interior strips
+// Temporal-blocking tiles of a simulation (fdtd_api.cu), cpl columns per lane: interior strips
 // [s0, s1) x rows [ra, rb) in nseg segments of L rows, and the list of the
 // other tiles (strip, r0, r1, 0).
 struct TilePlan {
   int s0 = 0, s1 = 0, ra = 1, rb = 1, L = 0, nseg = 0;
   std::vector<int4> general;
 };
-int fdtd_plan_tiles(const fdtd_sim *s, int K, int L, TilePlan *plan);
+int fdtd_plan_tiles(const fdtd_sim *s, int K, int L, int cpl, TilePlan *plan);
 
 // The stencil view of a simulation's current field set (fdtd_api.cu).
 template <typename R>

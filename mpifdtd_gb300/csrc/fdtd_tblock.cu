@@ -17,33 +17,39 @@ using tile::te_tile;
 
 constexpr int kWarps = 4;  // warps (tiles) per block
 
-// Register cap through the resident-block count: the interior kernel keeps
-// its K levels in at most 128 registers up to 16 bytes of level state per
-// component (FP32 K <= 4, FP64 K <= 2), which leaves 16 warps per SM to hide
-// the HBM latency of the level-0 loads; deeper blocks get 168 (12 warps).
-template <typename R, int K> constexpr int interior_min_blocks() { return sizeof(R) * K > 16 ? 3 : 4; }
+// Register cap through the resident-block count (blocks of 4 warps per SM):
+// measured on the 16416^2 FP32 grid, TM at K = 4 is fastest at 4 blocks (128
+// registers; 5 spills), TE at K = 4 at 5 blocks (102 registers, fewer live
+// values), K <= 2 at 6 blocks; FP64 and K = 8 keep 3-4 (their levels need
+// more registers); two columns per lane double the level state (3-4 blocks).
+template <typename R, int K, bool TM, int CPL> constexpr int interior_min_blocks()
+{
+  return CPL == 2 ? (K > 2 ? 3 : 4)
+                  : sizeof(R) == 8 ? (K > 2 ? 3 : 4) : (K >= 8 ? 3 : K == 4 ? (TM ? 4 : 5) : 6);
+}
 
 // interior tiles: strips [s0, s1) x segments of rows [ra, rb), no auxiliaries
-template <typename R, int K, bool TM>
-__global__ void __launch_bounds__(32 * kWarps, (interior_min_blocks<R, K>())) tblock_interior_kernel(StencilView<R> v, TBlockView<R> tb)
+template <typename R, int K, bool TM, int CPL>
+__global__ void __launch_bounds__(32 * kWarps, (interior_min_blocks<R, K, TM, CPL>()))
+    tblock_interior_kernel(StencilView<R> v, TBlockView<R> tb)
 {
   const int strip = tb.s0 + (int)blockIdx.x * kWarps + (int)(threadIdx.x >> 5);
   if (strip >= tb.s1) return;  // whole warp
   const int r0 = tb.ra + (int)blockIdx.y * tb.L;
   const int r1 = min(r0 + tb.L, tb.rb);
-  if (TM) tm_tile<R, K, false>(v, tb, strip, r0, r1, K);
-  else te_tile<R, K, false>(v, tb, strip, r0, r1, K);
+  if (TM) tm_tile<R, K, false, CPL>(v, tb, strip, r0, r1, K);
+  else te_tile<R, K, false, CPL>(v, tb, strip, r0, r1, K);
 }
 
 // every other tile, from the work-list
-template <typename R, int K, bool TM>
+template <typename R, int K, bool TM, int CPL>
 __global__ void __launch_bounds__(32 * kWarps, 2) tblock_general_kernel(StencilView<R> v, TBlockView<R> tb)
 {
   const int w = (int)blockIdx.x * kWarps + (int)(threadIdx.x >> 5);
   if (w >= tb.ntiles) return;  // whole warp
   const int4 t4 = tb.tiles[w];
-  if (TM) tm_tile<R, K, true>(v, tb, t4.x, t4.y, t4.z, K);
-  else te_tile<R, K, true>(v, tb, t4.x, t4.y, t4.z, K);
+  if (TM) tm_tile<R, K, true, CPL>(v, tb, t4.x, t4.y, t4.z, K);
+  else te_tile<R, K, true, CPL>(v, tb, t4.x, t4.y, t4.z, K);
 }
 
 // NTFF surface samples of level lev from the line buffers (zero on the halo ring)
@@ -98,19 +104,19 @@ __global__ void line_gather_kernel(StencilView<R> v, TBlockView<R> tb, NtffView 
   vals[n.ncell + c] = hv;
 }
 
-template <typename R, int K>
+template <typename R, int K, int CPL>
 void launch_depth(const StencilView<R> &v, const TBlockView<R> &tb, bool tm, cudaStream_t st)
 {
   const dim3 blk(32 * kWarps);
   if (tb.s1 > tb.s0 && tb.nseg > 0) {
     const dim3 g((unsigned)((tb.s1 - tb.s0 + kWarps - 1) / kWarps), (unsigned)tb.nseg);
-    if (tm) tblock_interior_kernel<R, K, true><<<g, blk, 0, st>>>(v, tb);
-    else tblock_interior_kernel<R, K, false><<<g, blk, 0, st>>>(v, tb);
+    if (tm) tblock_interior_kernel<R, K, true, CPL><<<g, blk, 0, st>>>(v, tb);
+    else tblock_interior_kernel<R, K, false, CPL><<<g, blk, 0, st>>>(v, tb);
   }
   if (tb.ntiles > 0) {
     const dim3 g((unsigned)((tb.ntiles + kWarps - 1) / kWarps));
-    if (tm) tblock_general_kernel<R, K, true><<<g, blk, 0, st>>>(v, tb);
-    else tblock_general_kernel<R, K, false><<<g, blk, 0, st>>>(v, tb);
+    if (tm) tblock_general_kernel<R, K, true, CPL><<<g, blk, 0, st>>>(v, tb);
+    else tblock_general_kernel<R, K, false, CPL><<<g, blk, 0, st>>>(v, tb);
   }
 }
 
@@ -119,12 +125,18 @@ void launch_depth(const StencilView<R> &v, const TBlockView<R> &tb, bool tm, cud
 template <typename R>
 void launch_tblock(const StencilView<R> &v, const TBlockView<R> &tb, int K, bool tm, cudaStream_t st)
 {
+  constexpr bool f32 = sizeof(R) == 4;
+  if (f32 && tb.cpl == 2) {  // two columns per lane: K = 2 or 4 (the host checks)
+    if (K == 2) launch_depth<R, 2, f32 ? 2 : 1>(v, tb, tm, st);
+    else if (K == 4) launch_depth<R, 4, f32 ? 2 : 1>(v, tb, tm, st);
+    return;
+  }
   switch (K) {
-  case 1: launch_depth<R, 1>(v, tb, tm, st); break;
-  case 2: launch_depth<R, 2>(v, tb, tm, st); break;
-  case 4: launch_depth<R, 4>(v, tb, tm, st); break;
+  case 1: launch_depth<R, 1, 1>(v, tb, tm, st); break;
+  case 2: launch_depth<R, 2, 1>(v, tb, tm, st); break;
+  case 4: launch_depth<R, 4, 1>(v, tb, tm, st); break;
   case 8:  // FP32 only: eight FP64 levels do not fit the register file
-    if (sizeof(R) == 4) launch_depth<R, sizeof(R) == 4 ? 8 : 4>(v, tb, tm, st);
+    if (f32) launch_depth<R, f32 ? 8 : 4, 1>(v, tb, tm, st);
     break;
   default: break;  // the host accepts 1, 2, 4 and (FP32) 8 only
   }

@@ -22,7 +22,7 @@ F64, F32 = 0, 1
 LAYOUT_GLOBAL, LAYOUT_SOLVER = 0, 1
 MODEL_NONE, MODEL_CIRCLE, MODEL_MORPHO = 0, 1, 3
 OPT_NTFF_MODE, OPT_NTFF_CHUNK, OPT_NTFF_BLOCK, OPT_ROWS = 1, 2, 3, 4
-OPT_TBLOCK, OPT_TBLOCK_ROWS = 5, 6
+OPT_TBLOCK, OPT_TBLOCK_ROWS, OPT_TBLOCK_COLS = 5, 6, 7
 
 _ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "bad state", 5: "unsupported"}
 
@@ -328,10 +328,11 @@ class Simulation:
         k, rows, ms = C.c_int(), C.c_int(), C.c_double()
         _check(self.lib.fdtd_autotune(self.h, C.byref(k), C.byref(rows), C.byref(ms)))
         n = self.lib.fdtd_autotune_report(self.h, None, 0)
-        table = np.zeros(3 * max(n, 0))
+        table = np.zeros(4 * max(n, 0))
         self.lib.fdtd_autotune_report(self.h, _dptr(table), n)
-        return {"tblock": k.value, "tblock_rows": rows.value, "stencil_ms_per_step": ms.value,
-                "candidates": [(int(a), int(b), float(c)) for a, b, c in table.reshape(-1, 3)]}
+        return {"tblock": k.value, "tblock_rows": rows.value, "tblock_cols": self.get_option(OPT_TBLOCK_COLS),
+                "stencil_ms_per_step": ms.value,
+                "candidates": [(int(a), int(b), int(c), float(d)) for a, b, c, d in table.reshape(-1, 4)]}
 
     def fill_model(self, model: int, params=()):
         p = np.ascontiguousarray(params, dtype=np.float64)

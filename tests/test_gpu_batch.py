@@ -69,12 +69,12 @@ def test_batch_rerun_after_reset_is_identical():
     b.close()
 
 
-@pytest.mark.parametrize("k", [2, 4, 8])
-def test_batch_fp32_farfield_within_1e3_of_fp64(k):
+@pytest.mark.parametrize("k,cols", [(2, 1), (4, 1), (8, 1), (2, 2), (4, 2)])
+def test_batch_fp32_farfield_within_1e3_of_fp64(k, cols):
     """FP32 fields (FP64 far-field sums) against the FP64 engine."""
     from mpifdtd_gb300.sweep import farfield_rel_err, mie_sweep, run_batch, run_sequential
     cases = mie_sweep(6)
-    ff32, _, _, _ = run_batch(cases, "f32", tblock=k)
+    ff32, _, _, _ = run_batch(cases, "f32", tblock=k, cols=cols)
     ff64, _, _ = run_sequential(cases, "f64")
     err = farfield_rel_err(ff32, ff64)
     assert err.max() <= 1e-3, err

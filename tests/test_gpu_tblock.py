@@ -112,8 +112,8 @@ def test_tblock_fp64_matches_oracle_c2_grid(solver):
 
 
 @pytest.mark.parametrize("solver", ["MPI_TM_UPML", "MPI_TE_UPML"])
-@pytest.mark.parametrize("k", [1, 2, 4, 8])
-def test_tblock_fp32_equals_fp32_one_step(solver, k):
+@pytest.mark.parametrize("k,cols", [(1, 1), (2, 1), (4, 1), (8, 1), (2, 2), (4, 2)])
+def test_tblock_fp32_equals_fp32_one_step(solver, k, cols):
     m = _engine()
     fi = m.FieldInfo(5220, 5220, 5, 10, 500, 0, 4000)
     sims = []
@@ -121,6 +121,8 @@ def test_tblock_fp32_equals_fp32_one_step(solver, k):
         s = m.Simulation(solver, fi, "f32")
         s.fill_model(m.MODEL_CIRCLE, [500.0, 2.25])
         s.set_option(m.OPT_TBLOCK, kk)
+        s.set_option(m.OPT_TBLOCK_COLS, cols)
+        s.set_option(m.OPT_TBLOCK_ROWS, 48 if cols == 2 else 0)
         s.run(200)
         sims.append(s)
     # same cell arithmetic; the kernels differ only in FMA contraction, so FP32
@@ -160,3 +162,5 @@ def test_tblock_rejects_serial_solver_and_fp64_depth8():
         s.set_option(m.OPT_TBLOCK, 8)
     with pytest.raises(m.FdtdError):
         s.set_option(m.OPT_TBLOCK, 3)
+    with pytest.raises(m.FdtdError):
+        s.set_option(m.OPT_TBLOCK_COLS, 2)   # FP64 fields
