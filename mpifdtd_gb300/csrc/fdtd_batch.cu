@@ -81,7 +81,7 @@ template <typename R, int K, bool TM, int CPL> constexpr int batch_min_blocks()
 }
 
 template <typename R, int K, bool AUX, bool TM, int CPL>
-__global__ void __launch_bounds__(32 * kBWarps, (AUX ? 2 : batch_min_blocks<R, K, TM, CPL>()))
+__global__ void __launch_bounds__(32 * kBWarps, (AUX ? 3 : batch_min_blocks<R, K, TM, CPL>()))
     batch_tile_kernel(const BatchInst<R> *__restrict__ inst, const int4 *__restrict__ tiles, int ntiles,
                       const BatchClock *__restrict__ clk)
 {

@@ -41,9 +41,10 @@ __global__ void __launch_bounds__(32 * kWarps, (interior_min_blocks<R, K, TM, CP
   else te_tile<R, K, false, CPL>(v, tb, strip, r0, r1, K);
 }
 
-// every other tile, from the work-list
+// every other tile, from the work-list (3 resident blocks: 14 % faster on the
+// sweep of small instances, where these tiles are a fifth of the cells, than 2)
 template <typename R, int K, bool TM, int CPL>
-__global__ void __launch_bounds__(32 * kWarps, 2) tblock_general_kernel(StencilView<R> v, TBlockView<R> tb)
+__global__ void __launch_bounds__(32 * kWarps, 3) tblock_general_kernel(StencilView<R> v, TBlockView<R> tb)
 {
   const int w = (int)blockIdx.x * kWarps + (int)(threadIdx.x >> 5);
   if (w >= tb.ntiles) return;  // whole warp
