@@ -346,11 +346,12 @@ def run_variants(m, args, torch, cells, ms_f64):
     if sim.status != 0:
         raise RuntimeError(f"engine status {sim.status:#x}")
     stencil = (prof["e_half"] + prof["h_half"]) / max(1, prof["steps"])
-    one_step = [c for k, _, c in tune["candidates"] if k == 0][0]
+    one_step = [c[-1] for c in tune["candidates"] if c[0] == 0][0]
     b_alg = B_ALG[("tm", "f32")]
     out["fp32_tm"] = {
         "value": cells / (ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms, "speedup_vs_fp64": ms_f64 / ms,
-        "tblock": tune["tblock"], "tblock_rows": tune["tblock_rows"], "stencil_ms_per_step": stencil,
+        "tblock": tune["tblock"], "tblock_rows": tune["tblock_rows"], "tblock_cols": tune["tblock_cols"],
+        "stencil_ms_per_step": stencil,
         "stencil_ms_per_step_one_step_kernels": one_step,
         "stencil_alg_gbs": cells * b_alg / (stencil * 1e-3) / 1e9, "bytes_per_cell_alg": b_alg,
         "ntff_deposit_ms_per_step": prof["ntff_deposit"] / max(1, prof["steps"]),
