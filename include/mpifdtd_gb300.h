@@ -134,8 +134,12 @@ int fdtd_get_ntff_guard(fdtd_sim *sim, int which, double *out_complex, int *guar
  * reference's FFT buffer overflows there, ntffTM.c:214-221). */
 int fdtd_spectrum(fdtd_sim *sim, double *out);
 /* Frequency-domain NTFF of the current fields, ntffTM_Frequency
- * (ntffTM.c:72-158, R0 = 1e6 * 500 nm in cells); out: 360 complex.  TM only:
- * the reference's TE version indexes through an unset sub-domain record. */
+ * (ntffTM.c:72-158: E_z far field) or ntffTE_Frequency (ntffTE.c:242-338:
+ * E_phi), R0 = 1e6 * 500 nm in cells; out: 360 complex.  For TE all four
+ * sides of the path use the global index (the shipped function reads three of
+ * them through field_subIndex, whose sub-domain record field_init no longer
+ * fills, field.c:112).  Angle a is the direction a + 180 degrees of the
+ * e^{-i w t} convention (the transform's kernel is e^{+i k r.r'}). */
 int fdtd_frequency(fdtd_sim *sim, double *out_complex);
 
 /* Running-DFT NTFF (no counterpart in the reference): accumulates, from the

@@ -1454,12 +1454,18 @@ extern "C" int fdtd_dft_spectrum(fdtd_sim *s, double *out)
 extern "C" int fdtd_frequency(fdtd_sim *s, double *out)
 {
   if (!s || !out) return fail(FDTD_E_ARG, "null argument");
-  if (!s->tm) return fail(FDTD_E_UNSUPPORTED, "frequency-domain NTFF is provided for TM (ntffTM.c:72-158) only");
   if (int rc = ensure_farfield(s)) return rc;
   FrequencyView f{};
-  f.e = s->d_f[0];
-  f.h[0] = s->d_f[3];
-  f.h[1] = s->d_f[4];
+  f.tm = s->tm ? 1 : 0;
+  if (s->tm) {  // slots: 0 Ez, 3 Hx, 4 Hy
+    f.e[0] = f.e[1] = s->d_f[0];
+    f.h[0] = s->d_f[3];
+    f.h[1] = s->d_f[4];
+  } else {      // slots: 0 Ex, 1 Ey, 6 Hz
+    f.e[0] = s->d_f[0];
+    f.e[1] = s->d_f[1];
+    f.h[0] = f.h[1] = s->d_f[6];
+  }
   f.f32 = s->f32 ? 1 : 0;   // FP32 fields are widened; the transform stays FP64
   f.P = s->pitch;
   f.ox = s->ox;
@@ -1470,9 +1476,9 @@ extern "C" int fdtd_frequency(fdtd_sim *s, double *out)
   f.cx = s->geo.ntff_cx;
   f.cy = s->geo.ntff_cy;
   f.k_s = s->geo.k_s;
-  f.sqrt_hu = sqrt((double)s->cfg.h_u_nm);
+  f.scale = s->tm ? sqrt((double)s->cfg.h_u_nm) : (double)s->cfg.h_u_nm;  // ntffTM.c:156, ntffTE.c:329
   f.dir = (const double2 *)s->d_dirs + 360;
-  // ntffTM.c:31 R0 = 1e6 * field_toCellUnit(500); ntffTM.c:82 coef
+  // ntffTM.c:31 R0 = 1e6 * field_toCellUnit(500); ntffTM.c:82 / ntffTE.c:256 coef
   const double R0 = 1.0e6 * (500.0 / s->cfg.h_u_nm);
   const std::complex<double> i_k(0.0, s->geo.k_s);
   const std::complex<double> c = std::sqrt(i_k / (8 * M_PI * R0)) * std::exp(i_k * R0);

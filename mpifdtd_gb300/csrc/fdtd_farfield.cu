@@ -6,7 +6,8 @@
 //               ntffTE.c:20-55), zero-padded 8192-point FFT per angle with the
 //               sign of cfft() (cfft.c:104-179: X[k] = sum x[n] e^{+2 pi i nk/N},
 //               no scaling), |E|^2 at 380..700 nm by linear interpolation.
-//   frequency : ntffTM_Frequency (ntffTM.c:72-158) on the current fields.
+//   frequency : ntffTM_Frequency (ntffTM.c:72-158) / ntffTE_Frequency
+//               (ntffTE.c:242-338) on the current fields.
 //
 // One block per angle.  The FFT runs in shared memory (8192 complex doubles =
 // 128 KB): radix-2 decimation in time after a bit-reversal load.
@@ -72,8 +73,16 @@ __global__ void __launch_bounds__(1024) spectrum_kernel(SpectrumView s)
   }
 }
 
-// ntffTM_Frequency: N_z, L_x, L_y integrals over the NTFF path of the current
-// fields, one block per angle; global-frame cell (x, y) is array cell (x-ox, y-ox).
+// Frequency-domain NTFF of the current fields, one block per angle; global
+// cell (x, y) is array cell (x-ox, y-ox).
+//   TM (ntffTM.c:72-158): N_z, L_x, L_y over the four sides lt..rt-1 /
+//     bm..tp-1, path points on the cell (r2 = (i-cx, j-cy)); bottom/right add,
+//     top/left subtract; E = coef (Z0 N_z + L_phi) sqrt(h_u).
+//   TE (ntffTE.c:242-338): N_x, N_y, L_z; the bottom side runs lt..rt
+//     inclusive, points half a cell along the side (i-cx+0.5 / j-cy+0.5);
+//     bottom/right subtract, top/left add; E_phi = coef (Z0 N_phi - L_z) h_u.
+//     All four sides use the global index (the shipped function reads three
+//     of them through field_subIndex, whose SUB_N_PY is never set: field.c:112).
 __device__ __forceinline__ double2 cexp_i(double ph)
 {
   double sn, cs;
@@ -97,33 +106,44 @@ __global__ void __launch_bounds__(256) frequency_kernel(FrequencyView f)
   const int ang = blockIdx.x;
   const double2 d = f.dir[ang];
   const double rx = d.x, ry = d.y;
-  double nz_r = 0, nz_i = 0, lx_r = 0, lx_i = 0, ly_r = 0, ly_i = 0;
-  const int nb = f.rt - f.lt, nr = f.tp - f.bm;
-  const int ncell = 2 * nb + 2 * nr;
+  // a0: N_z (TM) | L_z (TE) ; a1: L_x | N_x (bottom/top) ; a2: L_y | N_y (right/left)
+  double a0r = 0, a0i = 0, a1r = 0, a1i = 0, a2r = 0, a2i = 0;
+  const int te = f.tm ? 0 : 1;
+  const int nb = f.rt - f.lt, nr = f.tp - f.bm, n0 = nb + te;  // bottom: rt inclusive for TE
+  const int ncell = n0 + nb + 2 * nr;
+  const double half = te ? 0.5 : 0.0;
   for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
     int x, y, side;
-    if (c < nb) { side = 0; x = f.lt + c; y = f.bm; }
-    else if (c < nb + nr) { side = 1; x = f.rt; y = f.bm + (c - nb); }
-    else if (c < 2 * nb + nr) { side = 2; x = f.lt + (c - nb - nr); y = f.tp; }
-    else { side = 3; x = f.lt; y = f.bm + (c - 2 * nb - nr); }
+    if (c < n0) { side = 0; x = f.lt + c; y = f.bm; }
+    else if (c < n0 + nr) { side = 1; x = f.rt; y = f.bm + (c - n0); }
+    else if (c < n0 + nb + nr) { side = 2; x = f.lt + (c - n0 - nr); y = f.tp; }
+    else { side = 3; x = f.lt; y = f.bm + (c - n0 - nb - nr); }
+    const bool horiz = side == 0 || side == 2;
     const long long k = (long long)(x - f.ox) * f.P + (y - f.ox);
-    const long long hoff = (side == 0 || side == 2) ? -1 : -(long long)f.P;
-    const void *hp = f.h[side == 0 || side == 2 ? 0 : 1];
-    const double2 ez = load_c(f.e, k, f.f32);
+    const long long hoff = horiz ? -1 : -(long long)f.P;
+    const void *hp = f.h[horiz ? 0 : 1];
+    const double2 ef = load_c(f.e[horiz ? 0 : 1], k, f.f32);
     const double2 ha = load_c(hp, k, f.f32), hb = load_c(hp, k + hoff, f.f32);
     const double hr = 0.5 * (ha.x + hb.x), hi = 0.5 * (ha.y + hb.y);
-    const double inner = __dadd_rn(__dmul_rn(rx, (double)x - f.cx), __dmul_rn(ry, (double)y - f.cy));
+    const double r2x = horiz ? __dadd_rn((double)x - f.cx, half) : (double)x - f.cx;
+    const double r2y = horiz ? (double)y - f.cy : __dadd_rn((double)y - f.cy, half);
+    const double inner = __dadd_rn(__dmul_rn(rx, r2x), __dmul_rn(ry, r2y));
     const double2 e = cexp_i(f.k_s * inner);
-    const double sg = side < 2 ? 1.0 : -1.0;       // bottom/right add, top/left subtract
-    nz_r += sg * (hr * e.x - hi * e.y);
-    nz_i += sg * (hr * e.y + hi * e.x);
-    const double er = sg * (ez.x * e.x - ez.y * e.y), ei = sg * (ez.x * e.y + ez.y * e.x);
-    if (side == 0 || side == 2) { lx_r += er; lx_i += ei; }
-    else { ly_r += er; ly_i += ei; }
+    double sg = side < 2 ? 1.0 : -1.0;  // TM: bottom/right add, top/left subtract
+    if (te) sg = -sg;                   // TE: the other way round
+    const double nr_ = sg * (hr * e.x - hi * e.y), ni_ = sg * (hr * e.y + hi * e.x);
+    const double er = sg * (ef.x * e.x - ef.y * e.y), ei = sg * (ef.x * e.y + ef.y * e.x);
+    if (!te) {
+      a0r += nr_; a0i += ni_;
+      if (horiz) { a1r += er; a1i += ei; } else { a2r += er; a2i += ei; }
+    } else {
+      a0r += er; a0i += ei;
+      if (horiz) { a1r += nr_; a1i += ni_; } else { a2r += nr_; a2i += ni_; }
+    }
   }
-  red[0][threadIdx.x] = nz_r; red[1][threadIdx.x] = nz_i;
-  red[2][threadIdx.x] = lx_r; red[3][threadIdx.x] = lx_i;
-  red[4][threadIdx.x] = ly_r; red[5][threadIdx.x] = ly_i;
+  red[0][threadIdx.x] = a0r; red[1][threadIdx.x] = a0i;
+  red[2][threadIdx.x] = a1r; red[3][threadIdx.x] = a1i;
+  red[4][threadIdx.x] = a2r; red[5][threadIdx.x] = a2i;
   __syncthreads();
   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
     if (threadIdx.x < w)
@@ -131,10 +151,12 @@ __global__ void __launch_bounds__(256) frequency_kernel(FrequencyView f)
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    // Lphi = -Lx sin + Ly cos ; result = coef (Z0 Nz + Lphi) sqrt(h_u)   (ntffTM.c:155-156)
-    const double lpr = -red[2][0] * ry + red[4][0] * rx, lpi = -red[3][0] * ry + red[5][0] * rx;
-    const double br = kZ0 * red[0][0] + lpr, bi = kZ0 * red[1][0] + lpi;
-    f.out[ang] = make_double2((f.coef.x * br - f.coef.y * bi) * f.sqrt_hu, (f.coef.x * bi + f.coef.y * br) * f.sqrt_hu);
+    // phi component of the bottom/top (x) and right/left (y) sums: -x sin + y cos
+    const double pr = -red[2][0] * ry + red[4][0] * rx, pi = -red[3][0] * ry + red[5][0] * rx;
+    double br, bi;
+    if (!te) { br = kZ0 * red[0][0] + pr; bi = kZ0 * red[1][0] + pi; }   // Z0 N_z + L_phi
+    else     { br = kZ0 * pr - red[0][0]; bi = kZ0 * pi - red[1][0]; }    // Z0 N_phi - L_z
+    f.out[ang] = make_double2((f.coef.x * br - f.coef.y * bi) * f.scale, (f.coef.x * bi + f.coef.y * br) * f.scale);
   }
 }
 

@@ -169,13 +169,15 @@ struct SpectrumView {
   double *out;             // [321][360]
 };
 struct FrequencyView {
-  const void *e;           // Ez (global cell (x,y) at array (x-ox)*P + (y-ox))
-  const void *h[2];        // Hx, Hy
+  // global cell (x,y) at array (x-ox)*P + (y-ox)
+  const void *e[2];        // TM: Ez, Ez ; TE: Ex (bottom/top sides), Ey (right/left)
+  const void *h[2];        // TM: Hx (bottom/top), Hy (right/left) ; TE: Hz, Hz
+  int tm;                  // ntffTM_Frequency, else ntffTE_Frequency
   int f32;                 // fields are float2 (FP32 mode) instead of double2
   int P, ox, lt, rt, bm, tp;
-  double cx, cy, k_s, sqrt_hu;
+  double cx, cy, k_s, scale;  // scale: sqrt(h_u_nm) (TM), h_u_nm (TE)
   const double2 *dir;      // [360] (cos, sin)
-  double2 coef;            // csqrt(i k/(8 pi R0)) e^{i k R0}  (ntffTM.c:82)
+  double2 coef;            // csqrt(i k/(8 pi R0)) e^{i k R0}  (ntffTM.c:82, ntffTE.c:256)
   double2 *out;            // [360]
 };
 void launch_spectrum(const SpectrumView &s, cudaStream_t st);

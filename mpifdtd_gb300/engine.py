@@ -280,7 +280,8 @@ class Simulation:
         return out
 
     def frequency(self) -> np.ndarray:
-        """Frequency-domain NTFF of the current fields (360 complex, TM)."""
+        """Frequency-domain NTFF of the current fields (360 complex): E_z far field
+        (TM, ntffTM_Frequency) or E_phi (TE, ntffTE_Frequency)."""
         out = np.empty(360, dtype=np.complex128)
         _check(self.lib.fdtd_frequency(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
         return out

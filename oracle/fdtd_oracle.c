@@ -17,7 +17,8 @@
  *   serial TE UPML        fdtdTE_upml.c:168-192, :252-412; ntffTE.c:57-157
  *   pulse source          field.c:224-256
  *   spectrum output       ntffTM.c:161-275, ntffTE.c:20-55,160-238, cfft.c:104-179
- *   frequency NTFF (TM)   ntffTM.c:72-158
+ *   frequency NTFF        ntffTM.c:72-158, ntffTE.c:242-338 (TE: global index
+ *                         on all four sides, see of_frequency)
  *
  * The MPI solvers are restated for one rank: the sub-domain is the whole grid
  * with a one-cell halo that stays zero (mpiTM_UPML.c:718-748 with
@@ -806,11 +807,54 @@ int of_time_output(of_sim *s, double *out)
   return 0;
 }
 
-/* ntffTM.c:72-158 on global-frame fields (for the MPI solver the one-rank
- * sub-domain is gathered to global x = i-1 first). */
+/* ntffTE.c:242-338 (E_phi of the H-polarised far field) on global-frame Ex,
+ * Ey, Hz.  The shipped function reads the bottom side through field_index and
+ * the other three through field_subIndex, whose SUB_N_PY stays 0 because
+ * field_init no longer calls mpiSplit (field.c:112); here all four sides use
+ * the global index, as ntffTM_Frequency does.  Everything else follows the
+ * shipped loops: the bottom side runs lt..rt inclusive, the others stop before
+ * rt / tp, path points sit half a cell along the side (r2 = i-cx+0.5 or
+ * j-cy+0.5), and the result scales by h_u_nm (not its square root). */
+static void frequency_te(const of_sim *s, const cplx *Ex, const cplx *Ey, const cplx *Hz, int NY, double *out)
+{
+  const double cx = s->cx, cy = s->cy, k_s = s->k_s;
+  const double R0 = 1.0e6 * (500.0 / s->fi.h_u_nm);
+  const double complex coef = csqrt(I * k_s / (8 * M_PI * R0)) * cexp(I * k_s * R0);
+  const int tp = s->top, bm = s->bottom, rt = s->right, lt = s->left;
+  for (int ang = 0; ang < 360; ang++) {
+    double rad = ang * M_PI / 180.0, rx = cos(rad), ry = sin(rad);
+    cplx Nx = 0, Ny = 0, Lz = 0;
+    for (int i = lt; i <= rt; i++) {                       /* n = (0,-1) */
+      int k = i * NY + bm;
+      cplx e = cexp(I * k_s * (rx * (i - cx + 0.5) + ry * (bm - cy)));
+      Nx -= 0.5 * (Hz[k] + Hz[k - 1]) * e; Lz -= Ex[k] * e;
+    }
+    for (int j = bm; j < tp; j++) {                        /* n = (1,0) */
+      int k = rt * NY + j;
+      cplx e = cexp(I * k_s * (rx * (rt - cx) + ry * (j - cy + 0.5)));
+      Ny -= 0.5 * (Hz[k] + Hz[k - NY]) * e; Lz -= Ey[k] * e;
+    }
+    for (int i = lt; i < rt; i++) {                        /* n = (0,1) */
+      int k = i * NY + tp;
+      cplx e = cexp(I * k_s * (rx * (i - cx + 0.5) + ry * (tp - cy)));
+      Nx += 0.5 * (Hz[k] + Hz[k - 1]) * e; Lz += Ex[k] * e;
+    }
+    for (int j = bm; j < tp; j++) {                        /* n = (-1,0) */
+      int k = lt * NY + j;
+      cplx e = cexp(I * k_s * (rx * (lt - cx) + ry * (j - cy + 0.5)));
+      Ny += 0.5 * (Hz[k] + Hz[k - NY]) * e; Lz += Ey[k] * e;
+    }
+    cplx Nphi = -Nx * sin(rad) + Ny * cos(rad);
+    cplx r = coef * (OF_Z0 * Nphi - Lz) * s->fi.h_u_nm;
+    out[2 * ang] = creal(r); out[2 * ang + 1] = cimag(r);
+  }
+}
+
+/* ntffTM.c:72-158 (TM) or ntffTE.c:242-338 (TE, frequency_te) on
+ * global-frame fields (for the MPI solvers the one-rank sub-domain is
+ * gathered to global x = i-1 first). */
 int of_frequency(of_sim *s, double *out)
 {
-  if (!s->tm) return -1;
   const int NX = s->n_px, NY = s->n_py;
   cplx *g[3];
   for (int q = 0; q < 3; q++) {
@@ -819,6 +863,11 @@ int of_frequency(of_sim *s, double *out)
     for (int x = 0; x < NX; x++)
       for (int y = 0; y < NY; y++)
         g[q][x * NY + y] = s->mpi ? src[(x + 1) * s->ny + (y + 1)] : src[x * NY + y];
+  }
+  if (!s->tm) {
+    frequency_te(s, g[0], g[1], g[2], NY, out);
+    for (int q = 0; q < 3; q++) free(g[q]);
+    return 0;
   }
   cplx *Ez = g[0], *Hx = g[1], *Hy = g[2];
   const double cx = s->cx, cy = s->cy, k_s = s->k_s;

@@ -235,7 +235,7 @@ class OracleSim:
         out = np.zeros(720)
         rc = self.lib.of_frequency(self.h, out.ctypes.data_as(C.POINTER(C.c_double)))
         if rc != 0:
-            raise ValueError("frequency-domain NTFF is restated for TM only")
+            raise ValueError("frequency-domain NTFF failed")
         return out.view(np.complex128)
 
 
