@@ -45,6 +45,8 @@ extern "C" {
 #define FDTD_MODEL_MORPHO 3    /* morphoScaleModel.c: {width_nm, thick0_nm, thick1_nm,
                                   layers, branch_nm, edge_rate, eps, per_lamella(0/1),
                                   width_0_nm, width_1_nm, ...}                   */
+#define FDTD_MODEL_ZIGZAG 5    /* zigzagModel.c: {width_nm, thickness_nm, layers,
+                                  degree, n (<=0: 1.56)}                          */
 
 /* Which array: fields (TM: 0 Ez, 1 Hx, 2 Hy; TE: 0 Ex, 1 Ey, 2 Hz),
  * NTFF accumulators (TM: 0 Ux, 1 Uy, 2 Wz; TE: 0 Wx, 1 Wy, 2 Uz). */
@@ -141,6 +143,19 @@ int fdtd_spectrum(fdtd_sim *sim, double *out);
  * fills, field.c:112).  Angle a is the direction a + 180 degrees of the
  * e^{-i w t} convention (the transform's kernel is e^{+i k r.r'}). */
 int fdtd_frequency(fdtd_sim *sim, double *out_complex);
+/* field_outputElliptic (field.c:322-343): |field|^2, bilinear as cbilinear
+ * (myComplex.c:40-52), on the circle of radius 1.2 lambda_s about the grid
+ * centre at ang = 180 .. 0 degrees; out[q] (181 doubles) is printed line
+ * q = 180 - ang.  which: fdtd_get_field numbering (the reference calls it on
+ * Ez for TM, Ey for TE).  A ring that leaves the grid is FDTD_E_ARG. */
+int fdtd_elliptic(fdtd_sim *sim, int which, double *out181);
+/* The same ring written as field_outputElliptic's text file ("%d %lf \n"). */
+int fdtd_write_elliptic(fdtd_sim *sim, int which, const char *path);
+/* drawer_outputImage (drawer.c:253-298): 24-bit BMP of permittivity `which`
+ * in the global frame (the reference draws getEps(): EPS_EZ for TM, EPS_EY
+ * for TE), (N_PX rounded down to a multiple of 4) x N_PY pixels, colour
+ * modelColorTransform (drawer.c:230-251), header as putBmpHeader. */
+int fdtd_write_model_image(fdtd_sim *sim, int which, const char *path);
 
 /* Running-DFT NTFF (no counterpart in the reference): accumulates, from the
  * time-blocked NTFF ring (mode 2), sum_t v(t) e^{i w t} of every path sample at

@@ -474,8 +474,9 @@ extern "C" int fdtd_fill_eps_model(fdtd_sim *s, int model, const double *params,
   if (!s) return fail(FDTD_E_ARG, "null simulation");
   if (n_params < 0 || (n_params > 0 && !params)) return fail(FDTD_E_ARG, "bad parameter vector");
   mdl_params m{};
-  if (model != FDTD_MODEL_NONE && model != FDTD_MODEL_CIRCLE && model != FDTD_MODEL_MORPHO)
-    return fail(FDTD_E_UNSUPPORTED, "model %d is not built in (circle 1, morpho 3, none 0)", model);
+  if (model != FDTD_MODEL_NONE && model != FDTD_MODEL_CIRCLE && model != FDTD_MODEL_MORPHO &&
+      model != FDTD_MODEL_ZIGZAG)
+    return fail(FDTD_E_UNSUPPORTED, "model %d is not built in (none 0, circle 1, morpho 3, zigzag 5)", model);
   if (mdl_init(&m, model, params, n_params, s->geo.n_px, s->geo.n_py, s->geo.n_pml, s->cfg.h_u_nm) != 0)
     return fail(FDTD_E_ARG, "bad parameters for model %d (see mpifdtd_gb300.h)", model);
   launch_eps_model((double *)s->d_eps[0], (double *)s->d_eps[1], (double *)s->d_eps[2], s->pitch, s->nxa,
@@ -1489,5 +1490,144 @@ extern "C" int fdtd_frequency(fdtd_sim *s, double *out)
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(out, s->d_freq, sizeof(double2) * 360, cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
+  return FDTD_OK;
+}
+
+// field_outputElliptic (field.c:322-343): |E|^2 of field `which`, bilinearly
+// interpolated as cbilinear does (myComplex.c:40-52) on the circle of radius
+// 1.2 lambda_s about (N_PX/2, N_PY/2), for ang = 180 down to 0; out[q] is the
+// line the reference prints as "q norm" with q = 180 - ang.  Points whose
+// 2 x 2 corner cells leave the grid are refused (the reference reads outside
+// its array there).
+extern "C" int fdtd_elliptic(fdtd_sim *s, int which, double *out)
+{
+  if (!s || !out) return fail(FDTD_E_ARG, "null argument");
+  const int slot = field_slot(s, which);
+  if (slot < 0) return fail(FDTD_E_ARG, "field index %d out of range", which);
+  const int NX = s->geo.n_px, NY = s->geo.n_py, n = 181;
+  const double lambda_s = s->geo.lambda_s;
+  std::vector<long long> idx(4 * n);
+  std::vector<double> wx(n), wy(n);
+  for (int ang = 180; ang >= 0; ang--) {
+    const int q = 180 - ang;
+    const double rad = ang * M_PI / 180.0;
+    const double x = 1.2 * lambda_s * cos(rad) + NX / 2.0;
+    const double y = 1.2 * lambda_s * sin(rad) + NY / 2.0;
+    const int i = (int)floor(x), j = (int)floor(y);
+    if (i < 0 || j < 0 || i + 1 >= NX || j + 1 >= NY)
+      return fail(FDTD_E_ARG, "elliptic ring point (%.3f, %.3f) at %d deg leaves the %d x %d grid", x, y, ang, NX, NY);
+    wx[q] = x - i;
+    wy[q] = y - j;
+    const long long k = (long long)(i - s->ox) * s->pitch + (j - s->ox);  // p[index] of global (i, j)
+    idx[4 * q + 0] = k;                 // p[index]
+    idx[4 * q + 1] = k + s->pitch;      // p[index + height]
+    idx[4 * q + 2] = k + 1;             // p[index + 1]
+    idx[4 * q + 3] = k + s->pitch + 1;  // p[index + height + 1]
+  }
+  void *d_idx = nullptr, *d_val = nullptr;
+  std::vector<double2> val(4 * n);
+  cudaError_t e = cudaMalloc(&d_idx, sizeof(long long) * idx.size());
+  if (e == cudaSuccess) e = cudaMalloc(&d_val, sizeof(double2) * val.size());
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_idx, idx.data(), sizeof(long long) * idx.size(), cudaMemcpyHostToDevice, s->stream);
+  if (e == cudaSuccess) {
+    launch_point_gather(s->d_f[slot], s->f32 ? 1 : 0, (const long long *)d_idx, 4 * n, (double2 *)d_val, s->stream);
+    s->launches += 1;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(val.data(), d_val, sizeof(double2) * val.size(), cudaMemcpyDeviceToHost, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  cudaFree(d_idx);
+  cudaFree(d_val);
+  if (e != cudaSuccess) return fail(FDTD_E_CUDA, "elliptic ring: %s", cudaGetErrorString(e));
+  for (int q = 0; q < n; q++) {
+    const double dx = wx[q], dy = wy[q];
+    const double2 *p = &val[4 * q];
+    // p[index]*(1-dx)*(1-dy) + p[index+height]*dx*(1-dy) + p[index+1]*(1-dx)*dy + p[index+height+1]*dx*dy
+    const double re = p[0].x * (1.0 - dx) * (1.0 - dy) + p[1].x * dx * (1.0 - dy) + p[2].x * (1.0 - dx) * dy + p[3].x * dx * dy;
+    const double im = p[0].y * (1.0 - dx) * (1.0 - dy) + p[1].y * dx * (1.0 - dy) + p[2].y * (1.0 - dx) * dy + p[3].y * dx * dy;
+    out[q] = re * re + im * im;  // cnorm (myComplex.c:33-38)
+  }
+  return FDTD_OK;
+}
+
+// The text file field_outputElliptic writes: "%d %lf \n" per angle.
+extern "C" int fdtd_write_elliptic(fdtd_sim *s, int which, const char *path)
+{
+  if (!path) return fail(FDTD_E_ARG, "null path");
+  double norm[181];
+  if (int rc = fdtd_elliptic(s, which, norm)) return rc;
+  FILE *fp = fopen(path, "w");
+  if (!fp) return fail(FDTD_E_ARG, "cannot open file %s", path);
+  for (int q = 0; q < 181; q++) fprintf(fp, "%d %lf \n", q, norm[q]);
+  if (fclose(fp) != 0) return fail(FDTD_E_ARG, "cannot write file %s", path);
+  return FDTD_OK;
+}
+
+namespace {
+// modelColorTransform over colorTransform(0) (drawer.c:230-251): green 1 less
+// (1 - 1/n^2) on every channel, channels kept as float like the reference's colorf.
+struct ColorF { float r, g, b; };
+ColorF model_color(double n)
+{
+  ColorF c{0.0f, 1.0f, 0.0f};  // colorTransform(0): a = 0, g = min(1, max(0, 2)) = 1
+  c.r = (float)(c.r - (1 - 1.0 / n / n));
+  c.g = (float)(c.g - (1 - 1.0 / n / n));
+  c.b = (float)(c.b - (1 - 1.0 / n / n));
+  return c;
+}
+// max(0, min(255, v*255)) with the reference's macros (function.h:7-8), stored to a byte
+unsigned char bmp_channel(float v)
+{
+  const float x = v * 255;
+  const float m = 255 < x ? 255.0f : x;
+  return (unsigned char)(0 > m ? 0.0f : m);
+}
+void put_le(std::vector<unsigned char> &b, unsigned long d, int bytes)
+{
+  for (int q = 0; q < bytes; q++) b.push_back((unsigned char)((d >> (8 * q)) & 0xFF));
+}
+}  // namespace
+
+// drawer_outputImage (drawer.c:253-298) with putBmpHeader (drawer.c:312-395):
+// a 24-bit BMP of permittivity `which` in the global frame, (N_PX & ~3) x N_PY
+// pixels, rows of constant y, colour from modelColorTransform.  The header
+// keeps the reference's bfSize = 54 + width * height.  (main.c:146 passes the
+// solver's own eps array, which for the MPI solvers carries the halo ring;
+// this writes the global frame the image is meant to show.)
+extern "C" int fdtd_write_model_image(fdtd_sim *s, int which, const char *path)
+{
+  if (!s || !path) return fail(FDTD_E_ARG, "null argument");
+  const int width = s->geo.n_px, height = s->geo.n_py;
+  const int data_width = (width >> 2) << 2;
+  if (data_width <= 0 || height <= 0) return fail(FDTD_E_ARG, "image of %d x %d cells has no 4-pixel column", width, height);
+  std::vector<double> model((size_t)width * height);
+  if (int rc = fdtd_get_eps(s, which, FDTD_LAYOUT_GLOBAL, model.data())) return rc;
+  std::vector<unsigned char> out;
+  out.reserve(54 + (size_t)height * data_width * 3);
+  out.push_back('B');
+  out.push_back('M');
+  put_le(out, 54 + (unsigned long)data_width * height, 4);  // bfSize
+  put_le(out, 0, 2);
+  put_le(out, 0, 2);
+  put_le(out, 54, 4);          // bfOffBits
+  put_le(out, 40, 4);          // biSize
+  put_le(out, data_width, 4);
+  put_le(out, height, 4);
+  put_le(out, 1, 2);           // planes
+  put_le(out, 24, 2);          // bits per pixel
+  for (int q = 0; q < 6; q++) put_le(out, 0, 4);
+  for (int j = 0; j < height; j++)
+    for (int i = 0; i < data_width; i++) {
+      const ColorF c = model_color(model[(size_t)i * height + j]);
+      out.push_back(bmp_channel(c.b));
+      out.push_back(bmp_channel(c.g));
+      out.push_back(bmp_channel(c.r));
+    }
+  FILE *fp = fopen(path, "wb");
+  if (!fp) return fail(FDTD_E_ARG, "can not open file %s", path);
+  const size_t w = fwrite(out.data(), 1, out.size(), fp);
+  if (fclose(fp) != 0 || w != out.size()) return fail(FDTD_E_ARG, "can not write file %s", path);
   return FDTD_OK;
 }

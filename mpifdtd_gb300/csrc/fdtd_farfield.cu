@@ -173,4 +173,16 @@ void launch_spectrum(const SpectrumView &s, cudaStream_t st)
 
 void launch_frequency(const FrequencyView &f, cudaStream_t st) { frequency_kernel<<<360, 256, 0, st>>>(f); }
 
+// A few field samples at given array indices (the elliptic ring's bilinear corners).
+__global__ void point_gather_kernel(const void *field, int f32, const long long *idx, int n, double2 *out)
+{
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) out[q] = load_c(field, idx[q], f32);
+}
+
+void launch_point_gather(const void *field, int f32, const long long *idx, int n, double2 *out, cudaStream_t st)
+{
+  if (n > 0) point_gather_kernel<<<(n + 255) / 256, 256, 0, st>>>(field, f32, idx, n, out);
+}
+
 }  // namespace fdtd

@@ -193,6 +193,8 @@ void launch_dft_accumulate(const NtffView &n, const DftView &d, int nb, double t
 void launch_dft_farfield(const NtffView &n, const DftView &d, int tm, const double2 *dir, double2 coef, double2 *X,
                          cudaStream_t st);
 void launch_frequency(const FrequencyView &f, cudaStream_t st);
+// out[q] = field[idx[q]] widened to FP64 (FP32 fields: f32 = 1), q < n
+void launch_point_gather(const void *field, int f32, const long long *idx, int n, double2 *out, cudaStream_t st);
 
 // Sets the calling thread's fdtd_last_error() message and returns code (fdtd_api.cu).
 int set_error(int code, const char *fmt, ...);

@@ -139,10 +139,12 @@ double field_pmlCoef_LXY(double ep_mu, double sig) { return 1.0 / (ep_mu + sig);
  *   MIE_CYLINDER (1): {radius_nm, eps}        default {500, 1.6^2}   circleModel.c:6-10
  *   MORPHO_SCALE (3): {width, thick0, thick1, layers, branch, edge_rate, eps,
  *                      per_lamella, widths...} default {300, 90, 90, 6, 0, 0, 1.56^2, 0}
+ *   ZIGZAG (5):       {width, thickness, layers, degree, n} default {300, 80, 5, 10, 1.56}
+ *                                                          zigzagModel.c:9-31
  * Returns 0, -1 on an unknown model. */
 int mpifdtd_models_set_params(int model, const double *p, int n)
 {
-  if (model != 0 && model != 1 && model != 3) return -1;
+  if (model != 0 && model != 1 && model != 3 && model != 5) return -1;
   g_model = model;
   g_nparams = n > 64 ? 64 : n;
   if (g_nparams > 0) memcpy(g_params, p, sizeof(double) * g_nparams);
@@ -153,11 +155,13 @@ void models_setModel(int model)
 {
   static const double circle[2] = {500, 0};
   static const double morpho[8] = {300, 90, 90, 6, 0, 0.0, 0, 0};
+  static const double zigzag[5] = {300, 80, 5, 10, 0};
   if (model == 1 && g_model != 1) mpifdtd_models_set_params(1, circle, 2);
   else if (model == 3 && g_model != 3) mpifdtd_models_set_params(3, morpho, 8);
+  else if (model == 5 && g_model != 5) mpifdtd_models_set_params(5, zigzag, 5);
   else if (model == 0) mpifdtd_models_set_params(0, NULL, 0);
-  else if (model != 1 && model != 3) {
-    printf("mpifdtd_gb300: model %d is not built in (NO_MODEL, MIE_CYLINDER, MORPHO_SCALE)\n", model);
+  else if (model != 1 && model != 3 && model != 5) {
+    printf("mpifdtd_gb300: model %d is not built in (NO_MODEL, MIE_CYLINDER, MORPHO_SCALE, ZIGZAG)\n", model);
     g_model = 0;
   }
 }

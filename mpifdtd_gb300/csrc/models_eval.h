@@ -4,6 +4,7 @@
  *
  *   circleModel.c:27-58   Mie cylinder, 10x10 sub-cell area/line average
  *   morphoScaleModel.c:101-253, :379-422   lamella ridge + trunk
+ *   zigzagModel.c:41-79, :146-161          zig-zag lamellae (thick lines)
  *   noModel.c:5-8
  * dispatched like models_eps (models.c:166-184): D_X -> (col,row) = (1,0),
  * D_Y -> (0,1), D_XY -> (1,1).
@@ -36,6 +37,10 @@ typedef struct mdl_params {
   int layers;
   double width[MDL_MAX_LAYERS], width_max, thick0, thick1, branch, height, ox, oy, ep, edge;
   double a[MDL_MAX_LAYERS], b1[MDL_MAX_LAYERS], b2[MDL_MAX_LAYERS];
+  /* zigzag (cell units); sin/cos of the angle taken once on the host, so the
+   * device evaluates with the host libm's values */
+  int zz_layers;
+  double zz_sin, zz_cos, zz_width, zz_thick, zz_height, zz_exw, zz_exh, zz_ox, zz_oy, zz_ep;
 } mdl_params;
 
 /* circleModel.c:27-58 */
@@ -125,10 +130,42 @@ MDL_FN double mdl_morpho(const mdl_params *m, double x, double y, int col, int r
   return 1.0 * (1 - cnt) + m->ep * cnt;
 }
 
+/* zigzagModel.c:41-79: sub-sample (sx, sy) is inside when its distance to
+ * the centre line of lamella k is at most the thickness; k from the height,
+ * clamped to [0, layers-1] as min(layerNum-1, max(0, .)) does.  pow(v, 2) of
+ * the reference is v * v (one rounding either way). */
+MDL_FN double mdl_zigzag(const mdl_params *m, double _x, double _y, int col, int row)
+{
+  const double x = _x - m->zz_ox, y = _y - m->zz_oy;
+  const double sn = m->zz_sin, cs = m->zz_cos, w = m->zz_width, t = m->zz_thick;
+  const double h = m->zz_height, exw = m->zz_exw, exh = m->zz_exh;
+  if (fabs(x) > w / 2.0 + exw + 0.5 || y < -exh - 0.5 || y > h + exh + 0.5) return 1.0;
+  const double rise = w * sn + cs * t / 2;  /* one lamella's step up */
+  const double px = -w * cs / 2.0;
+  double cnt = 0;
+  const double split = 10, half = split / 2;
+  for (double i = -half + 0.5; i < half; i += 1)
+    for (double j = -half + 0.5; j < half; j += 1) {
+      const double sx = x + col * i / split, sy = y + row * j / split;
+      if (fabs(sx) > w / 2 + exw || sy < -exh || sy > h + exh) continue;
+      const double q = sy / rise;
+      const double qm = 0 > q ? 0 : q;
+      const int k = (int)(m->zz_layers - 1 < qm ? m->zz_layers - 1 : qm);
+      const double py = floor((double)((k + 1) / 2)) * 2 * (w * sn) + k * cs * t / 2;
+      const double vx = (1 - ((k & 1) << 1)) * cs, vy = sn;
+      const double ax = sx - px, ay = sy - py, proj = ax * vx + ay * vy;
+      const double d2 = ax * ax + ay * ay - proj * proj;
+      if (d2 <= t * t) cnt += 1;
+    }
+  cnt /= split * split;
+  return 1.0 * (1 - cnt) + m->zz_ep * cnt;
+}
+
 MDL_FN double mdl_eps(const mdl_params *m, double x, double y, int col, int row)
 {
   if (m->kind == 1) return mdl_circle(m, x, y, col, row);
   if (m->kind == 3) return mdl_morpho(m, x, y, col, row);
+  if (m->kind == 5) return mdl_zigzag(m, x, y, col, row);
   return 1.0;
 }
 
@@ -136,6 +173,8 @@ MDL_FN double mdl_eps(const mdl_params *m, double x, double y, int col, int row)
  * circle p = {radius_nm, eps (<=0: 1.6^2)}
  * morpho p = {width_nm, thick0_nm, thick1_nm, layers, branch_nm, edge_rate, eps (<=0: 1.56^2),
  *             per_lamella (0/1), width_0_nm, width_1_nm, ...}
+ * zigzag p = {width_nm, thickness_nm, layers, degree, n (<=0: N_0 = 1.56)}; the reference's
+ *             statics are integers, so width, thickness, layers and degree are truncated
  * Returns 0, or -1 on a bad parameter vector. */
 MDL_FN int mdl_init(mdl_params *m, int kind, const double *p, int np, int n_px, int n_py, int n_pml, double h_u)
 {
@@ -150,6 +189,24 @@ MDL_FN int mdl_init(mdl_params *m, int kind, const double *p, int np, int n_px, 
     m->posx = n_px / 2;
     m->posy = n_py / 2;
     m->eps_c = (np > 1 && p[1] > 0) ? p[1] : 1.6 * 1.6 * 1.0;
+    return 0;
+  }
+  if (kind == 5) {
+    if (np < 4) return -1;
+    const int width = (int)p[0], thick = (int)p[1], layers = (int)p[2], degree = (int)p[3];
+    if (layers < 1 || width < 0 || thick < 0) return -1;
+    const double rad = degree * M_PI / 180.0;
+    m->zz_layers = layers;
+    m->zz_sin = sin(rad);
+    m->zz_cos = cos(rad);
+    m->zz_width = width / h_u;
+    m->zz_thick = thick / h_u;
+    m->zz_height = (m->zz_width * m->zz_sin) * layers + layers * m->zz_thick / 2 * m->zz_cos;
+    m->zz_exw = m->zz_thick / 2.0 * m->zz_sin;
+    m->zz_exh = m->zz_thick / 2.0 * m->zz_cos;
+    m->zz_ox = n_px / 2.0;
+    m->zz_oy = (n_py - m->zz_height) / 2.0;
+    m->zz_ep = (np > 4 && p[4] > 0) ? p[4] * p[4] * 1.0 : 1.56 * 1.56 * 1.0;
     return 0;
   }
   if (kind == 3) {

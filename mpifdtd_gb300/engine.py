@@ -20,7 +20,7 @@ SOLVERS = {"TM_UPML": TM_UPML_2D, "TE_UPML": TE_UPML_2D,
            "MPI_TM_UPML": MPI_TM_UPML_2D, "MPI_TE_UPML": MPI_TE_UPML_2D}
 F64, F32 = 0, 1
 LAYOUT_GLOBAL, LAYOUT_SOLVER = 0, 1
-MODEL_NONE, MODEL_CIRCLE, MODEL_MORPHO = 0, 1, 3
+MODEL_NONE, MODEL_CIRCLE, MODEL_MORPHO, MODEL_ZIGZAG = 0, 1, 3, 5
 OPT_NTFF_MODE, OPT_NTFF_CHUNK, OPT_NTFF_BLOCK, OPT_ROWS = 1, 2, 3, 4
 OPT_TBLOCK, OPT_TBLOCK_ROWS, OPT_TBLOCK_COLS = 5, 6, 7
 
@@ -102,6 +102,9 @@ def load():
         "fdtd_get_stream": (I, [P, C.POINTER(P)]),
         "fdtd_spectrum": (I, [P, dp]),
         "fdtd_frequency": (I, [P, dp]),
+        "fdtd_elliptic": (I, [P, I, dp]),
+        "fdtd_write_elliptic": (I, [P, I, C.c_char_p]),
+        "fdtd_write_model_image": (I, [P, I, C.c_char_p]),
         "fdtd_profile_enable": (I, [P, I]),
         "fdtd_profile_read": (I, [P, dp, C.POINTER(C.c_longlong)]),
         "fdtd_set_option": (I, [P, I, I]),
@@ -285,6 +288,26 @@ class Simulation:
         out = np.empty(360, dtype=np.complex128)
         _check(self.lib.fdtd_frequency(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
         return out
+
+    def _e_index(self, which):
+        """The E field the reference's outputs use: Ez (TM), Ey (TE)."""
+        return (0 if self.tm else 1) if which is None else int(which)
+
+    def elliptic(self, which=None) -> np.ndarray:
+        """field_outputElliptic's ring: |E|^2 at 181 points of the 1.2 lambda
+        circle, index q = 180 - angle (TM: Ez, TE: Ey unless `which`)."""
+        out = np.empty(181)
+        _check(self.lib.fdtd_elliptic(self.h, self._e_index(which), out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def write_elliptic(self, path, which=None):
+        """The ring as field_outputElliptic's text file."""
+        _check(self.lib.fdtd_write_elliptic(self.h, self._e_index(which), str(path).encode()))
+
+    def write_model_image(self, path, which=None):
+        """drawer_outputImage's 24-bit BMP of the permittivity the solver's
+        getEps() returns (TM: EPS_EZ, TE: EPS_EY unless `which`), global frame."""
+        _check(self.lib.fdtd_write_model_image(self.h, self._e_index(which), str(path).encode()))
 
     def profile(self, on: bool = True):
         """Record CUDA events around every launch class on the engine stream."""

@@ -8,7 +8,8 @@
  *   field parameters      field.c:89-143 (field_init), field.c:312-319 (nextStep)
  *   PML sigma profiles    field.c:259-283
  *   models                noModel.c:5-8, circleModel.c:27-58,74-81,
- *                         morphoScaleModel.c:101-253,379-422, models.c:166-184
+ *                         morphoScaleModel.c:101-253,379-422, zigzagModel.c:41-79,
+ *                         146-161, models.c:166-184
  *   MPI TM UPML (np=1)    mpiTM_UPML.c:196-217 update, :431-530 kernels,
  *                         :337-374 source, :663-716 coefficients, :840-1037 ntff
  *   MPI TE UPML (np=1)    mpiTE_UPML.c:290-304 update, :337-399 kernels,
@@ -67,6 +68,8 @@ struct of_sim {
   double m_width[16], m_width_max, m_thick[2], m_branch, m_height, m_ox, m_oy, m_ep, m_edge;
   int m_layers;
   double m_a[16], m_b1[16], m_b2[16];
+  int z_layers;
+  double z_rad, z_width, z_thick, z_height, z_exw, z_exh, z_ox, z_oy, z_ep;
   /* arrays */
   int nx, ny, ncell, ox;                 /* array dims; global x = i + ox */
   cplx *f[9];
@@ -179,6 +182,34 @@ static double eps_discs(const of_sim *s, double x, double y)
   return e;
 }
 
+/* zigzagModel.c:41-79 eps: lamellae as thick lines zig-zagging up a
+ * trunkless ridge, 10x10 sub-cell area/line average */
+static double eps_zigzag(const of_sim *s, double _x, double _y, int col, int row)
+{
+  double x = _x - s->z_ox, y = _y - s->z_oy;
+  const double rad = s->z_rad, width_s = s->z_width, thickness_s = s->z_thick;
+  const double height_s = s->z_height, exw = s->z_exw, exh = s->z_exh;
+  if (fabs(x) > width_s / 2.0 + exw + 0.5 || y < -exh - 0.5 || y > height_s + exh + 0.5) return OF_EPS0;
+  double cnt = 0;
+  const double split = 10, half = split / 2;
+  for (double i = -half + 0.5; i < half; i += 1)
+    for (double j = -half + 0.5; j < half; j += 1) {
+      double sx = x + col * i / split, sy = y + row * j / split;
+      if (fabs(sx) > width_s / 2 + exw || sy < -exh || sy > height_s + exh) continue;
+      double q = sy / (width_s * sin(rad) + cos(rad) * thickness_s / 2);
+      double m = 0 > q ? 0 : q;
+      int k = (int)(s->z_layers - 1 < m ? s->z_layers - 1 : m);   /* min(layerNum-1, max(0, q)) */
+      double px = -width_s * cos(rad) / 2.0;
+      double py = floor((k + 1) / 2) * 2 * (width_s * sin(rad)) + k * cos(rad) * thickness_s / 2;
+      double vx = (1 - ((k & 1) << 1)) * cos(rad);
+      double vy = sin(rad);
+      double sqr = pow(sx - px, 2) + pow(sy - py, 2) - pow((sx - px) * vx + (sy - py) * vy, 2);
+      if (sqr <= thickness_s * thickness_s) cnt += 1;
+    }
+  cnt /= split * split;
+  return OF_EPS0 * (1 - cnt) + s->z_ep * cnt;
+}
+
 /* models.c:166-184 (D_X -> (1,0), D_Y -> (0,1), D_XY -> (1,1)) */
 static double model_eps(const of_sim *s, double x, double y, int col, int row)
 {
@@ -186,6 +217,7 @@ static double model_eps(const of_sim *s, double x, double y, int col, int row)
   case OF_MODEL_CIRCLE: return eps_circle(s, x, y, col, row);
   case OF_MODEL_MORPHO: return eps_morpho(s, x, y, col, row);
   case OF_MODEL_DISCS: return eps_discs(s, x, y);
+  case OF_MODEL_ZIGZAG: return eps_zigzag(s, x, y, col, row);
   default: return OF_EPS0;
   }
 }
@@ -197,12 +229,24 @@ static double meps(const of_sim *s, double x, double y, int mode)
   return model_eps(s, x, y, 1, 1);
 }
 
-/* circleModel.c:74-81, morphoScaleModel.c:379-422 */
+/* circleModel.c:74-81, morphoScaleModel.c:379-422, zigzagModel.c:146-161 */
 static void model_init(of_sim *s)
 {
   const double *p = s->model.p;
   double hu = s->fi.h_u_nm;
-  if (s->model.kind == OF_MODEL_CIRCLE) {
+  if (s->model.kind == OF_MODEL_ZIGZAG) {
+    const int layers = (int)p[2];
+    s->z_layers = layers;
+    s->z_rad = (int)p[3] * M_PI / 180.0;
+    s->z_width = (int)p[0] / hu;
+    s->z_thick = (int)p[1] / hu;
+    s->z_height = (s->z_width * sin(s->z_rad)) * layers + layers * s->z_thick / 2 * cos(s->z_rad);
+    s->z_exw = s->z_thick / 2.0 * sin(s->z_rad);
+    s->z_exh = s->z_thick / 2.0 * cos(s->z_rad);
+    s->z_ox = s->n_px / 2.0;
+    s->z_oy = (s->n_py - s->z_height) / 2.0;
+    s->z_ep = p[4] > 0 ? p[4] * p[4] * OF_EPS0 : 1.56 * 1.56 * OF_EPS0;
+  } else if (s->model.kind == OF_MODEL_CIRCLE) {
     s->c_radius = p[0] / hu;
     s->c_posx = s->n_px / 2;
     s->c_posy = s->n_py / 2;

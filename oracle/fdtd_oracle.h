@@ -17,11 +17,12 @@ extern "C" {
 /* Solver selection, numbered like enum SOLVER in simulator.h:8-18. */
 enum { OF_TM_UPML = 2, OF_TE_UPML = 3, OF_MPI_TM_UPML = 4, OF_MPI_TE_UPML = 5 };
 
-/* Models: the reference's noModel.c / circleModel.c / morphoScaleModel.c, plus
+/* Models: the reference's noModel.c / circleModel.c / morphoScaleModel.c /
+ * zigzagModel.c, plus
  * a seeded "discs" map used to make golden vectors with permittivity inside the
  * PML and several materials (it goes through the reference's models_eps
  * callback path, models.c:132-150, via the harness). */
-enum { OF_MODEL_NONE = 0, OF_MODEL_CIRCLE = 1, OF_MODEL_MORPHO = 2, OF_MODEL_DISCS = 3 };
+enum { OF_MODEL_NONE = 0, OF_MODEL_CIRCLE = 1, OF_MODEL_MORPHO = 2, OF_MODEL_DISCS = 3, OF_MODEL_ZIGZAG = 4 };
 
 typedef struct of_field_info {      /* field.h:20-28 FieldInfo */
   int width_nm, height_nm, h_u_nm, pml, lambda_nm, angle_deg, step_num;
@@ -29,7 +30,8 @@ typedef struct of_field_info {      /* field.h:20-28 FieldInfo */
 
 /* circle: p = {radius_nm, eps (<=0: N=1.6 default)}
  * morpho: p = {width_nm, thick0_nm, thick1_nm, layers, branch_nm, edge_rate, eps (<=0: 1.56^2)}
- * discs : p = {n, cx0, cy0, r0, eps0, cx1, ...} in cell units, n <= 8           */
+ * discs : p = {n, cx0, cy0, r0, eps0, cx1, ...} in cell units, n <= 8
+ * zigzag: p = {width_nm, thickness_nm, layers, degree, n (<=0: N_0 = 1.56)}     */
 typedef struct of_model { int kind; double p[40]; } of_model;
 
 typedef struct of_sim of_sim;

@@ -31,7 +31,7 @@ REF_SRC = Path(os.environ.get("MPIFDTD_REFERENCE", "/root/reference"))
 TM_UPML_2D, TE_UPML_2D, MPI_TM_UPML_2D, MPI_TE_UPML_2D = 2, 3, 4, 5
 SOLVERS = {"TM_UPML": TM_UPML_2D, "TE_UPML": TE_UPML_2D,
            "MPI_TM_UPML": MPI_TM_UPML_2D, "MPI_TE_UPML": MPI_TE_UPML_2D}
-MODEL_NONE, MODEL_CIRCLE, MODEL_MORPHO, MODEL_DISCS = 0, 1, 2, 3
+MODEL_NONE, MODEL_CIRCLE, MODEL_MORPHO, MODEL_DISCS, MODEL_ZIGZAG = 0, 1, 2, 3, 4
 NFFT = 8192
 
 
@@ -74,6 +74,11 @@ class Model:
         else:
             p += [0.0]
         return Model(MODEL_MORPHO, [float(v) for v in p])
+
+    @staticmethod
+    def zigzag(width_nm=300, thickness_nm=80, layers=5, degree=10, n=0.0):
+        """zigzagModel.c: lamellae at `degree` zig-zagging up; n <= 0: N_0 = 1.56."""
+        return Model(MODEL_ZIGZAG, [float(width_nm), float(thickness_nm), float(layers), float(degree), float(n)])
 
     @staticmethod
     def discs(discs):

@@ -9,17 +9,18 @@ REF     ?= /root/reference
 ORACLE  := $(patsubst %/,%,$(dir $(lastword $(MAKEFILE_LIST))))
 OUT     := $(ORACLE)/_ref
 CC      ?= gcc
+# drawer.c is compiled without USE_OPENGL: only its BMP writer remains.
 # -std=gnu99 and -DLINUX_OS are what the reference needs (function.c:47 guards
 # its directory helpers on LINUX_OS; -std=c99 hides M_PI).  -ffp-contract=off
 # keeps the x86 rounding when this is built on an FMA-capable host.
 CFLAGS  := -std=gnu99 -O3 -fPIC -ffp-contract=off -DLINUX_OS -w -I$(ORACLE)/mpi_stub -I$(REF)
 
 REF_SRCS := field.c simulator.c fdtdTM.c fdtdTE.c nsFdtdTM.c nsFdtdTE.c noModel.c \
-            multiLayerModel.c zigzagModel.c traceImageModel.c concentricCircleModel.c \
-            ntffTM.c ntffTE.c ntff.c cfft.c myComplex.c function.c parser.c
+            multiLayerModel.c traceImageModel.c concentricCircleModel.c \
+            ntffTM.c ntffTE.c ntff.c cfft.c myComplex.c function.c parser.c drawer.c
 HARNESS  := ref_mpi_tm.c ref_mpi_te.c ref_ser_tm.c ref_ser_te.c ref_models.c \
-            ref_circle.c ref_morpho.c ref_driver.c
+            ref_circle.c ref_morpho.c ref_zigzag.c ref_driver.c
 
-$(OUT)/libfdtdref.so: $(addprefix $(REF)/,$(REF_SRCS)) $(addprefix $(ORACLE)/ref_harness/,$(HARNESS)) $(ORACLE)/mpi_stub/mpi.h
+$(OUT)/libfdtdref.so: $(ORACLE)/ref.mk $(addprefix $(REF)/,$(REF_SRCS)) $(addprefix $(ORACLE)/ref_harness/,$(HARNESS)) $(ORACLE)/mpi_stub/mpi.h
 	mkdir -p $(OUT)
 	$(CC) $(CFLAGS) -shared -o $@ $(addprefix $(REF)/,$(REF_SRCS)) $(addprefix $(ORACLE)/ref_harness/,$(HARNESS)) -lm

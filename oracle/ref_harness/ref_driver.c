@@ -20,11 +20,13 @@ extern void refh_circle_set_radius_nm(int r);
 extern void refh_circle_set_eps(double e);
 extern void refh_morpho_set(int width, int thick0, int thick1, int layers, int branch, double edge_rate);
 extern void refh_morpho_set_eps(double e);
+extern void refh_zigzag_set(int width, int thick, int layers, int deg);
 
-enum { RM_NONE = 0, RM_CIRCLE = 1, RM_MORPHO = 2, RM_CALLBACK = 3 };
+enum { RM_NONE = 0, RM_CIRCLE = 1, RM_MORPHO = 2, RM_CALLBACK = 3, RM_ZIGZAG = 4 };
 
 /* model params: circle {radius_nm, eps (<=0: reference default)};
- * morpho {width, thick0, thick1, layers, branch, edge_rate, eps (<=0: default)} */
+ * morpho {width, thick0, thick1, layers, branch, edge_rate, eps (<=0: default)};
+ * zigzag {width, thickness, layers, degree} (index N_0 = 1.56 is a #define) */
 int refh_setup(int solver, int width_nm, int height_nm, int h_u_nm, int pml,
                int lambda_nm, int angle_deg, int step_num,
                int model, const double *mp, double (*cb)(double, double, int, int))
@@ -38,6 +40,10 @@ int refh_setup(int solver, int width_nm, int height_nm, int h_u_nm, int pml,
     refh_morpho_set((int)mp[0], (int)mp[1], (int)mp[2], (int)mp[3], (int)mp[4], mp[5]);
     break;
   case RM_CALLBACK: refh_models_set_callback(cb); break;
+  case RM_ZIGZAG:
+    models_setModel(ZIGZAG);
+    refh_zigzag_set((int)mp[0], (int)mp[1], (int)mp[2], (int)mp[3]);
+    break;
   default: return -1;
   }
   FieldInfo fi;

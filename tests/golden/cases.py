@@ -6,8 +6,9 @@ Each case is run on the reference's own sources compiled unmodified
 kind "full"  : complete fields / eps on the active cells, NTFF rows for the
                angles in NTFF_ROWS plus per-angle sums and norms of every row.
 kind "stats" : per-row sums and norms only (large grids).
-Extras: "spectrum" (ntff*_TimeOutput, serial solvers) and "frequency"
-(ntffTM_Frequency on the final fields).
+Extras: "spectrum" (ntff*_TimeOutput, serial solvers), "frequency"
+(ntffTM_Frequency on the final fields), "elliptic" (field_outputElliptic's
+file of the final E field) and "image" (drawer_outputImage's BMP of eps).
 """
 
 # FieldInfo order (field.h:20-28): width_nm, height_nm, h_u_nm, pml, lambda_nm, angle_deg, step_num
@@ -19,17 +20,24 @@ CASES = {
     "mpi_tm_vacuum_c1": dict(solver="MPI_TM_UPML", fi=(1380, 1380, 5, 10, 400, 0, 2000),
                              model=("none",), steps=2000, kind="stats"),
     "mpi_tm_circle": dict(solver="MPI_TM_UPML", fi=(300, 320, 5, 6, 100, 0, 150),
-                          model=("circle", 60, 0.0), steps=150, kind="full", extras=("frequency",)),
+                          model=("circle", 60, 0.0), steps=150, kind="full",
+                          extras=("frequency", "elliptic", "image")),
     "mpi_te_circle": dict(solver="MPI_TE_UPML", fi=(300, 320, 5, 6, 100, 0, 150),
-                          model=("circle", 60, 0.0), steps=150, kind="full"),
+                          model=("circle", 60, 0.0), steps=150, kind="full", extras=("elliptic", "image")),
     "mpi_tm_discs_30deg": dict(solver="MPI_TM_UPML", fi=(310, 300, 5, 7, 80, 30, 140),
                                model=("discs", DISCS_A), steps=140, kind="full"),
     "mpi_te_discs_60deg": dict(solver="MPI_TE_UPML", fi=(300, 310, 5, 7, 80, 60, 140),
                                model=("discs", DISCS_B), steps=140, kind="full"),
     "mpi_tm_morpho": dict(solver="MPI_TM_UPML", fi=(330, 340, 5, 6, 90, 0, 130),
-                          model=("morpho", 150, 20, 25, 3, 10, 0.5, 0.0), steps=130, kind="full"),
+                          model=("morpho", 150, 20, 25, 3, 10, 0.5, 0.0), steps=130, kind="full",
+                          extras=("image",)),
     "mpi_te_morpho_eps225": dict(solver="MPI_TE_UPML", fi=(330, 340, 5, 6, 90, 15, 130),
                                  model=("morpho", 150, 20, 25, 3, 0, 0.0, 2.25), steps=130, kind="full"),
+    # zigzagModel.c at its first structure (300 nm, 80 nm, 5 layers, 10 deg) and a steeper one
+    "mpi_tm_zigzag": dict(solver="MPI_TM_UPML", fi=(500, 600, 5, 8, 100, 0, 120),
+                          model=("zigzag", 300, 80, 5, 10), steps=120, kind="full", extras=("image",)),
+    "mpi_te_zigzag_40deg": dict(solver="MPI_TE_UPML", fi=(400, 420, 5, 8, 90, 20, 120),
+                                model=("zigzag", 200, 50, 3, 40), steps=120, kind="full"),
     "ser_tm_circle": dict(solver="TM_UPML", fi=(300, 300, 5, 8, 100, 0, 700),
                           model=("circle", 60, 0.0), steps=700, kind="full", rows="few",
                           extras=("spectrum", "frequency")),
@@ -60,6 +68,8 @@ def make_model(spec):
         return Model.circle(spec[1], spec[2])
     if kind == "discs":
         return Model.discs(spec[1])
+    if kind == "zigzag":
+        return Model.zigzag(*spec[1:5])
     if kind == "morpho":
         w, t0, t1, layers, branch, edge, eps = spec[1:8]
         return Model.morpho(w, t0, t1, layers, branch, edge, eps)

@@ -96,6 +96,7 @@ def test_host_field_api_matches_oracle_geometry(libs, oracle_built):
 @pytest.mark.parametrize("model,params,oracle_model", [
     (1, [60.0, 0.0], ("circle", 60, 0.0)),
     (3, [150.0, 20.0, 25.0, 3.0, 10.0, 0.5, 0.0, 0.0], ("morpho", 150, 20, 25, 3, 10, 0.5, 0.0)),
+    (5, [200.0, 50.0, 3.0, 40.0, 0.0], ("zigzag", 200, 50, 3, 40)),
 ])
 def test_host_models_eps_equals_oracle(libs, oracle_built, model, params, oracle_model):
     """models_eps of the library's host API gives the oracle's (= reference's) permittivity bit-for-bit."""

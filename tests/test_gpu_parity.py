@@ -70,7 +70,7 @@ def test_gpu_spectrum_rejects_more_than_8192_steps():
 
 
 MODEL_CASES = ["mpi_tm_circle", "mpi_te_circle", "mpi_tm_morpho", "mpi_te_morpho_eps225", "ser_tm_circle",
-               "ser_te_circle"]
+               "ser_te_circle", "mpi_tm_zigzag", "mpi_te_zigzag_40deg"]
 
 
 def _product_model(spec):
@@ -80,13 +80,15 @@ def _product_model(spec):
     if spec[0] == "morpho":
         w, t0, t1, layers, branch, edge, eps = spec[1:8]
         return m.MODEL_MORPHO, [w, t0, t1, layers, branch, edge, eps, 0.0]
+    if spec[0] == "zigzag":
+        return m.MODEL_ZIGZAG, [float(v) for v in spec[1:5]] + [0.0]
     raise ValueError(spec)
 
 
 @pytest.mark.parametrize("name", MODEL_CASES)
 def test_gpu_model_fill_equals_reference_eps(name):
-    """Device evaluators of circleModel.c / morphoScaleModel.c give the
-    reference's permittivity bit-for-bit at every staggered point."""
+    """Device evaluators of circleModel.c / morphoScaleModel.c / zigzagModel.c
+    give the reference's permittivity bit-for-bit at every staggered point."""
     m = _engine()
     c = CASES[name]
     ref = np.load(GOLDEN / f"{name}.npz")
