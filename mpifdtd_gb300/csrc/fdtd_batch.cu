@@ -37,9 +37,9 @@ namespace fdtd {
 namespace {
 
 struct BatchClock {
-  double t;  // engine time of the block's first step
-  int q;     // blocks run so far (field-set parity)
-  int pad;
+  double t;     // engine time of the block's first step
+  int q;        // blocks run so far (field-set parity)
+  int next[2];  // next unclaimed tile of the interior [0] / general [1] list (reset by the clock kernel)
 };
 
 // Per instance and per field-set parity p (blocks q with q % 2 == p): the
@@ -71,6 +71,7 @@ __global__ void batch_clock_kernel(BatchClock *clk, int K)
 {
   clk->t += K;
   clk->q += 1;
+  clk->next[0] = clk->next[1] = 0;  // both tile kernels of the block have finished (after the join)
 }
 
 // resident blocks per SM of the interior tile kernel (see interior_min_blocks in fdtd_tblock.cu)
@@ -80,15 +81,22 @@ template <typename R, int K, bool TM, int CPL> constexpr int batch_min_blocks()
                   : sizeof(R) == 8 ? (K > 2 ? 3 : 4) : (K >= 8 ? 3 : K == 4 ? (TM ? 4 : 5) : 6);
 }
 
+// Persistent: each warp claims the next tile of the list (sorted by cost,
+// largest first) until the list is exhausted, so the tail is one tile long
+// whatever the mix of tile heights and finished instances.
 template <typename R, int K, bool AUX, bool TM, int CPL>
 __global__ void __launch_bounds__(32 * kBWarps, (AUX ? 3 : batch_min_blocks<R, K, TM, CPL>()))
     batch_tile_kernel(const BatchInst<R> *__restrict__ inst, const int4 *__restrict__ tiles, int ntiles,
-                      const BatchClock *__restrict__ clk)
+                      BatchClock *clk)
 {
   const double t = clk->t;
   const int p = clk->q & 1;
-  const int nw = (int)gridDim.x * kBWarps;
-  for (int w = (int)blockIdx.x * kBWarps + (int)(threadIdx.x >> 5); w < ntiles; w += nw) {
+  int *next = &clk->next[AUX ? 1 : 0];
+  for (;;) {
+    int w = 0;
+    if ((threadIdx.x & 31) == 0) w = atomicAdd(next, 1);
+    w = __shfl_sync(0xffffffffu, w, 0);
+    if (w >= ntiles) break;  // whole warp
     const int4 tl = tiles[w];
     const BatchInst<R> &I = inst[tl.x];
     const int left = I.n_steps - (int)t;
@@ -297,6 +305,11 @@ static int batch_plan(fdtd_batch *b)
     b->rows[i] = L;
     omega[i] = s->geo.omega_s;
   }
+  // largest tiles first (rows walked = height + 2K), so the warps that take the
+  // last tiles of a launch finish together
+  auto taller = [](const int4 &a, const int4 &c) { return a.w - a.z > c.w - c.z; };
+  std::stable_sort(tint.begin(), tint.end(), taller);
+  std::stable_sort(tgen.begin(), tgen.end(), taller);
   for (fdtd_sim *s : b->sims) BCK(cudaStreamSynchronize(s->stream));
   cudaFree(b->d_inst);
   cudaFree(b->d_tint);
@@ -329,7 +342,7 @@ static void batch_block(fdtd_batch *b)
   cudaStream_t st = b->stream;
   const int n = (int)b->sims.size();
   auto *inst = (BatchInst<R> *)b->d_inst;
-  const auto *clk = (BatchClock *)b->d_clock;
+  auto *clk = (BatchClock *)b->d_clock;
   batch_source_kernel<R><<<(n * K + 127) / 128, 128, 0, st>>>(inst, (const double *)b->d_omega, n, K, clk);
   // the two tile kernels run side by side (fork onto the second stream, join)
   cudaEventRecord(b->ev_fork, st);
@@ -409,7 +422,7 @@ extern "C" int fdtd_batch_run(fdtd_batch *b)
   }
   for (fdtd_sim *s : b->sims) BCK(cudaStreamSynchronize(s->stream));
   if (int rc = b->f32 ? batch_descriptors<float>(b) : batch_descriptors<double>(b)) return rc;
-  BatchClock c0{0.0, 0, 0};
+  BatchClock c0{0.0, 0, {0, 0}};
   BCK(cudaMemcpyAsync(b->d_clock, &c0, sizeof c0, cudaMemcpyHostToDevice, b->stream));
   if (!b->graph) {
     cudaGraph_t g = nullptr;
