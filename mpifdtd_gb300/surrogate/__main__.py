@@ -1,6 +1,6 @@
 """Train and evaluate the far-field surrogate on data from the batched engine.
 
-    python -m mpifdtd_gb300.surrogate --train 4096 --val 256 --steps 3000
+    python -m mpifdtd_gb300.surrogate --train 4096 --val 256 --steps 20000
 
 Prints one JSON object: FDTD data-generation rate, training time, held-out
 errors (network and network-free baseline), network throughput and the
@@ -18,9 +18,10 @@ def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m mpifdtd_gb300.surrogate")
     ap.add_argument("--train", type=int, default=1024)
     ap.add_argument("--val", type=int, default=256)
-    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--steps", type=int, default=20000)
     ap.add_argument("--batch", type=int, default=128)
-    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--no-shift", action="store_true", help="no random translations of the training maps")
     ap.add_argument("--seed", type=int, default=20261207)
     ap.add_argument("--tol", type=float, default=0.02)
     a = ap.parse_args(argv)
@@ -30,14 +31,16 @@ def main(argv=None):
     gen = Generator(group=64)
     maps, inten, sec = S.generate(a.train + a.val, a.seed, gen)
     net = FNO(seed=1)
-    t_train = S.train(net, maps[:a.train], inten[:a.train], steps=a.steps, batch=a.batch, lr=a.lr)
+    t_train = S.train(net, maps[:a.train], inten[:a.train], steps=a.steps, batch=a.batch, lr=a.lr,
+                      shift=not a.no_shift)
     ev = S.evaluate(net, maps[a.train:], inten[a.train:], inten[:a.train])
     rate = S.inference_rate(net)
     k = max(1, int(np.ceil(0.01 * a.val)))
     audit = Generator(group=k)
     _, st = S.screen(net, maps[a.train:], gen, audit_frac=0.01, tol=a.tol, batch=a.val, audit_gen=audit)
     out = {"maps": a.train + a.val, "fdtd_structures_per_s": (a.train + a.val) / sec,
-           "train": {"maps": a.train, "with_mirror_images": 2 * a.train, "steps": a.steps, "seconds": t_train},
+           "train": {"maps": a.train, "with_mirror_images": 2 * a.train, "steps": a.steps, "lr": a.lr,
+                     "random_translations": not a.no_shift, "seconds": t_train},
            "heldout_rel_l2": ev, "network_structures_per_s": rate,
            "screen": {k2: v for k2, v in st.items()}}
     json.dump(out, sys.stdout)

@@ -39,10 +39,47 @@ def mirror(maps, inten):
     return maps[:, :, ::-1].copy(), np.asarray(inten)[:, :, ang].copy()
 
 
+def shift_ranges(maps, margin=6):
+    """Per map the integer shifts (dx_lo, dx_hi, dy_lo, dy_hi) that keep its
+    structure at least `margin` cells inside the map (the NTFF path runs 5
+    cells inside the map's edge); a structure already closer stays put on
+    that side."""
+    g = maps.shape[1]
+    out = np.zeros((len(maps), 4), np.int64)
+    for q, m in enumerate(maps):
+        xs = np.nonzero(m.any(axis=1))[0]
+        ys = np.nonzero(m.any(axis=0))[0]
+        if len(xs) == 0:
+            continue
+        for a, (lo, hi) in enumerate(((xs[0], xs[-1]), (ys[0], ys[-1]))):
+            out[q, 2 * a] = min(0, margin - lo)
+            out[q, 2 * a + 1] = max(0, (g - 1 - margin) - hi)
+    return out
+
+
+def shifted(dev_maps, idx, ranges, rng):
+    """dev_maps[idx] each translated by a random in-range (dx, dy): the
+    far-field intensity of a translated structure is the same (the plane wave
+    and the far field only change phase), measured on FDTD data to 0.5 %
+    median (shifts up to 100 cells)."""
+    import torch
+    r = ranges[idx]
+    dx = rng.integers(r[:, 0], r[:, 1] + 1)
+    dy = rng.integers(r[:, 2], r[:, 3] + 1)
+    g = dev_maps.shape[1]
+    ar = np.arange(g)
+    xi = torch.tensor((ar[None, :] - dx[:, None]) % g, device="cuda")
+    yi = torch.tensor((ar[None, :] - dy[:, None]) % g, device="cuda")
+    b = torch.tensor(idx, device="cuda")
+    return dev_maps[b[:, None, None], xi[:, :, None], yi[:, None, :]].contiguous()
+
+
 def train(net: FNO, maps, inten, steps=400, batch=128, lr=1e-3, seed=0, log=None, target="lin", augment=True,
-          wd=0.0):
+          wd=0.0, shift=True):
     """Adam (cosine-decayed learning rate) on minibatches of normalised far
-    fields, the training set doubled by its mirror images; returns seconds."""
+    fields, the training set doubled by its mirror images; with `shift` every
+    minibatch structure is also translated at random within the map (same
+    far-field intensity).  Returns seconds."""
     import torch
     if augment:
         mm, mi = mirror(maps, inten)
@@ -53,16 +90,19 @@ def train(net: FNO, maps, inten, steps=400, batch=128, lr=1e-3, seed=0, log=None
     target = torch.tensor(inten, device="cuda")
     net.set_normalisation(target, target=target_mode)
     y_all = net.encode(target)
-    x_all = net.pool(dev_maps)
+    x_all = None if shift else net.pool(dev_maps)
+    ranges = shift_ranges(maps) if shift else None
     n = len(maps)
     rng = np.random.default_rng(seed)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for it in range(steps):
-        idx = torch.tensor(rng.choice(n, batch, replace=n < batch), device="cuda")
+        pick = rng.choice(n, batch, replace=n < batch)
+        idx = torch.tensor(pick, device="cuda")
         frac = it / max(1, steps - 1)
         step_lr = lr * 0.5 * (1 + math.cos(math.pi * frac))  # cosine decay
-        loss, g = net.loss_and_grads(x_all[idx].contiguous(), y_all[idx].contiguous())
+        x = net.pool(shifted(dev_maps, pick, ranges, rng)) if shift else x_all[idx].contiguous()
+        loss, g = net.loss_and_grads(x, y_all[idx].contiguous())
         net.adam_step(g, lr=step_lr, wd=wd)
         if log is not None and (it % 100 == 0 or it == steps - 1):
             log(it, float(loss.mean()))

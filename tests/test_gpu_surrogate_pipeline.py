@@ -35,6 +35,20 @@ def test_mirror_augmentation_matches_the_physics(trained):
     assert np.median(S.rel_err(fm, mi)) < 0.02
 
 
+def test_translation_augmentation_matches_the_physics(trained):
+    """A structure translated within its map keeps its far-field intensity
+    (the plane wave and the far field only change phase); the training
+    translations stay inside the ranges shift_ranges allows."""
+    import torch
+    S, gen, net, maps, inten = trained
+    sub = maps[:8]
+    ranges = S.shift_ranges(sub)
+    moved = S.shifted(torch.tensor(sub, device="cuda"), np.arange(8), ranges, np.random.default_rng(3)).cpu().numpy()
+    assert np.array_equal(moved.sum(axis=(1, 2)), sub.sum(axis=(1, 2)))   # nothing wrapped or lost
+    fm = gen.far_field(moved)
+    assert np.median(S.rel_err(fm, inten[:8])) < 0.02
+
+
 def test_screening_fallback_and_audit(trained):
     S, gen, net, maps, inten = trained
     part = maps[192:256]
