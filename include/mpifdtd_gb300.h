@@ -30,10 +30,17 @@ extern "C" {
 #define FDTD_E_UNSUPPORTED 5   /* valid request the engine does not implement   */
 
 /* Solver ids: the values of enum SOLVER in simulator.h:8-18. */
+#define FDTD_TM_2D 0           /* serial TM split-field PML (fdtdTM.c), FP64 only   */
+#define FDTD_TE_2D 1           /* serial TE split-field PML (fdtdTE.c), FP64 only   */
 #define FDTD_TM_UPML 2         /* serial TM UPML  (fdtdTM_upml.c)  */
 #define FDTD_TE_UPML 3         /* serial TE UPML  (fdtdTE_upml.c)  */
 #define FDTD_MPI_TM_UPML 4     /* MPI TM UPML     (mpiTM_UPML.c), one-rank semantics */
 #define FDTD_MPI_TE_UPML 5     /* MPI TE UPML     (mpiTE_UPML.c), one-rank semantics */
+#define FDTD_NS_TM_2D 6        /* serial TM non-standard FDTD (nsFdtdTM.c), FP64 only */
+#define FDTD_NS_TE_2D 7        /* serial TE non-standard FDTD (nsFdtdTE.c), FP64 only */
+/* The split-field and NS solvers have no NTFF (the reference's have none):
+ * they run, give fields, permittivity and the elliptic ring; the NTFF,
+ * spectrum, frequency and blocking calls return FDTD_E_STATE / UNSUPPORTED. */
 
 /* Field precision of the stencil.  The NTFF accumulation is FP64 in both. */
 #define FDTD_F64 0
@@ -48,7 +55,8 @@ extern "C" {
 #define FDTD_MODEL_ZIGZAG 5    /* zigzagModel.c: {width_nm, thickness_nm, layers,
                                   degree, n (<=0: 1.56)}                          */
 
-/* Which array: fields (TM: 0 Ez, 1 Hx, 2 Hy; TE: 0 Ex, 1 Ey, 2 Hz),
+/* Which array: fields (TM: 0 Ez, 1 Hx, 2 Hy; TE: 0 Ex, 1 Ey, 2 Hz; the
+ * split-field and NS solvers add 3, 4: TM Ezx, Ezy; TE Hzx, Hzy),
  * NTFF accumulators (TM: 0 Ux, 1 Uy, 2 Wz; TE: 0 Wx, 1 Wy, 2 Uz). */
 
 /* Layout of copied-out fields / permittivity:

@@ -2,9 +2,10 @@
  * mpifdtd_upml.h -- the reference's UPML solver entry points, served by the
  * GB300 engine (libmpifdtd_upml.so on top of libmpifdtd_gb300.so).
  *
- * Drop-in for the four solver translation units of rennone/mpiFDTD that
- * simulator.c binds (simulator.c:134-205): link libmpifdtd_upml.so instead of
- * mpiTM_UPML.c, mpiTE_UPML.c, fdtdTM_upml.c and fdtdTE_upml.c; simulator.c,
+ * Drop-in for the eight solver translation units of rennone/mpiFDTD that
+ * simulator.c binds (simulator.c:32-205): link libmpifdtd_upml.so instead of
+ * mpiTM_UPML.c, mpiTE_UPML.c, fdtdTM_upml.c, fdtdTE_upml.c, fdtdTM.c,
+ * fdtdTE.c, nsFdtdTM.c and nsFdtdTE.c; simulator.c,
  * field.c, models.c and the models stay as they are.  The library calls back
  * into the host program's field_getFieldInfo(), field_getTime(),
  * field_getRayCoef(), field_getWaveAngle() and models_eps() exactly where the
@@ -16,8 +17,9 @@
  *   init()   allocates the device state, fills the permittivity through
  *            models_eps() at the solver's staggered points and modes
  *   update() one time step on the GPU at field_getTime()/field_getRayCoef()
- *   reset()  zeroes the fields (serial solvers first write the far-field
- *            spectrum files, as ntffTM_TimeOutput does)
+ *   reset()  zeroes the fields (serial UPML solvers first write the far-field
+ *            spectrum files, as ntffTM_TimeOutput does; split-field / NS ones
+ *            the field_outputElliptic ring file)
  *   finish() releases everything (serial solvers write the spectrum first)
  *   get*()   borrowed host pointers in the reference solver's own layout,
  *            refreshed from the device on each call after an update()
@@ -77,6 +79,63 @@ extern double complex *fdtdTE_upml_getEy(void);
 extern double complex *fdtdTE_upml_getHz(void);
 extern double *fdtdTE_upml_getEps(void);
 
+/* fdtdTM.h (split-field PML TM) */
+extern void (*fdtdTM_getUpdate(void))(void);
+extern void (*fdtdTM_getFinish(void))(void);
+extern void (*fdtdTM_getReset(void))(void);
+extern void (*fdtdTM_getInit(void))(void);
+extern double complex *fdtdTM_getEzx(void);
+extern double complex *fdtdTM_getEzy(void);
+extern double complex *fdtdTM_getEz(void);
+extern double complex *fdtdTM_getHy(void);
+extern double complex *fdtdTM_getHx(void);
+extern double *fdtdTM_getEps(void);
+
+/* fdtdTE.h (split-field PML TE) */
+extern void (*fdtdTE_getUpdate(void))(void);
+extern void (*fdtdTE_getFinish(void))(void);
+extern void (*fdtdTE_getReset(void))(void);
+extern void (*fdtdTE_getInit(void))(void);
+extern double complex *fdtdTE_getEx(void);
+extern double complex *fdtdTE_getEy(void);
+extern double complex *fdtdTE_getHzx(void);
+extern double complex *fdtdTE_getHzy(void);
+extern double complex *fdtdTE_getHz(void);
+extern double *fdtdTE_getEps(void);
+
+/* nsFdtdTM.h (non-standard FDTD TM); getEpsX/Y/Z are public in nsFdtdTM.c:33-35.
+ * nsFdtdTM_getSolver (a Solver record whose fields the reference leaves unset)
+ * is not provided. */
+extern void (*nsFdtdTM_getUpdate(void))(void);
+extern void (*nsFdtdTM_getFinish(void))(void);
+extern void (*nsFdtdTM_getReset(void))(void);
+extern void (*nsFdtdTM_getInit(void))(void);
+extern double complex *nsFdtdTM_getEzx(void);
+extern double complex *nsFdtdTM_getEzy(void);
+extern double complex *nsFdtdTM_getEz(void);
+extern double complex *nsFdtdTM_getHy(void);
+extern double complex *nsFdtdTM_getHx(void);
+extern double *nsFdtdTM_getEps(void);
+extern double *nsFdtdTM_getEpsX(void);
+extern double *nsFdtdTM_getEpsY(void);
+extern double *nsFdtdTM_getEpsZ(void);
+
+/* nsFdtdTE.h (non-standard FDTD TE); getEpsX/Y/Z are public in nsFdtdTE.c:33-35.
+ * nsFdtdTE_getSolver is not provided (as for TM). */
+extern void (*nsFdtdTE_getUpdate(void))(void);
+extern void (*nsFdtdTE_getFinish(void))(void);
+extern void (*nsFdtdTE_getReset(void))(void);
+extern void (*nsFdtdTE_getInit(void))(void);
+extern double complex *nsFdtdTE_getHzx(void);
+extern double complex *nsFdtdTE_getHzy(void);
+extern double complex *nsFdtdTE_getHz(void);
+extern double complex *nsFdtdTE_getEy(void);
+extern double complex *nsFdtdTE_getEx(void);
+extern double *nsFdtdTE_getEps(void);
+extern double *nsFdtdTE_getEpsX(void);
+extern double *nsFdtdTE_getEpsY(void);
+extern double *nsFdtdTE_getEpsZ(void);
+
 /* Extensions (no counterpart in the reference).
  * The reference reports errors with printf + exit(2) (function.c:27-32,
  * simulator.c:234-237); the drop-in does the same by default.  Mode 1 makes
@@ -84,7 +143,7 @@ extern double *fdtdTE_upml_getEps(void);
  * mpifdtd_upml_last_status() (FDTD_OK or an FDTD_E_* code). */
 extern void mpifdtd_upml_set_error_mode(int return_instead_of_exit);
 extern int mpifdtd_upml_last_status(void);
-/* The engine simulation behind a solver (4 MPI TM, 5 MPI TE, 2 TM, 3 TE), or
+/* The engine simulation behind a solver (enum SOLVER value 0..7), or
  * NULL before init(): lets a host use the extended C ABI of mpifdtd_gb300.h. */
 struct fdtd_sim;
 extern struct fdtd_sim *mpifdtd_upml_engine(int solver);

@@ -48,7 +48,17 @@ int fail(int code, const char *fmt, ...)
     if (e_ != cudaSuccess) return fail(FDTD_E_CUDA, "%s: %s", #call, cudaGetErrorString(e_));      \
   } while (0)
 
-bool is_tm(int solver) { return solver == FDTD_TM_UPML || solver == FDTD_MPI_TM_UPML; }
+bool is_tm(int solver)
+{
+  return solver == FDTD_TM_UPML || solver == FDTD_MPI_TM_UPML || solver == FDTD_TM_2D || solver == FDTD_NS_TM_2D;
+}
+// 0 UPML, 1 split-field PML, 2 NS-FDTD
+int family_of(int solver)
+{
+  if (solver == FDTD_TM_2D || solver == FDTD_TE_2D) return 1;
+  if (solver == FDTD_NS_TM_2D || solver == FDTD_NS_TE_2D) return 2;
+  return 0;
+}
 bool is_mpi(int solver) { return solver == FDTD_MPI_TM_UPML || solver == FDTD_MPI_TE_UPML; }
 
 // field.c:259-283 (M = 2)
@@ -307,6 +317,7 @@ static void free_sim(fdtd_sim *s)
   cudaFree(s->d_tiles);
   for (int a = 0; a < 2; a++) { cudaFree(s->d_ieps64[a]); cudaFree(s->d_ieps32[a]); }
   for (int a = 0; a < 3; a++) cudaFree(s->d_eps[a]);
+  cudaFree(s->d_coef);
   for (int a = 0; a < 4; a++) { cudaFree(s->d_tab64[a]); cudaFree(s->d_tab32[a]); }
   cudaFree(s->d_ex);
   cudaFree(s->d_ey);
@@ -337,11 +348,11 @@ extern "C" int fdtd_create(int solver, const fdtd_config *cfg, fdtd_sim **out)
 {
   if (!cfg || !out) return fail(FDTD_E_ARG, "null argument");
   *out = nullptr;
-  if (solver != FDTD_TM_UPML && solver != FDTD_TE_UPML && solver != FDTD_MPI_TM_UPML &&
-      solver != FDTD_MPI_TE_UPML)
-    return fail(FDTD_E_ARG, "solver %d is not a UPML solver (2..5)", solver);
+  if (solver < FDTD_TM_2D || solver > FDTD_NS_TE_2D) return fail(FDTD_E_ARG, "solver %d is not one of 0..7", solver);
   if (cfg->precision != FDTD_F64 && cfg->precision != FDTD_F32)
     return fail(FDTD_E_ARG, "precision must be FDTD_F64 or FDTD_F32");
+  if (family_of(solver) && cfg->precision != FDTD_F64)
+    return fail(FDTD_E_UNSUPPORTED, "the split-field and NS solvers run in FP64 only");
   for (int q = 0; q < 7; q++)
     if (cfg->reserved[q]) return fail(FDTD_E_ARG, "reserved fields must be zero");
   if (cfg->flags & ~FDTD_CFG_NO_TIME_NTFF) return fail(FDTD_E_ARG, "unknown config flags %#x", cfg->flags);
@@ -358,7 +369,9 @@ extern "C" int fdtd_create(int solver, const fdtd_config *cfg, fdtd_sim **out)
   s->solver = solver;
   s->tm = is_tm(solver);
   s->mpi = is_mpi(solver);
+  s->family = family_of(solver);
   s->cfg = *cfg;
+  if (s->family) s->cfg.flags |= FDTD_CFG_NO_TIME_NTFF;  // these solvers have no NTFF
   s->geo = geo;
   s->f32 = cfg->precision == FDTD_F32;
   // array frame: MPI -> (N_PX+2) x (N_PY+2) halo ring, x = i-1; serial -> N_PX x N_PY, x = i
@@ -369,7 +382,7 @@ extern "C" int fdtd_create(int solver, const fdtd_config *cfg, fdtd_sim **out)
   s->ncols = s->nj + 2;
   s->pitch = (s->ncols + 7) / 8 * 8;
   s->esize = s->f32 ? sizeof(float2) : sizeof(double2);
-  s->nslots = s->tm ? 7 : 8;
+  s->nslots = s->family ? 5 : s->tm ? 7 : 8;
   if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
     cudaGetLastError();
     delete s;
@@ -399,6 +412,14 @@ extern "C" int fdtd_create(int solver, const fdtd_config *cfg, fdtd_sim **out)
       cudaGetLastError();
       free_sim(s);
       return fail(FDTD_E_NOMEM, "cudaMalloc of permittivity failed");
+    }
+  }
+  if (s->family) {
+    s->ncoef = solver == FDTD_NS_TE_2D ? 10 : 9;
+    if (cudaMalloc(&s->d_coef, (size_t)s->ncoef * ecount * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      free_sim(s);
+      return fail(FDTD_E_NOMEM, "cudaMalloc of the per-cell coefficients failed");
     }
   }
   if ((rc = build_tables(s)) || (rc = build_ntff(s)) || (rc = fdtd_fill_eps_model(s, FDTD_MODEL_NONE, nullptr, 0))) {
@@ -435,6 +456,10 @@ extern "C" int fdtd_get_geometry(const fdtd_sim *s, fdtd_geometry *out)
 // kStatusBadEps and makes the call fail.
 static int derive_inv_eps(fdtd_sim *s)
 {
+  if (s->family) {  // split-field / NS: per-cell coefficients from the permittivity before the next step
+    s->coef_dirty = true;
+    return FDTD_OK;
+  }
   const size_t count = (size_t)s->nxa * s->pitch;
   const int neps = s->tm ? 1 : 2;
   CK(cudaMemsetAsync(s->d_status, 0, sizeof(unsigned int), s->stream));
@@ -479,10 +504,22 @@ extern "C" int fdtd_fill_eps_model(fdtd_sim *s, int model, const double *params,
     return fail(FDTD_E_UNSUPPORTED, "model %d is not built in (none 0, circle 1, morpho 3, zigzag 5)", model);
   if (mdl_init(&m, model, params, n_params, s->geo.n_px, s->geo.n_py, s->geo.n_pml, s->cfg.h_u_nm) != 0)
     return fail(FDTD_E_ARG, "bad parameters for model %d (see mpifdtd_gb300.h)", model);
+  const bool alt = s->tm ? (s->mpi || s->family != 0) : s->solver == FDTD_NS_TE_2D;
   launch_eps_model((double *)s->d_eps[0], (double *)s->d_eps[1], (double *)s->d_eps[2], s->pitch, s->nxa,
-                   s->ncols, s->ox, s->geo.n_px, s->geo.n_py, s->tm, s->mpi, m, s->stream);
+                   s->ncols, s->ox, s->geo.n_px, s->geo.n_py, s->tm, alt, m, s->stream);
   s->launches += 1;
   CK(cudaGetLastError());
+  if (s->solver == FDTD_NS_TE_2D) {  // nsFdtdTE.c:114-121 sets EPS_* on the inner cells only (FOR_FOR)
+    const size_t rowb = (size_t)s->pitch * sizeof(double);
+    for (int a = 0; a < 3; a++) {
+      char *e = (char *)s->d_eps[a];
+      CK(cudaMemsetAsync(e, 0, rowb, s->stream));
+      CK(cudaMemsetAsync(e + (size_t)(s->geo.n_px - 1) * rowb, 0, rowb, s->stream));
+      CK(cudaMemset2DAsync(e, rowb, 0, sizeof(double), s->geo.n_px, s->stream));
+      CK(cudaMemset2DAsync(e + (size_t)(s->geo.n_py - 1) * sizeof(double), rowb, 0, sizeof(double), s->geo.n_px,
+                           s->stream));
+    }
+  }
   return derive_inv_eps(s);
 }
 
@@ -712,9 +749,15 @@ static void mark(fdtd_sim *s)
   cudaEventRecord(s->ev_pool[s->ev_used++], s->stream);
 }
 
+static void enqueue_split(fdtd_sim *s, double time, double ray_coef);
+
 template <typename R>
 static void enqueue_step(fdtd_sim *s, double time, double ray_coef)
 {
+  if (s->family) {
+    enqueue_split(s, time, ray_coef);
+    return;
+  }
   const StencilView<R> v = view_of<R>(s);
   const NtffView n = ntff_view(s);
   cudaStream_t st = s->stream;
@@ -1111,8 +1154,190 @@ extern "C" int fdtd_profile_read(fdtd_sim *s, double *ms_out, long long *steps)
   return FDTD_OK;
 }
 
+// ------------------------------------------------- split-field / NS solvers
+
+// Per-cell coefficients of the split-field PML solvers (fdtdTM.c:187-241,
+// fdtdTE.c:198-238) and the NS-FDTD solvers (nsFdtdTM.c:213-291,
+// nsFdtdTE.c:106-182), from the permittivity as it is now, in the reference's
+// expression order (this file is compiled without contraction).  Layout:
+// fdtd_split.cu.
+static int split_coefficients(fdtd_sim *s)
+{
+  const fdtd_geometry &g = s->geo;
+  const int NX = g.n_px, NY = g.n_py, P = s->pitch, npml = g.n_pml;
+  const size_t plane = (size_t)s->nxa * P;
+  std::vector<double> eps[3];
+  for (int a = 0; a < 3; a++) {
+    eps[a].resize((size_t)NX * NY);
+    if (int rc = fdtd_get_eps(s, a, FDTD_LAYOUT_GLOBAL, eps[a].data())) return rc;
+  }
+  for (int a = 0; a < 3; a++)
+    for (int x = 1; x < NX - 1; x++)
+      for (int y = 1; y < NY - 1; y++) {
+        const double e = eps[a][(size_t)x * NY + y];
+        if (!(e > 0.0) || !std::isfinite(e)) return fail(FDTD_E_ARG, "permittivity must be finite and > 0 inside");
+      }
+  std::vector<double> c((size_t)s->ncoef * plane, 0.0);
+  auto C = [&](int q, int x, int y) -> double & { return c[q * plane + (size_t)x * P + y]; };
+  auto sx = [&](double x) { return sigma_axis(x, npml, g.n_x, NX); };  // field_sigmaX (field.c:259-270)
+  auto sy = [&](double y) { return sigma_axis(y, npml, g.n_y, NY); };  // field_sigmaY (field.c:272-283)
+  const double EPS0 = 1.0, C0 = kC, MU0 = 1.0 / kC / kC, LIGHT = kC;   // field.h:70-74
+  const double R = 1.0e-8, M = 2.0;
+  // field.c:132-133 pmlCoef / pmlCoef_LXY
+  auto pml = [](double ep, double sig) { return (1.0 - sig / ep) / (1.0 + sig / ep); };
+  auto lxy = [](double ep, double sig) { return 1.0 / (ep + sig); };
+  // nsFdtdTM.c:199-208 beta / coef1
+  auto beta = [](double a) { return tanh(a) / (1 + pow(tanh(a), 2)); };
+  auto coef1 = [](double a, double b) { return (1 - b) / (1 + b); };
+  const double w_s = g.omega_s, k_s = g.k_s;
+  // source amplitude of field_nsScatteredWaveNotUPML (field.c:168-174) at permittivity e
+  auto ns_amp = [&](double e) {
+    const double n = sqrt(e / EPS0);
+    const double u0 = sin(w_s * 0.5) / sin(k_s * 0.5);
+    const double u1 = sin(w_s * 0.5) / sin(n * k_s * 0.5);
+    const double _n = u0 / u1;
+    return 1.0 / (_n * n) - 1.0;
+  };
+  // u z / (1 + b) style factors of the NS coefficients: u = sin(w/2) / sin(k n / 2)
+  auto ns_u = [&](double e) {
+    const double n = sqrt(e / EPS0);
+    const double kk = k_s * n;
+    return sin(w_s * 0.5) / sin(kk * 0.5);
+  };
+  switch (s->solver) {
+  case FDTD_TM_2D: {
+    const double sig_max = -(M + 1.0) * EPS0 * LIGHT / 2.0 / npml * log(R);
+    for (int x = 0; x < NX; x++)
+      for (int y = 0; y < NY; y++) {
+        const double eez = eps[0][(size_t)x * NY + y];
+        const double sig_ez_x = sig_max * sx(x), sig_ez_y = sig_max * sy(y);
+        const double sig_hx_yy = MU0 / EPS0 * (sig_max * sy(y + 0.5));
+        const double sig_hy_xx = MU0 / EPS0 * (sig_max * sx(x + 0.5));
+        C(0, x, y) = pml(eez, sig_ez_x);
+        C(1, x, y) = lxy(eez, sig_ez_x);
+        C(2, x, y) = pml(eez, sig_ez_y);
+        C(3, x, y) = lxy(eez, sig_ez_y);
+        C(4, x, y) = pml(MU0, sig_hx_yy);
+        C(5, x, y) = lxy(MU0, sig_hx_yy);
+        C(6, x, y) = pml(MU0, sig_hy_xx);
+        C(7, x, y) = lxy(MU0, sig_hy_xx);
+        C(8, x, y) = EPS0 / eez - 1.0;
+      }
+    break;
+  }
+  case FDTD_TE_2D: {
+    const double sig_max = -(M + 1.0) * EPS0 * LIGHT / 2.0 / npml * log(R);
+    for (int x = 0; x < NX; x++)
+      for (int y = 0; y < NY; y++) {
+        const double eex = eps[0][(size_t)x * NY + y], eey = eps[1][(size_t)x * NY + y];
+        const double sig_ex_y = sig_max * sy(y), sig_ey_x = sig_max * sx(x);
+        const double sig_hz_xx = MU0 / EPS0 * (sig_max * sx(x + 0.5));
+        const double sig_hz_yy = MU0 / EPS0 * (sig_max * sy(y + 0.5));
+        C(0, x, y) = pml(eex, sig_ex_y);
+        C(1, x, y) = lxy(eex, sig_ex_y);
+        C(2, x, y) = pml(eey, sig_ey_x);
+        C(3, x, y) = lxy(eey, sig_ey_x);
+        C(4, x, y) = pml(MU0, sig_hz_xx);
+        C(5, x, y) = lxy(MU0, sig_hz_xx);
+        C(6, x, y) = pml(MU0, sig_hz_yy);
+        C(7, x, y) = lxy(MU0, sig_hz_yy);
+        C(8, x, y) = EPS0 / eey - 1.0;
+      }
+    break;
+  }
+  case FDTD_NS_TM_2D: {
+    const double sig_max = -(M + 1.0) * EPS0 * C0 / npml * log(R);
+    for (int x = 0; x < NX; x++)
+      for (int y = 0; y < NY; y++) {
+        const size_t k = (size_t)x * NY + y;
+        const double eez = eps[0][k], ehx = eps[1][k], ehy = eps[2][k];
+        const double sig_ez_x = sig_max * sx(x), sig_ez_y = sig_max * sy(y);
+        const double sig_hx_y = sig_max * sy(y + 0.5), sig_hy_x = sig_max * sx(x + 0.5);
+        const double a_hx_y = sig_hx_y / (2 * EPS0), a_hy_x = sig_hy_x / (2 * EPS0);
+        const double a_ez_x = sig_ez_x / (2 * EPS0), a_ez_y = sig_ez_y / (2 * EPS0);
+        const double b_hx_y = beta(a_hx_y), b_hy_x = beta(a_hy_x), b_ez_x = beta(a_ez_x), b_ez_y = beta(a_ez_y);
+        const double z_ez = sqrt(MU0 / eez), u_ez = ns_u(eez);
+        C(0, x, y) = coef1(a_ez_x, b_ez_x);
+        C(1, x, y) = u_ez * z_ez / (1 + b_ez_x);
+        C(2, x, y) = coef1(a_ez_y, b_ez_y);
+        C(3, x, y) = u_ez * z_ez / (1.0 + b_ez_x);  // nsFdtdTM.c:268: b_ez_x, as written
+        const double z_hx = sqrt(MU0 / ehx), u_hx = ns_u(ehx);
+        C(4, x, y) = coef1(a_hx_y, b_hx_y);
+        C(5, x, y) = u_hx / z_hx / (1.0 + b_hx_y);
+        const double z_hy = sqrt(MU0 / ehy), u_hy = ns_u(ehy);
+        C(6, x, y) = coef1(a_hy_x, b_hy_x);
+        C(7, x, y) = u_hy / z_hy / (1.0 + b_hy_x);
+        C(8, x, y) = ns_amp(eez);
+      }
+    break;
+  }
+  default: {  // FDTD_NS_TE_2D, inner cells only (FOR_FOR)
+    const double sig_max = -(M + 1.0) * EPS0 * C0 / npml * log(R);
+    for (int x = 1; x < NX - 1; x++)
+      for (int y = 1; y < NY - 1; y++) {
+        const size_t k = (size_t)x * NY + y;
+        const double eex = eps[0][k], eey = eps[1][k], ehz = eps[2][k];
+        const double sig_ex_y = sig_max * sy(y), sig_ey_x = sig_max * sx(x);
+        const double sig_hz_x = sig_max * sx(x + 0.5), sig_hz_y = sig_max * sy(y + 0.5);
+        const double a_ex_y = sig_ex_y / (2 * eex), a_ey_x = sig_ey_x / (2 * eey);
+        const double a_hz_x = sig_hz_x / (2 * ehz), a_hz_y = sig_hz_y / (2 * ehz);
+        const double b_ex_y = beta(a_ex_y), b_ey_x = beta(a_ey_x), b_hz_x = beta(a_hz_x), b_hz_y = beta(a_hz_y);
+        const double z_hz = sqrt(MU0 / ehz), u_hz = ns_u(ehz);
+        C(4, x, y) = coef1(a_hz_x, b_hz_x);
+        C(5, x, y) = u_hz / z_hz / (1.0 + b_hz_x);
+        C(6, x, y) = coef1(a_hz_y, b_hz_y);
+        C(7, x, y) = u_hz / z_hz / (1.0 + b_hz_y);
+        const double z_ex = sqrt(MU0 / eex), u_ex = ns_u(eex);
+        C(0, x, y) = coef1(a_ex_y, b_ex_y);
+        C(1, x, y) = u_ex * z_ex / (1.0 + b_ex_y);
+        const double z_ey = sqrt(MU0 / eey), u_ey = ns_u(eey);
+        C(2, x, y) = coef1(a_ey_x, b_ey_x);
+        C(3, x, y) = u_ey * z_ey / (1.0 + b_ey_x);
+        C(8, x, y) = ns_amp(eex);
+        C(9, x, y) = ns_amp(eey);
+      }
+    break;
+  }
+  }
+  CK(cudaMemcpy(s->d_coef, c.data(), c.size() * sizeof(double), cudaMemcpyHostToDevice));
+  s->coef_dirty = false;
+  return FDTD_OK;
+}
+
+// One update() of a split-field / NS solver at (time, ray_coef).
+static void enqueue_split(fdtd_sim *s, double time, double ray_coef)
+{
+  SplitView v{};
+  for (int a = 0; a < 5; a++) v.f[a] = (double2 *)s->d_f[a];
+  const size_t plane = (size_t)s->nxa * s->pitch;
+  for (int q = 0; q < s->ncoef; q++) v.c[q] = (const double *)s->d_coef + q * plane;
+  v.P = s->pitch;
+  v.n_px = s->geo.n_px;
+  v.n_py = s->geo.n_py;
+  v.ray = ray_coef;
+  v.t = time;
+  v.w_s = s->geo.omega_s;
+  const double k_s = s->geo.k_s;
+  const double rad = s->cfg.angle_deg * M_PI / 180.0;  // field.c:162-163, 186-187
+  v.ks_cos = cos(rad) * k_s;
+  v.ks_sin = sin(rad) * k_s;
+  const double r = 1.0 / 6.0 + k_s * k_s / 180.0 - pow(k_s, 4) / 23040;  // nsFdtdTM.c:114-115
+  v.r_2 = r / 2.0;
+  v.co = cos((s->cfg.angle_deg + 90) * M_PI / 180.0);  // nsFdtdTE.c:228-229
+  v.si = sin((s->cfg.angle_deg + 90) * M_PI / 180.0);
+  mark(s);
+  launch_split_step(v, s->solver, s->stream);
+  mark(s);
+  mark(s);
+  mark(s);
+  mark(s);
+  s->launches += 2;
+  if (s->profiling) s->prof_steps++;
+}
+
 static int prepare_step(fdtd_sim *s)
 {
+  if (s->family && s->coef_dirty) return split_coefficients(s);
   if (s->ntff_mode == 1 && s->window_dirty) return build_windows(s);
   return FDTD_OK;
 }
@@ -1214,6 +1439,12 @@ extern "C" int fdtd_get_status(fdtd_sim *s, unsigned int *flags)
 static int field_slot(const fdtd_sim *s, int which)
 {
   static const int tm_slot[3] = {0, 3, 4}, te_slot[3] = {0, 1, 6};
+  // split-field / NS: 3, 4 are the split parts (TM Ezx, Ezy; TE Hzx, Hzy)
+  static const int split_tm_slot[5] = {0, 3, 4, 1, 2}, split_te_slot[5] = {0, 1, 2, 3, 4};
+  if (s->family) {
+    if (which < 0 || which > 4) return -1;
+    return s->tm ? split_tm_slot[which] : split_te_slot[which];
+  }
   if (which < 0 || which > 2) return -1;
   return s->tm ? tm_slot[which] : te_slot[which];
 }
@@ -1455,6 +1686,7 @@ extern "C" int fdtd_dft_spectrum(fdtd_sim *s, double *out)
 extern "C" int fdtd_frequency(fdtd_sim *s, double *out)
 {
   if (!s || !out) return fail(FDTD_E_ARG, "null argument");
+  if (s->family) return fail(FDTD_E_UNSUPPORTED, "the split-field and NS solvers have no NTFF");
   if (int rc = ensure_farfield(s)) return rc;
   FrequencyView f{};
   f.tm = s->tm ? 1 : 0;

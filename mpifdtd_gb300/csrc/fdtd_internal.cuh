@@ -193,6 +193,16 @@ void launch_dft_accumulate(const NtffView &n, const DftView &d, int nb, double t
 void launch_dft_farfield(const NtffView &n, const DftView &d, int tm, const double2 *dir, double2 coef, double2 *X,
                          cudaStream_t st);
 void launch_frequency(const FrequencyView &f, cudaStream_t st);
+// fdtd_split.cu: split-field PML and NS-FDTD solvers (one step = two launches)
+struct SplitView {
+  double2 *f[5];         // TM: 0 Ez 1 Ezx 2 Ezy 3 Hx 4 Hy ; TE: 0 Ex 1 Ey 2 Hz 3 Hzx 4 Hzy
+  const double *c[10];   // per-cell coefficients (fdtd_split.cu)
+  int P, n_px, n_py;
+  double ray, t, w_s, ks_cos, ks_sin;  // source: ray_coef, time, omega, k (cos, sin of the wave angle)
+  double r_2, co, si;                  // NS operator weight; NS TE source directions
+};
+void launch_split_step(const SplitView &v, int solver, cudaStream_t st);
+
 // out[q] = field[idx[q]] widened to FP64 (FP32 fields: f32 = 1), q < n
 void launch_point_gather(const void *field, int f32, const long long *idx, int n, double2 *out, cudaStream_t st);
 
@@ -200,8 +210,11 @@ void launch_point_gather(const void *field, int f32, const long long *idx, int n
 int set_error(int code, const char *fmt, ...);
 
 // fdtd_setup.cu
+// alt: TM -- the MPI / split-field / NS staggering (HX at D_Y, HY at D_X) instead
+// of the serial UPML one (D_XY everywhere); TE -- HZ sampled once at D_XY (NS TE)
+// instead of the mean of D_X and D_Y
 void launch_eps_model(double *e0, double *e1, double *e2, int P, int nxa, int ncols, int ox, int n_px, int n_py,
-                      bool tm, bool mpi, const mdl_params &m, cudaStream_t st);
+                      bool tm, bool alt, const mdl_params &m, cudaStream_t st);
 void launch_inv_eps(const double *eps, double *ie64, float *ie32, size_t count, unsigned int *status,
                     cudaStream_t st);
 void launch_fill(double *p, double v, size_t count, cudaStream_t st);

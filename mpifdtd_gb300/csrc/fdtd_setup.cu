@@ -7,6 +7,9 @@
 //   serial TM  EZ (x,y,D_XY)  HX (x,y+.5,D_XY) HY (x+.5,y,D_XY) fdtdTM_upml.c:237-239
 //   TE       EX (x+.5,y,D_Y)  EY (x,y+.5,D_X)
 //            HZ 0.5*(eps(x+.5,y+.5,D_X) + eps(x+.5,y+.5,D_Y))  mpiTE_UPML.c:503-505
+//   split-field and NS TM as MPI TM (fdtdTM.c:206-208, nsFdtdTM.c:233-235),
+//   split-field TE as TE (fdtdTE.c:207-209), NS TE with HZ (x+.5,y+.5,D_XY)
+//   (nsFdtdTE.c:118-120)
 #include <cuda_runtime.h>
 
 #include "fdtd_internal.cuh"
@@ -15,7 +18,7 @@
 namespace fdtd {
 
 __global__ void eps_model_kernel(double *e0, double *e1, double *e2, int P, int nxa, int ncols, int ox, int n_px,
-                                 int n_py, int tm, int mpi, mdl_params m)
+                                 int n_py, int tm, int alt, mdl_params m)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
@@ -28,12 +31,13 @@ __global__ void eps_model_kernel(double *e0, double *e1, double *e2, int P, int 
   if (x >= 0 && x < n_px && y >= 0 && y < n_py) {
     if (tm) {
       a = mdl_eps(&m, x, y, 1, 1);
-      b = mpi ? mdl_eps(&m, x, y + 0.5, 0, 1) : mdl_eps(&m, x, y + 0.5, 1, 1);
-      c = mpi ? mdl_eps(&m, x + 0.5, y, 1, 0) : mdl_eps(&m, x + 0.5, y, 1, 1);
+      b = alt ? mdl_eps(&m, x, y + 0.5, 0, 1) : mdl_eps(&m, x, y + 0.5, 1, 1);
+      c = alt ? mdl_eps(&m, x + 0.5, y, 1, 0) : mdl_eps(&m, x + 0.5, y, 1, 1);
     } else {
       a = mdl_eps(&m, x + 0.5, y, 0, 1);
       b = mdl_eps(&m, x, y + 0.5, 1, 0);
-      c = 0.5 * (mdl_eps(&m, x + 0.5, y + 0.5, 1, 0) + mdl_eps(&m, x + 0.5, y + 0.5, 0, 1));
+      c = alt ? mdl_eps(&m, x + 0.5, y + 0.5, 1, 1)
+              : 0.5 * (mdl_eps(&m, x + 0.5, y + 0.5, 1, 0) + mdl_eps(&m, x + 0.5, y + 0.5, 0, 1));
     }
   }
   e0[k] = a;
@@ -59,11 +63,11 @@ __global__ void fill_kernel(double *p, double v, size_t count)
 }
 
 void launch_eps_model(double *e0, double *e1, double *e2, int P, int nxa, int ncols, int ox, int n_px, int n_py,
-                      bool tm, bool mpi, const mdl_params &m, cudaStream_t st)
+                      bool tm, bool alt, const mdl_params &m, cudaStream_t st)
 {
   (void)ncols;
   dim3 b(32, 8), g((unsigned)((P + 31) / 32), (unsigned)((nxa + 7) / 8));
-  eps_model_kernel<<<g, b, 0, st>>>(e0, e1, e2, P, nxa, ncols, ox, n_px, n_py, tm ? 1 : 0, mpi ? 1 : 0, m);
+  eps_model_kernel<<<g, b, 0, st>>>(e0, e1, e2, P, nxa, ncols, ox, n_px, n_py, tm ? 1 : 0, alt ? 1 : 0, m);
 }
 
 void launch_inv_eps(const double *eps, double *ie64, float *ie32, size_t count, unsigned int *status,

@@ -10,6 +10,10 @@
 struct fdtd_sim {
   int solver = 0;
   bool tm = false, mpi = false, f32 = false;
+  int family = 0;               // 0 UPML, 1 split-field PML (fdtdTM.c / fdtdTE.c), 2 NS-FDTD (nsFdtd*.c)
+  void *d_coef = nullptr;       // family 1, 2: per-cell coefficients (fdtd_split.cu), ncoef x nxa x pitch
+  int ncoef = 0;
+  bool coef_dirty = true;       // the permittivity changed since the coefficients were made
   fdtd_config cfg{};
   fdtd_geometry geo{};
   // array frame (see fdtd_internal.cuh)

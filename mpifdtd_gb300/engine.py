@@ -14,10 +14,11 @@ import numpy as np
 
 from . import build as _build
 
-# simulator.h:8-18 enum SOLVER values of the UPML solvers
-TM_UPML_2D, TE_UPML_2D, MPI_TM_UPML_2D, MPI_TE_UPML_2D = 2, 3, 4, 5
+# simulator.h:8-18 enum SOLVER values
+TM_2D, TE_2D, TM_UPML_2D, TE_UPML_2D, MPI_TM_UPML_2D, MPI_TE_UPML_2D, NS_TM_2D, NS_TE_2D = range(8)
 SOLVERS = {"TM_UPML": TM_UPML_2D, "TE_UPML": TE_UPML_2D,
-           "MPI_TM_UPML": MPI_TM_UPML_2D, "MPI_TE_UPML": MPI_TE_UPML_2D}
+           "MPI_TM_UPML": MPI_TM_UPML_2D, "MPI_TE_UPML": MPI_TE_UPML_2D,
+           "TM_2D": TM_2D, "TE_2D": TE_2D, "NS_TM_2D": NS_TM_2D, "NS_TE_2D": NS_TE_2D}
 F64, F32 = 0, 1
 LAYOUT_GLOBAL, LAYOUT_SOLVER = 0, 1
 MODEL_NONE, MODEL_CIRCLE, MODEL_MORPHO, MODEL_ZIGZAG = 0, 1, 3, 5
@@ -201,7 +202,7 @@ class Simulation:
     # -- properties
     @property
     def tm(self):
-        return self.solver in (TM_UPML_2D, MPI_TM_UPML_2D)
+        return self.solver in (TM_UPML_2D, MPI_TM_UPML_2D, TM_2D, NS_TM_2D)
 
     @property
     def mpi(self):

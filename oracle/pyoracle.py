@@ -29,8 +29,11 @@ REF_SRC = Path(os.environ.get("MPIFDTD_REFERENCE", "/root/reference"))
 
 # simulator.h:8-18
 TM_UPML_2D, TE_UPML_2D, MPI_TM_UPML_2D, MPI_TE_UPML_2D = 2, 3, 4, 5
+TM_2D, TE_2D, NS_TM_2D, NS_TE_2D = 0, 1, 6, 7
 SOLVERS = {"TM_UPML": TM_UPML_2D, "TE_UPML": TE_UPML_2D,
-           "MPI_TM_UPML": MPI_TM_UPML_2D, "MPI_TE_UPML": MPI_TE_UPML_2D}
+           "MPI_TM_UPML": MPI_TM_UPML_2D, "MPI_TE_UPML": MPI_TE_UPML_2D,
+           # run by RefSim only (the C restatement covers the UPML solvers)
+           "TM_2D": TM_2D, "TE_2D": TE_2D, "NS_TM_2D": NS_TM_2D, "NS_TE_2D": NS_TE_2D}
 MODEL_NONE, MODEL_CIRCLE, MODEL_MORPHO, MODEL_DISCS, MODEL_ZIGZAG = 0, 1, 2, 3, 4
 NFFT = 8192
 
@@ -275,6 +278,11 @@ def ref_lib():
             f = getattr(lib, f"refh_{pre}_eps")
             f.restype = C.c_void_p
             f.argtypes = [C.c_int]
+        for pre in ("splittm", "splitte", "nstm", "nste"):
+            for suf in ("field", "eps"):
+                f = getattr(lib, f"refh_{pre}_{suf}")
+                f.restype = C.c_void_p
+                f.argtypes = [C.c_int]
         for pre in ("mpitm", "mpite"):
             getattr(lib, f"refh_{pre}_dims").argtypes = [C.POINTER(C.c_int)] * 2
         lib.field_getTime.restype = C.c_double
@@ -286,7 +294,8 @@ def ref_lib():
 class RefSim:
     """The reference itself (one at a time: it keeps global state)."""
 
-    _PRE = {MPI_TM_UPML_2D: "mpitm", MPI_TE_UPML_2D: "mpite", TM_UPML_2D: "sertm", TE_UPML_2D: "serte"}
+    _PRE = {MPI_TM_UPML_2D: "mpitm", MPI_TE_UPML_2D: "mpite", TM_UPML_2D: "sertm", TE_UPML_2D: "serte",
+            TM_2D: "splittm", TE_2D: "splitte", NS_TM_2D: "nstm", NS_TE_2D: "nste"}
 
     def __init__(self, solver, fi: FieldInfo, model: Model | None = None):
         self.lib = ref_lib()

@@ -15,11 +15,12 @@ CC      ?= gcc
 # keeps the x86 rounding when this is built on an FMA-capable host.
 CFLAGS  := -std=gnu99 -O3 -fPIC -ffp-contract=off -DLINUX_OS -w -I$(ORACLE)/mpi_stub -I$(REF)
 
-REF_SRCS := field.c simulator.c fdtdTM.c fdtdTE.c nsFdtdTM.c nsFdtdTE.c noModel.c \
+REF_SRCS := field.c simulator.c noModel.c \
             multiLayerModel.c traceImageModel.c concentricCircleModel.c \
             ntffTM.c ntffTE.c ntff.c cfft.c myComplex.c function.c parser.c drawer.c
 HARNESS  := ref_mpi_tm.c ref_mpi_te.c ref_ser_tm.c ref_ser_te.c ref_models.c \
-            ref_circle.c ref_morpho.c ref_zigzag.c ref_driver.c
+            ref_circle.c ref_morpho.c ref_zigzag.c ref_split_tm.c ref_split_te.c ref_ns_tm.c \
+            ref_ns_te.c ref_driver.c
 
 $(OUT)/libfdtdref.so: $(ORACLE)/ref.mk $(addprefix $(REF)/,$(REF_SRCS)) $(addprefix $(ORACLE)/ref_harness/,$(HARNESS)) $(ORACLE)/mpi_stub/mpi.h
 	mkdir -p $(OUT)

@@ -15,6 +15,10 @@ extern void refh_mpitm_init(void);
 extern void refh_mpite_init(void);
 extern void refh_sertm_init(void);
 extern void refh_serte_init(void);
+extern void refh_splittm_init(void);
+extern void refh_splitte_init(void);
+extern void refh_nstm_init(void);
+extern void refh_nste_init(void);
 extern void refh_models_set_callback(double (*fn)(double, double, int, int));
 extern void refh_circle_set_radius_nm(int r);
 extern void refh_circle_set_eps(double e);
@@ -58,6 +62,10 @@ int refh_setup(int solver, int width_nm, int height_nm, int h_u_nm, int pml,
   case MPI_TE_UPML_2D: refh_mpite_init(); break;
   case TM_UPML_2D: refh_sertm_init(); break;
   case TE_UPML_2D: refh_serte_init(); break;
+  case TM_2D: refh_splittm_init(); break;
+  case TE_2D: refh_splitte_init(); break;
+  case NS_TM_2D: refh_nstm_init(); break;
+  case NS_TE_2D: refh_nste_init(); break;
   default: return -2;
   }
   return 0;

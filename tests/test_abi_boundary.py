@@ -136,7 +136,7 @@ def test_dropin_without_gpu_reports_and_returns(libs):
 REF = Path(os.environ.get("MPIFDTD_REFERENCE", "/root/reference"))
 REF_HOST_SOURCES = ["main.c", "simulator.c", "field.c", "models.c", "noModel.c", "circleModel.c",
                     "morphoScaleModel.c", "multiLayerModel.c", "zigzagModel.c", "traceImageModel.c",
-                    "concentricCircleModel.c", "fdtdTM.c", "fdtdTE.c", "nsFdtdTM.c", "nsFdtdTE.c", "ntffTM.c",
+                    "concentricCircleModel.c", "ntffTM.c",
                     "ntffTE.c", "ntff.c", "cfft.c", "myComplex.c", "function.c", "parser.c", "drawer.c"]
 
 
@@ -144,7 +144,8 @@ REF_HOST_SOURCES = ["main.c", "simulator.c", "field.c", "models.c", "noModel.c",
 def test_reference_program_links_against_dropin(libs, tmp_path):
     """The reference's own host program -- main.c, simulator.c, field.c,
     models.c and the rest, unmodified -- links with libmpifdtd_upml.so in place
-    of mpiTM_UPML.c, mpiTE_UPML.c, fdtdTM_upml.c and fdtdTE_upml.c."""
+    of all eight solver sources (mpiTM_UPML.c, mpiTE_UPML.c, fdtdTM_upml.c,
+    fdtdTE_upml.c, fdtdTM.c, fdtdTE.c, nsFdtdTM.c, nsFdtdTE.c)."""
     b = libs["build"]
     exe = tmp_path / "mpi_fdtd2D"
     cmd = ["gcc", "-std=gnu99", "-O1", "-w", "-DLINUX_OS", f"-I{ROOT / 'oracle' / 'mpi_stub'}", f"-I{REF}",
@@ -154,3 +155,4 @@ def test_reference_program_links_against_dropin(libs, tmp_path):
     assert r.returncode == 0, r.stderr[-3000:]
     syms = subprocess.run(["nm", str(exe)], capture_output=True, text=True).stdout
     assert " U mpi_fdtdTM_upml_getUpdate" in syms and " U fdtdTE_upml_getInit" in syms
+    assert " U fdtdTM_getUpdate" in syms and " U nsFdtdTE_getInit" in syms

@@ -39,7 +39,8 @@ def libs():
 
 VOIDFN = C.CFUNCTYPE(None)
 PREFIX = {"MPI_TM_UPML": "mpi_fdtdTM_upml_", "MPI_TE_UPML": "mpi_fdtdTE_upml_",
-          "TM_UPML": "fdtdTM_upml_", "TE_UPML": "fdtdTE_upml_"}
+          "TM_UPML": "fdtdTM_upml_", "TE_UPML": "fdtdTE_upml_",
+          "TM_2D": "fdtdTM_", "TE_2D": "fdtdTE_", "NS_TM_2D": "nsFdtdTM_", "NS_TE_2D": "nsFdtdTE_"}
 
 
 def _fn(lib, name, restype):
@@ -125,3 +126,44 @@ def test_dropin_serial_reset_writes_reference_spectrum(libs, name, tmp_path):
         _fn(upml, pre + "getFinish", VOIDFN)()()            # finish() writes the spectrum again (reset first)
     finally:
         os.chdir(cwd)
+
+
+@pytest.mark.parametrize("name,ring", [("split_tm_circle", "tm_5nm.txt"), ("split_te_circle_30deg", "te_5nm.txt"),
+                                       ("ns_te_circle_20deg", "ns_te_5nm.txt")])
+def test_dropin_split_and_ns_solvers(libs, name, ring, tmp_path):
+    """The split-field PML and NS-FDTD entry points (fdtdTM.h, fdtdTE.h,
+    nsFdtdTE.h): fields, split parts and getEps against the reference's golden
+    vectors; reset() writes field_outputElliptic's ring file."""
+    upml, pre, shape, _ = drive(libs, name)
+    ref = np.load(GOLDEN / f"{name}.npz")
+    tm = "TM" in pre
+    names = ("getEz", "getHx", "getHy") if tm else ("getEx", "getEy", "getHz")
+    got = [_array(_fn(upml, pre + g, C.c_void_p)(), shape, np.complex128) for g in names]
+    for w in range(3):
+        assert rel(got[w], ref[f"field{w}"]) <= 1e-12, (name, names[w])
+    parts = ("getEzx", "getEzy") if tm else ("getHzx", "getHzy")
+    a, b = (_array(_fn(upml, pre + g, C.c_void_p)(), shape, np.complex128) for g in parts)
+    if not tm:                                              # Hz = Hzx + Hzy after calcH
+        np.testing.assert_array_equal(a + b, got[2])
+    eps = _array(_fn(upml, pre + "getEps", C.c_void_p)(), shape, np.float64)
+    np.testing.assert_array_equal(eps, ref["eps0"] if tm else ref["eps1"])   # EPS_EZ / EPS_EY
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        _fn(upml, pre + "getReset", VOIDFN)()()
+    finally:
+        os.chdir(cwd)
+    lines = (tmp_path / ring).read_text().splitlines()
+    want = ref["elliptic_text"].tobytes().decode().splitlines()
+    assert len(lines) == len(want) == 181
+    got_v = np.array([float(x.split()[1]) for x in lines])
+    want_v = np.array([float(x.split()[1]) for x in want])
+    assert np.abs(got_v - want_v).max() <= 1e-6 + 1e-12
+    a = _array(_fn(upml, pre + names[0], C.c_void_p)(), shape, np.complex128)
+    assert np.all(a == 0)                                   # reset zeroes the fields
+    os.chdir(tmp_path)
+    try:
+        _fn(upml, pre + "getFinish", VOIDFN)()()            # finish() = reset() + free (writes the ring again)
+    finally:
+        os.chdir(cwd)
+    assert upml.mpifdtd_upml_last_status() == 0

@@ -39,7 +39,7 @@ def run_gpu(name, precision="f64"):
     sim.run(c["steps"])
     fields = [sim.field(w) for w in range(3)]
     eps = [sim.eps(w) for w in range(3)]
-    ntff = [sim.ntff(w) for w in range(3)]
+    ntff = [] if c.get("ref_only") else [sim.ntff(w) for w in range(3)]   # split-field / NS: no NTFF
     out = capture(fields, eps, ntff, sim.array_size, c["kind"], c.get("rows", "all"))
     extras = c.get("extras", ())
     if "spectrum" in extras:
@@ -70,7 +70,8 @@ def test_gpu_spectrum_rejects_more_than_8192_steps():
 
 
 MODEL_CASES = ["mpi_tm_circle", "mpi_te_circle", "mpi_tm_morpho", "mpi_te_morpho_eps225", "ser_tm_circle",
-               "ser_te_circle", "mpi_tm_zigzag", "mpi_te_zigzag_40deg"]
+               "ser_te_circle", "mpi_tm_zigzag", "mpi_te_zigzag_40deg", "split_tm_circle", "split_te_circle_30deg",
+               "ns_tm_morpho", "ns_te_circle_20deg"]
 
 
 def _product_model(spec):
@@ -246,3 +247,18 @@ def test_gpu_ntff_guards_untouched():
     sim, _ = run_gpu("mpi_tm_circle")
     for w in range(3):
         assert np.all(sim.ntff_guard(w) == 0)
+
+
+def test_gpu_split_and_ns_solvers_refuse_ntff_and_fp32():
+    """The split-field / NS solvers have no NTFF and run in FP64 only."""
+    m = _engine()
+    fi = m.FieldInfo(300, 300, 5, 10, 100, 0, 20)
+    with pytest.raises(m.FdtdError):
+        m.Simulation("TM_2D", fi, "f32")
+    sim = m.Simulation("NS_TM_2D", fi)
+    sim.run(5)
+    for call in (sim.frequency, sim.spectrum, lambda: sim.ntff(0)):
+        with pytest.raises(m.FdtdError):
+            call()
+    ez, ezx, ezy = sim.field(0), sim.field(3), sim.field(4)
+    np.testing.assert_array_equal(ez, ezx + ezy)            # nsFdtdTM.c:73-76: Ez = Ezx + Ezy
