@@ -385,7 +385,11 @@ __device__ __forceinline__ void block_field(const NtffView &n, double2 *acc, lon
     for (int j = 0; j <= nb + 1; j++) {
       const double4 q = dg[(size_t)j * 2 * n.ncell];
       const double2 f = make_double2(fma(-a, q.z, q.x), fma(-a, q.w, q.y));
-      if (f.x != 0.0 || f.y != 0.0) red_c(n, acc, m0 + j - 1, f);
+      // skip (+-)0 + (+-)0i: tested on the bit patterns (integer ALU), not with two
+      // FP64 compares, which would double the FP64 work of the loop
+      const unsigned long long bits =
+          (unsigned long long)__double_as_longlong(f.x) | (unsigned long long)__double_as_longlong(f.y);
+      if (bits << 1) red_c(n, acc, m0 + j - 1, f);
     }
     return;
   }
