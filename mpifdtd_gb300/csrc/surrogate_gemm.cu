@@ -5,9 +5,10 @@
 //   C[M,N] (FP32 or BF16, row-major, ldc) = A[M,K] . B[N,K]^T (+ bias[N])
 //   (+ C if accumulate), optional GELU, with A, B BF16 row-major ("K-major").
 //
-// One CTA computes one 128 x BN output tile with 128 threads:
+// One CTA computes one 128 x BN output tile with 128 threads, two CTAs per SM
+// (so that one CTA's epilogue runs under the other's MMAs):
 //   thread 0 (warp 0)  TMA producer: 128 x 64 and BN x 64 operand tiles, 128-byte
-//                      swizzled, into a 4-stage shared-memory ring (mbarrier
+//                      swizzled, into a 3-stage shared-memory ring (mbarrier
 //                      full[s] with the transaction byte count);
 //   thread 32 (warp 1) MMA issuer: four tcgen05.mma.kind::f16 (K = 16 each) per
 //                      stage into an FP32 accumulator in TMEM, tcgen05.commit
@@ -32,7 +33,8 @@
 
 namespace sg {
 
-constexpr int BM = 128, BK = 64, STAGES = 4;
+constexpr int BM = 128, BK = 64, STAGES = 3;  // 3 x 32 KB (BN = 128): two CTAs fit in an SM
+constexpr int GROUP_M = 8;  // tile raster: GROUP_M row tiles share their column tiles' B panels in L2
 constexpr unsigned kSpinLimit = 1u << 26;  // ~ seconds of polling, then give up
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -148,7 +150,7 @@ struct Epilogue {
 };
 
 template <int BN>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(128, 2)
     gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, Epilogue ep,
                         int K, int b_batched, unsigned *err)
 {
@@ -162,7 +164,16 @@ __global__ void __launch_bounds__(128, 1)
   uint64_t *done = empty + STAGES;
   uint32_t *tmem_slot = (uint32_t *)(done + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN, z = blockIdx.z;
+  // grouped raster of the (column, row) tiles: consecutive CTAs walk GROUP_M
+  // row tiles for each column tile, so the A and B panels of the CTAs in
+  // flight stay in L2
+  const int n_tiles = gridDim.x, m_tiles = gridDim.y;
+  const int id = blockIdx.y * n_tiles + blockIdx.x;
+  const int group = id / (GROUP_M * n_tiles);
+  const int first_m = group * GROUP_M;
+  const int gm = min(GROUP_M, m_tiles - first_m);
+  const int in_group = id - group * GROUP_M * n_tiles;
+  const int m0 = (first_m + in_group % gm) * BM, n0 = (in_group / gm) * BN, z = blockIdx.z;
   const int nk = K / BK;
 
   if (threadIdx.x == 0) {
