@@ -22,6 +22,8 @@ def main(argv=None):
     ap.add_argument("--batch", type=int, default=128)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--no-shift", action="store_true", help="no random translations of the training maps")
+    ap.add_argument("--views", type=int, default=1,
+                    help="average the prediction over the structure, its mirror image and views-2 translations")
     ap.add_argument("--seed", type=int, default=20261207)
     ap.add_argument("--tol", type=float, default=0.02)
     a = ap.parse_args(argv)
@@ -33,15 +35,18 @@ def main(argv=None):
     net = FNO(seed=1)
     t_train = S.train(net, maps[:a.train], inten[:a.train], steps=a.steps, batch=a.batch, lr=a.lr,
                       shift=not a.no_shift)
-    ev = S.evaluate(net, maps[a.train:], inten[a.train:], inten[:a.train])
+    ev = S.evaluate(net, maps[a.train:], inten[a.train:], inten[:a.train], views=a.views)
+    ev1 = ev if a.views <= 1 else S.evaluate(net, maps[a.train:], inten[a.train:])
     rate = S.inference_rate(net)
     k = max(1, int(np.ceil(0.01 * a.val)))
     audit = Generator(group=k)
-    _, st = S.screen(net, maps[a.train:], gen, audit_frac=0.01, tol=a.tol, batch=a.val, audit_gen=audit)
+    _, st = S.screen(net, maps[a.train:], gen, audit_frac=0.01, tol=a.tol, batch=a.val, audit_gen=audit,
+                     views=a.views)
     out = {"maps": a.train + a.val, "fdtd_structures_per_s": (a.train + a.val) / sec,
            "train": {"maps": a.train, "with_mirror_images": 2 * a.train, "steps": a.steps, "lr": a.lr,
                      "random_translations": not a.no_shift, "seconds": t_train},
-           "heldout_rel_l2": ev, "network_structures_per_s": rate,
+           "heldout_rel_l2": ev, "views": a.views, "heldout_rel_l2_one_view": ev1, "network_structures_per_s": rate,
+           "network_structures_per_s_with_views": rate / max(1, a.views),
            "screen": {k2: v for k2, v in st.items()}}
     json.dump(out, sys.stdout)
     print()

@@ -110,11 +110,31 @@ def train(net: FNO, maps, inten, steps=400, batch=128, lr=1e-3, seed=0, log=None
     return time.perf_counter() - t0
 
 
-def evaluate(net: FNO, maps, inten, train_inten=None):
+def predict(net: FNO, maps, views=1, seed=11):
+    """Far-field intensity [N, 31, 360] of host maps.  views > 1 averages the
+    network over symmetric views of each structure, whose far-field
+    intensities are the same up to the known angle map: its mirror image
+    (y -> -y, phi -> -phi) and views - 2 random translations."""
+    import torch
+    dev = torch.tensor(maps, device="cuda")
+    pred = net.predict(dev)
+    if views <= 1:
+        return pred.cpu().numpy()
+    ang = torch.tensor((360 - np.arange(360)) % 360, device="cuda")
+    acc = pred + net.predict(torch.flip(dev, dims=[2]).contiguous())[:, :, ang]
+    if views > 2:
+        ranges = shift_ranges(np.asarray(maps))
+        rng = np.random.default_rng(seed)
+        idx = np.arange(len(maps))
+        for _ in range(views - 2):
+            acc += net.predict(shifted(dev, idx, ranges, rng))
+    return (acc / views).cpu().numpy()
+
+
+def evaluate(net: FNO, maps, inten, train_inten=None, views=1):
     """Errors of the network and of the network-free baseline (the mean
     far field of the training set, the best constant prediction)."""
-    import torch
-    pred = net.predict(torch.tensor(maps, device="cuda")).cpu().numpy()
+    pred = predict(net, maps, views)
     err = rel_err(pred, inten)
     out = {"median": float(np.median(err)), "p90": float(np.percentile(err, 90)),
            "within_2pct": float(np.mean(err <= 0.02)), "n": int(len(err))}
@@ -127,7 +147,8 @@ def evaluate(net: FNO, maps, inten, train_inten=None):
 
 
 def inference_rate(net: FNO, n=16384, batch=4096, seed=99):
-    """Structures per second of the network alone (maps already on the GPU)."""
+    """Structures per second of the network alone (maps already on the GPU,
+    one view per structure)."""
     import torch
     maps = torch.tensor(make_maps(min(n, 512), seed), device="cuda")
     reps = (n + len(maps) - 1) // len(maps)
@@ -140,12 +161,13 @@ def inference_rate(net: FNO, n=16384, batch=4096, seed=99):
     return n / (time.perf_counter() - t0)
 
 
-def screen(net: FNO, maps, gen: Generator, audit_frac=0.01, tol=0.02, batch=4096, seed=7, audit_gen=None):
-    """Audited surrogate screening.  Per screening batch: predict all, run
-    FDTD on ceil(audit_frac * batch) random structures (audit_gen: a
-    generator sized for the audit), and if any of them is off by more than
-    tol, replace the batch by FDTD (gen).  Returns (intensity, stats)."""
-    import torch
+def screen(net: FNO, maps, gen: Generator, audit_frac=0.01, tol=0.02, batch=4096, seed=7, audit_gen=None,
+           views=1):
+    """Audited surrogate screening.  Per screening batch: predict all (views:
+    see predict), run FDTD on ceil(audit_frac * batch) random structures
+    (audit_gen: a generator sized for the audit), and if any of them is off
+    by more than tol, replace the batch by FDTD (gen).  Returns (intensity,
+    stats)."""
     rng = np.random.default_rng(seed)
     audit_gen = audit_gen or gen
     out = np.zeros((len(maps), 31, 360), np.float32)
@@ -153,7 +175,7 @@ def screen(net: FNO, maps, gen: Generator, audit_frac=0.01, tol=0.02, batch=4096
     t0 = time.perf_counter()
     for s in range(0, len(maps), batch):
         part = maps[s:s + batch]
-        pred = net.predict(torch.tensor(part, device="cuda")).cpu().numpy()
+        pred = predict(net, part, views)
         k = max(1, int(math.ceil(audit_frac * len(part))))
         pick = rng.choice(len(part), k, replace=False)
         ref = audit_gen.far_field(part[pick])

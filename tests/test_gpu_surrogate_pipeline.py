@@ -49,6 +49,18 @@ def test_translation_augmentation_matches_the_physics(trained):
     assert np.median(S.rel_err(fm, inten[:8])) < 0.02
 
 
+def test_multi_view_prediction_averages_symmetric_views(trained):
+    """predict(views=2) is the mean of the direct prediction and the mirrored
+    structure's prediction mapped back (phi -> -phi)."""
+    S, gen, net, maps, inten = trained
+    sub = maps[192:200]
+    direct = S.predict(net, sub)
+    mirrored = S.predict(net, sub[:, :, ::-1].copy())[:, :, (360 - np.arange(360)) % 360]
+    np.testing.assert_allclose(S.predict(net, sub, views=2), 0.5 * (direct + mirrored), rtol=1e-5, atol=1e-7)
+    four = S.predict(net, sub, views=4)
+    assert four.shape == direct.shape and np.isfinite(four).all()
+
+
 def test_screening_fallback_and_audit(trained):
     S, gen, net, maps, inten = trained
     part = maps[192:256]
