@@ -16,7 +16,7 @@ DISCS_A = [(8.0, 30.0, 7.0, 3.0), (30.0, 32.0, 10.0, 2.25), (50.0, 14.0, 6.0, 4.
 DISCS_B = [(20.0, 20.0, 9.0, 2.0), (45.0, 40.0, 12.0, 3.5), (58.0, 58.0, 5.0, 1.3)]
 
 CASES = {
-    # SURVEY config 1 exactly as the reference runs it: vacuum keeps every field 0.
+    # The 276^2 vacuum run exactly as the reference runs it: every field stays 0.
     "mpi_tm_vacuum_c1": dict(solver="MPI_TM_UPML", fi=(1380, 1380, 5, 10, 400, 0, 2000),
                              model=("none",), steps=2000, kind="stats"),
     "mpi_tm_circle": dict(solver="MPI_TM_UPML", fi=(300, 320, 5, 6, 100, 0, 150),
@@ -57,7 +57,7 @@ CASES = {
     "ns_te_circle_20deg": dict(solver="NS_TE_2D", fi=(300, 320, 5, 10, 100, 20, 200),
                                model=("circle", 60, 0.0), steps=200, kind="full", ref_only=True,
                                extras=("elliptic",)),
-    # SURVEY config 2 grid (1044^2, eps 2.25 override) for the first 40 of 4000 steps.
+    # The 1044^2 Mie grid (r 500 nm, eps 2.25 override) for the first 40 of 4000 steps.
     "mpi_tm_c2_head": dict(solver="MPI_TM_UPML", fi=(5220, 5220, 5, 10, 500, 0, 4000),
                            model=("circle", 500, 2.25), steps=40, kind="stats"),
     "mpi_te_c2_head": dict(solver="MPI_TE_UPML", fi=(5220, 5220, 5, 10, 500, 0, 4000),

@@ -44,7 +44,7 @@ def _mie_error(ff, r, lam, eps, pol, incidence=0.0):
     return mie.pattern_error(np.abs(ff) ** 2, ref)[0]
 
 
-# SURVEY config-2 grid: 1044^2 cells of 5 nm, r = 500 nm, lambda = 500 nm, 4000 steps
+# The 1044^2 Mie grid: 5 nm cells, r = 500 nm, lambda = 500 nm, 4000 steps
 C2 = (5220, 5220, 5, 10, 500, 0, 4000)
 
 

@@ -1,6 +1,6 @@
 """GPU parity: the CUDA engine against the reference's golden vectors and the oracle.
 
-Bar (the benchmark spec): FP64 fields and NTFF accumulators within 1e-12 relative L2
+Bar: FP64 fields and NTFF accumulators within 1e-12 relative L2
 of the reference.  Permittivity is an input here: the golden ("full") cases
 carry the reference's own eps arrays, the others take the oracle's.
 """
@@ -172,7 +172,7 @@ def test_gpu_rows_per_thread_variants(name, rows):
 
 def test_gpu_fp32_error_against_fp64():
     """FP32 fields with FP64 NTFF: field relative L2 and far-field error (dB)
-    against the FP64 engine on the 1044^2 Mie case (config-2 grid, eps 2.25)."""
+    against the FP64 engine on the 1044^2 Mie case (r 500 nm, eps 2.25)."""
     from mpifdtd_gb300.precision import compare_precisions
     m = _engine()
     fi = m.FieldInfo(5220, 5220, 5, 10, 500, 0, 4000)
@@ -183,7 +183,7 @@ def test_gpu_fp32_error_against_fp64():
 
 
 def test_gpu_vacuum_config1_exact_zero():
-    """SURVEY config 1 (276^2, vacuum, 2000 steps): every output stays exactly 0."""
+    """The 276^2 vacuum run (2000 steps): every output stays exactly 0."""
     _, got = run_gpu("mpi_tm_vacuum_c1")
     for k, v in got.items():
         if not k.startswith("meta_"):
@@ -192,7 +192,7 @@ def test_gpu_vacuum_config1_exact_zero():
 
 @pytest.mark.parametrize("solver", ["MPI_TM_UPML", "MPI_TE_UPML"])
 def test_gpu_fp64_matches_oracle_full_c2_grid(solver):
-    """1044^2 Mie cylinder (SURVEY config 2 grid, eps 2.25), 120 steps: full arrays."""
+    """1044^2 Mie cylinder (r 500 nm, eps 2.25), 120 steps: full arrays."""
     from oracle.pyoracle import FieldInfo as OFI, Model, OracleSim
     m = _engine()
     fi = (5220, 5220, 5, 10, 500, 0, 4000)

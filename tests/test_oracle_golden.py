@@ -45,7 +45,7 @@ def test_oracle_matches_reference_golden(oracle_built, name):
 
 
 def test_vacuum_stays_exactly_zero(oracle_built):
-    """the scattered-field source is zero where eps == 1."""
+    """The scattered-field source is zero where eps == 1, so vacuum stays exactly 0."""
     ref = dict(np.load(GOLDEN / "mpi_tm_vacuum_c1.npz"))
     for k, v in ref.items():
         if not k.startswith("meta_"):
@@ -53,7 +53,7 @@ def test_vacuum_stays_exactly_zero(oracle_built):
 
 
 def test_ntff_guards_untouched_on_golden_cases(oracle_built):
-    """Flat NTFF indexing never leaves the 360*arraySize block here."""
+    """The flat [360][arraySize] NTFF indexing never leaves the 360*arraySize block here."""
     c = CASES["mpi_tm_circle"]
     sim = OracleSim(c["solver"], FieldInfo(*c["fi"]), make_model(c["model"]))
     sim.step(c["steps"])
