@@ -1,8 +1,8 @@
 /*
  * fdtd_oracle.h -- CPU restatement of rennone/mpiFDTD's UPML time-stepping
  * path.  TEST INFRASTRUCTURE: only tests/, __graft_entry__.smoke() and the
- * CPU-baseline leg of bench.py may load it, and only as the checker or as the
- * timed CPU baseline.  The product (mpifdtd_gb300) never links or calls it.
+ * CPU-baseline leg of bench.py may load it, and only as the reference the
+ * results are compared with or as the timed CPU baseline.  The product (mpifdtd_gb300) never links or calls it.
  *
  * Parity pin: the restatement is checked against golden vectors produced by
  * the reference's own C sources compiled unmodified (oracle/ref.mk ->

@@ -2,8 +2,8 @@
 
 * ``OracleSim`` wraps ``fdtd_oracle.c``, the project's C restatement of the
   reference's UPML path (built into ``oracle/_build``).  It runs anywhere a C
-  compiler exists, including the GPU machine, and is the checker for the CUDA path
-  and the CPU baseline of ``bench.py``.
+  compiler exists and is what the tests compare the CUDA path with, and the
+  CPU baseline of ``bench.py``.
 * ``RefSim`` wraps the reference's own C sources compiled unmodified
   (``oracle/ref.mk`` -> ``oracle/_ref/libfdtdref.so``).  It exists only where
   the reference sources are present and pins ``OracleSim``; its outputs are
