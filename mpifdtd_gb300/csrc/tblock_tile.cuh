@@ -104,6 +104,18 @@ __device__ __forceinline__ void st_cols(T *p, const bool *own, const T *val)
     if (own[q]) p[q] = val[q];
 }
 
+// L2 prefetch of the row holding p[0] .. p[32 CPL - 1] of a warp (elements of
+// `bytes` each): the lanes at 128-byte strides and the last lane issue it, so
+// every line the warp's row touches is requested once.  The prefetched rows
+// are rows the tile loads two row-steps later; a prefetch takes no register.
+template <int CPL>
+__device__ __forceinline__ void prefetch_row(const void *p, int bytes)
+{
+  const int lane = threadIdx.x & 31, per_line = 128 / (bytes * CPL);
+  if (per_line <= 1 || lane % per_line == 0 || lane == 31)
+    asm volatile("prefetch.L2 [%0];" ::"l"(p));
+}
+
 // One lane's view of its tile.
 template <int CPL>
 struct Lane {
@@ -240,6 +252,17 @@ __device__ __forceinline__ void tm_tile(const StencilView<R> &v, const TBlockVie
       ph0[q] = ph1[q];
     }
     load0(r + 2, pe1, ph1);
+    if (!AUX) {  // rows the interior tile loads two row-steps later
+      const int rp = r + 4, ap = rp + 1;
+      if (ap >= 1 && ap <= v.ni) {
+        prefetch_row<CPL>(Dz + (size_t)ap * P + j, sizeof(T));
+        prefetch_row<CPL>(IE + (size_t)ap * P + j, sizeof(R));
+      }
+      if (rp >= 1 && rp <= v.ni) {
+        prefetch_row<CPL>(Hx + (size_t)rp * P + j, sizeof(T));
+        prefetch_row<CPL>(Hy + (size_t)rp * P + j, sizeof(T));
+      }
+    }
 #pragma unroll
     for (int l = 1; l <= K; l++) {
       const int e = r - l + 1, h = r - l;
@@ -442,6 +465,16 @@ __device__ __forceinline__ void te_tile(const StencilView<R> &v, const TBlockVie
       ph0[q] = ph1[q];
     }
     load0(r + 2, pe1, ph1);
+    if (!AUX) {  // rows the interior tile loads two row-steps later
+      const int rp = r + 4, ap = rp + 1;
+      if (ap >= 1 && ap <= v.ni) {
+        prefetch_row<CPL>(Dx + (size_t)ap * P + j, sizeof(T));
+        prefetch_row<CPL>(Dy + (size_t)ap * P + j, sizeof(T));
+        prefetch_row<CPL>(IEX + (size_t)ap * P + j, sizeof(R));
+        prefetch_row<CPL>(IEY + (size_t)ap * P + j, sizeof(R));
+      }
+      if (rp >= 1 && rp <= v.ni) prefetch_row<CPL>(Hz + (size_t)rp * P + j, sizeof(T));
+    }
 #pragma unroll
     for (int l = 1; l <= K; l++) {
       const int e = r - l + 1, h = r - l;
