@@ -252,7 +252,7 @@ __device__ __forceinline__ void tm_tile(const StencilView<R> &v, const TBlockVie
       ph0[q] = ph1[q];
     }
     load0(r + 2, pe1, ph1);
-    if (!AUX) {  // rows the interior tile loads two row-steps later
+    {  // rows the tile loads two row-steps later
       const int rp = r + 4, ap = rp + 1;
       if (ap >= 1 && ap <= v.ni) {
         prefetch_row<CPL>(Dz + (size_t)ap * P + j, sizeof(T));
@@ -465,7 +465,7 @@ __device__ __forceinline__ void te_tile(const StencilView<R> &v, const TBlockVie
       ph0[q] = ph1[q];
     }
     load0(r + 2, pe1, ph1);
-    if (!AUX) {  // rows the interior tile loads two row-steps later
+    {  // rows the tile loads two row-steps later
       const int rp = r + 4, ap = rp + 1;
       if (ap >= 1 && ap <= v.ni) {
         prefetch_row<CPL>(Dx + (size_t)ap * P + j, sizeof(T));
