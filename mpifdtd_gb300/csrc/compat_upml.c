@@ -90,8 +90,8 @@ static void release(slot *s)
 }
 
 /* setCoefficient()'s permittivity: mpiTM_UPML.c:680-682, mpiTE_UPML.c:503-505,
- * fdtdTM_upml.c:237-239, fdtdTE_upml.c:374-376, fdtdTM.c:206-208,
- * fdtdTE.c:207-209, nsFdtdTM.c:233-235, nsFdtdTE.c:118-120 (inner cells only),
+ * fdtdTM_upml.c:237-239, fdtdTE_upml.c:374-376, fdtdTM.c:209-211,
+ * fdtdTE.c:210-212, nsFdtdTM.c:244-246, nsFdtdTE.c:119-121 (inner cells only),
  * on the global frame. */
 static void fill_eps(const slot *s, double *e0, double *e1, double *e2)
 {
@@ -210,8 +210,8 @@ static void write_spectrum(const double *spec)
 }
 
 /* field_outputElliptic of the E field the split-field / NS reset() writes:
- * fdtdTM.c:148-151 "tm_%dnm.txt" (Ez), fdtdTE.c:259-262 "te_%dnm.txt" (Ey),
- * nsFdtdTM.c:161-164 "ns_tm_%dnm.txt", nsFdtdTE.c:201-204 "ns_te_%dnm.txt" */
+ * fdtdTM.c:158-159 "tm_%dnm.txt" (Ez), fdtdTE.c:273-274 "te_%dnm.txt" (Ey),
+ * nsFdtdTM.c:163-164 "ns_tm_%dnm.txt", nsFdtdTE.c:222-223 "ns_te_%dnm.txt" */
 static void write_elliptic(slot *s)
 {
   static const char *fmt[4] = {"tm_%dnm.txt", "te_%dnm.txt", "ns_tm_%dnm.txt", "ns_te_%dnm.txt"};

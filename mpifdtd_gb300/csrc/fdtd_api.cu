@@ -509,7 +509,7 @@ extern "C" int fdtd_fill_eps_model(fdtd_sim *s, int model, const double *params,
                    s->ncols, s->ox, s->geo.n_px, s->geo.n_py, s->tm, alt, m, s->stream);
   s->launches += 1;
   CK(cudaGetLastError());
-  if (s->solver == FDTD_NS_TE_2D) {  // nsFdtdTE.c:114-121 sets EPS_* on the inner cells only (FOR_FOR)
+  if (s->solver == FDTD_NS_TE_2D) {  // nsFdtdTE.c:116-121 sets EPS_* on the inner cells only (FOR_FOR)
     const size_t rowb = (size_t)s->pitch * sizeof(double);
     for (int a = 0; a < 3; a++) {
       char *e = (char *)s->d_eps[a];
@@ -1156,9 +1156,9 @@ extern "C" int fdtd_profile_read(fdtd_sim *s, double *ms_out, long long *steps)
 
 // ------------------------------------------------- split-field / NS solvers
 
-// Per-cell coefficients of the split-field PML solvers (fdtdTM.c:187-241,
-// fdtdTE.c:198-238) and the NS-FDTD solvers (nsFdtdTM.c:213-291,
-// nsFdtdTE.c:106-182), from the permittivity as it is now, in the reference's
+// Per-cell coefficients of the split-field PML solvers (fdtdTM.c:167-242,
+// fdtdTE.c:170-238) and the NS-FDTD solvers (nsFdtdTM.c:231-307,
+// nsFdtdTE.c:100-181), from the permittivity as it is now, in the reference's
 // expression order (this file is compiled without contraction).  Layout:
 // fdtd_split.cu.
 static int split_coefficients(fdtd_sim *s)
@@ -1183,10 +1183,10 @@ static int split_coefficients(fdtd_sim *s)
   auto sy = [&](double y) { return sigma_axis(y, npml, g.n_y, NY); };  // field_sigmaY (field.c:272-283)
   const double EPS0 = 1.0, C0 = kC, MU0 = 1.0 / kC / kC, LIGHT = kC;   // field.h:70-74
   const double R = 1.0e-8, M = 2.0;
-  // field.c:132-133 pmlCoef / pmlCoef_LXY
+  // field.c:288-295 pmlCoef / pmlCoef_LXY
   auto pml = [](double ep, double sig) { return (1.0 - sig / ep) / (1.0 + sig / ep); };
   auto lxy = [](double ep, double sig) { return 1.0 / (ep + sig); };
-  // nsFdtdTM.c:199-208 beta / coef1
+  // nsFdtdTM.c:221-229 beta / coef1
   auto beta = [](double a) { return tanh(a) / (1 + pow(tanh(a), 2)); };
   auto coef1 = [](double a, double b) { return (1 - b) / (1 + b); };
   const double w_s = g.omega_s, k_s = g.k_s;
@@ -1260,7 +1260,7 @@ static int split_coefficients(fdtd_sim *s)
         C(0, x, y) = coef1(a_ez_x, b_ez_x);
         C(1, x, y) = u_ez * z_ez / (1 + b_ez_x);
         C(2, x, y) = coef1(a_ez_y, b_ez_y);
-        C(3, x, y) = u_ez * z_ez / (1.0 + b_ez_x);  // nsFdtdTM.c:268: b_ez_x, as written
+        C(3, x, y) = u_ez * z_ez / (1.0 + b_ez_x);  // nsFdtdTM.c:287: b_ez_x, as written
         const double z_hx = sqrt(MU0 / ehx), u_hx = ns_u(ehx);
         C(4, x, y) = coef1(a_hx_y, b_hx_y);
         C(5, x, y) = u_hx / z_hx / (1.0 + b_hx_y);
@@ -1321,9 +1321,9 @@ static void enqueue_split(fdtd_sim *s, double time, double ray_coef)
   const double rad = s->cfg.angle_deg * M_PI / 180.0;  // field.c:162-163, 186-187
   v.ks_cos = cos(rad) * k_s;
   v.ks_sin = sin(rad) * k_s;
-  const double r = 1.0 / 6.0 + k_s * k_s / 180.0 - pow(k_s, 4) / 23040;  // nsFdtdTM.c:114-115
+  const double r = 1.0 / 6.0 + k_s * k_s / 180.0 - pow(k_s, 4) / 23040;  // nsFdtdTM.c:117
   v.r_2 = r / 2.0;
-  v.co = cos((s->cfg.angle_deg + 90) * M_PI / 180.0);  // nsFdtdTE.c:228-229
+  v.co = cos((s->cfg.angle_deg + 90) * M_PI / 180.0);  // nsFdtdTE.c:244-245
   v.si = sin((s->cfg.angle_deg + 90) * M_PI / 180.0);
   mark(s);
   launch_split_step(v, s->solver, s->stream);

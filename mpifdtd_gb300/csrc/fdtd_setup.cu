@@ -7,9 +7,9 @@
 //   serial TM  EZ (x,y,D_XY)  HX (x,y+.5,D_XY) HY (x+.5,y,D_XY) fdtdTM_upml.c:237-239
 //   TE       EX (x+.5,y,D_Y)  EY (x,y+.5,D_X)
 //            HZ 0.5*(eps(x+.5,y+.5,D_X) + eps(x+.5,y+.5,D_Y))  mpiTE_UPML.c:503-505
-//   split-field and NS TM as MPI TM (fdtdTM.c:206-208, nsFdtdTM.c:233-235),
-//   split-field TE as TE (fdtdTE.c:207-209), NS TE with HZ (x+.5,y+.5,D_XY)
-//   (nsFdtdTE.c:118-120)
+//   split-field and NS TM as MPI TM (fdtdTM.c:209-211, nsFdtdTM.c:244-246),
+//   split-field TE as TE (fdtdTE.c:210-212), NS TE with HZ (x+.5,y+.5,D_XY)
+//   (nsFdtdTE.c:119-121)
 #include <cuda_runtime.h>
 
 #include "fdtd_internal.cuh"

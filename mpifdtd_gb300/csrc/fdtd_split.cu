@@ -60,7 +60,7 @@ __device__ __forceinline__ double2 second(double2 a, double2 b, double2 c) { ret
   const long long P = v.P;                                      \
   const long long k = (long long)i * P + j;
 
-// ---- split-field TM (fdtdTM.c:277-309): calcH, then calcE, then the source on Ezx
+// ---- split-field TM (fdtdTM.c:290-327): calcH, then calcE, then the source on Ezx
 
 __global__ void split_tm_h(SplitView v)
 {
@@ -86,7 +86,7 @@ __global__ void split_tm_e(SplitView v)
   Ezy[k] = ezy;
 }
 
-// ---- split-field TE (fdtdTE.c:280-321): calcE, the source on Ey, then calcH
+// ---- split-field TE (fdtdTE.c:283-321): calcE, the source on Ey, then calcH
 
 __global__ void split_te_e(SplitView v)
 {
@@ -113,7 +113,7 @@ __global__ void split_te_h(SplitView v)
   Hz[k] = cadd2(hzx, hzy);
 }
 
-// ---- NS-FDTD TM (nsFdtdTM.c:66-150): calcH from Ez with the NS operator,
+// ---- NS-FDTD TM (nsFdtdTM.c:68-151): calcH from Ez with the NS operator,
 // calcE, the source on Ezy, then Ez = Ezx + Ezy
 
 __global__ void ns_tm_h(SplitView v)
@@ -141,7 +141,7 @@ __global__ void ns_tm_e(SplitView v)
   Ez[k] = cadd2(ezx, ezy);
 }
 
-// ---- NS-FDTD TE (nsFdtdTE.c:218-293): calcH, Hz = Hzx + Hzy, calcE with the
+// ---- NS-FDTD TE (nsFdtdTE.c:233-308): calcH, Hz = Hzx + Hzy, calcE with the
 // NS operator, then the sources on Ex (cos) and Ey (sin) of angle + 90 deg
 
 __global__ void ns_te_h(SplitView v)
@@ -179,19 +179,19 @@ void launch_split_step(const SplitView &v, int solver, cudaStream_t st)
   const dim3 b(32, 8);
   const dim3 g((unsigned)((v.n_py - 2 + 31) / 32), (unsigned)((v.n_px - 2 + 7) / 8));
   switch (solver) {
-  case 0:  // TM_2D: update() = calcH(); calcE(); source (fdtdTM.c:277-284)
+  case 0:  // TM_2D: update() = calcH(); calcE(); source (fdtdTM.c:290-297)
     split_tm_h<<<g, b, 0, st>>>(v);
     split_tm_e<<<g, b, 0, st>>>(v);
     break;
-  case 1:  // TE_2D: calcE(); source; calcH() (fdtdTE.c:280-285)
+  case 1:  // TE_2D: calcE(); source; calcH() (fdtdTE.c:283-288)
     split_te_e<<<g, b, 0, st>>>(v);
     split_te_h<<<g, b, 0, st>>>(v);
     break;
-  case 6:  // NS_TM_2D (nsFdtdTM.c:66-77)
+  case 6:  // NS_TM_2D (nsFdtdTM.c:68-80)
     ns_tm_h<<<g, b, 0, st>>>(v);
     ns_tm_e<<<g, b, 0, st>>>(v);
     break;
-  default:  // NS_TE_2D (nsFdtdTE.c:218-236)
+  default:  // NS_TE_2D (nsFdtdTE.c:233-252)
     ns_te_h<<<g, b, 0, st>>>(v);
     ns_te_e<<<g, b, 0, st>>>(v);
     break;
