@@ -18,6 +18,9 @@
  *   serial TE UPML        fdtdTE_upml.c:168-192, :252-412; ntffTE.c:57-157
  *   pulse source          field.c:224-256
  *   spectrum output       ntffTM.c:161-275, ntffTE.c:20-55,160-238, cfft.c:104-179
+ *   split-field PML       fdtdTM.c:167-242, :290-327; fdtdTE.c:170-238, :283-321
+ *   NS-FDTD               nsFdtdTM.c:68-151, :221-307; nsFdtdTE.c:90-181, :233-308;
+ *                         sources field.c:155-196
  *   frequency NTFF        ntffTM.c:72-158, ntffTE.c:242-338 (TE: global index
  *                         on all four sides, see of_frequency)
  *
@@ -55,6 +58,7 @@ typedef double complex cplx;
 
 struct of_sim {
   int solver, tm, mpi;
+  int family;                            /* 0 UPML, 1 split-field PML, 2 NS-FDTD */
   of_field_info fi;
   /* field.c:89-143 */
   int n_px, n_py, n_pml, n_x, n_y;
@@ -405,14 +409,18 @@ static void coefficients(of_sim *s)
     }
 }
 
+static void coefficients_split(of_sim *s);
+
 of_sim *of_create(int solver, const of_field_info *fi, const of_model *m)
 {
-  if (solver != OF_TM_UPML && solver != OF_TE_UPML && solver != OF_MPI_TM_UPML && solver != OF_MPI_TE_UPML)
+  if (solver != OF_TM_UPML && solver != OF_TE_UPML && solver != OF_MPI_TM_UPML && solver != OF_MPI_TE_UPML &&
+      solver != OF_TM_2D && solver != OF_TE_2D && solver != OF_NS_TM_2D && solver != OF_NS_TE_2D)
     return NULL;
   of_sim *s = (of_sim *)zalloc(sizeof(of_sim));
   s->solver = solver;
-  s->tm = (solver == OF_TM_UPML || solver == OF_MPI_TM_UPML);
+  s->tm = (solver == OF_TM_UPML || solver == OF_MPI_TM_UPML || solver == OF_TM_2D || solver == OF_NS_TM_2D);
   s->mpi = (solver == OF_MPI_TM_UPML || solver == OF_MPI_TE_UPML);
+  s->family = (solver == OF_TM_2D || solver == OF_TE_2D) ? 1 : (solver == OF_NS_TM_2D || solver == OF_NS_TE_2D) ? 2 : 0;
   s->fi = *fi;
   if (m) s->model = *m;
   field_setup(s);
@@ -425,6 +433,10 @@ of_sim *of_create(int solver, const of_field_info *fi, const of_model *m)
   for (int a = 0; a < 9; a++) s->f[a] = (cplx *)zalloc(sizeof(cplx) * s->ncell);
   for (int a = 0; a < 15; a++) s->c[a] = (double *)zalloc(sizeof(double) * s->ncell);
   for (int a = 0; a < 3; a++) s->eps[a] = (double *)zalloc(sizeof(double) * s->ncell);
+  if (s->family) {  /* no NTFF in these solvers */
+    coefficients_split(s);
+    return s;
+  }
   size_t nt = (size_t)360 * s->array_size + 2 * OF_GUARD;
   for (int a = 0; a < 3; a++) { s->nt_base[a] = (cplx *)zalloc(sizeof(cplx) * nt); s->nt[a] = s->nt_base[a] + OF_GUARD; }
   coefficients(s);
@@ -735,10 +747,229 @@ static void ntff_serial(of_sim *s)
   }
 }
 
+/* ------------------------------------------- split-field PML and NS-FDTD */
+/* fdtdTM.c, fdtdTE.c, nsFdtdTM.c, nsFdtdTE.c on the N_PX x N_PY frame.
+ * field slots: TM 0 Ez 1 Ezx 2 Ezy 3 Hx 4 Hy ; TE 0 Ex 1 Ey 2 Hz 3 Hzx 4 Hzy
+ * coefficients, as the reference names them:
+ *   TM 0 C_EZX 1 C_EZXLX 2 C_EZY 3 C_EZYLY 4 C_HX 5 C_HXLY 6 C_HY 7 C_HYLX
+ *   TE 0 C_EX 1 C_EXLY 2 C_EY 3 C_EYLX 4 C_HZX 5 C_HZXLX 6 C_HZY 7 C_HZYLY */
+
+static double pml_coef(double ep_mu, double sig) { return (1.0 - sig / ep_mu) / (1.0 + sig / ep_mu); } /* field.c:288-291 */
+static double pml_lxy(double ep_mu, double sig) { return 1.0 / (ep_mu + sig); }                      /* field.c:292-295 */
+static double ns_beta(double a) { return tanh(a) / (1 + pow(tanh(a), 2)); }                          /* nsFdtdTM.c:221-224 */
+static double ns_coef1(double a, double b) { return (1 - b) / (1 + b); }                              /* nsFdtdTM.c:226-229 */
+static double ns_u(const of_sim *s, double e)   /* sin(w/2) / sin(k n / 2), n = sqrt(eps) */
+{
+  double n = sqrt(e / OF_EPS0);
+  double k = s->k_s * n;
+  return sin(s->w_s * 0.5) / sin(k * 0.5);
+}
+
+static void coefficients_split(of_sim *s)
+{
+  const double R = 1.0e-8, M = 2.0;
+  double **c = s->c, **e = s->eps;
+  const int NX = s->n_px, NY = s->n_py;
+  if (s->solver == OF_TM_2D) {                        /* fdtdTM.c:167-242 */
+    const double sig_max = -(M + 1.0) * OF_EPS0 * OF_C / 2.0 / s->n_pml * log(R);
+    for (int i = 0; i < NX; i++)
+      for (int j = 0; j < NY; j++) {
+        int k = i * NY + j;
+        e[0][k] = meps(s, i, j, DXY_);
+        e[1][k] = meps(s, i, j + 0.5, DY_);
+        e[2][k] = meps(s, i + 0.5, j, DX_);
+        double sig_ez_x = sig_max * sigma_x(s, i), sig_ez_y = sig_max * sigma_y(s, j);
+        double sig_hx_y = sig_max * sigma_y(s, j + 0.5), sig_hx_yy = OF_MU0 / OF_EPS0 * sig_hx_y;
+        double sig_hy_x = sig_max * sigma_x(s, i + 0.5), sig_hy_xx = OF_MU0 / OF_EPS0 * sig_hy_x;
+        c[0][k] = pml_coef(e[0][k], sig_ez_x);
+        c[1][k] = pml_lxy(e[0][k], sig_ez_x);
+        c[2][k] = pml_coef(e[0][k], sig_ez_y);
+        c[3][k] = pml_lxy(e[0][k], sig_ez_y);
+        c[4][k] = pml_coef(OF_MU0, sig_hx_yy);
+        c[5][k] = pml_lxy(OF_MU0, sig_hx_yy);
+        c[6][k] = pml_coef(OF_MU0, sig_hy_xx);
+        c[7][k] = pml_lxy(OF_MU0, sig_hy_xx);
+      }
+  } else if (s->solver == OF_TE_2D) {                 /* fdtdTE.c:170-238 */
+    const double sig_max = -(M + 1.0) * OF_EPS0 * OF_C / 2.0 / s->n_pml * log(R);
+    for (int i = 0; i < NX; i++)
+      for (int j = 0; j < NY; j++) {
+        int k = i * NY + j;
+        e[0][k] = meps(s, i + 0.5, j, DY_);
+        e[1][k] = meps(s, i, j + 0.5, DX_);
+        e[2][k] = 0.5 * (meps(s, i + 0.5, j + 0.5, DX_) + meps(s, i + 0.5, j + 0.5, DY_));
+        double sig_ex_y = sig_max * sigma_y(s, j), sig_ey_x = sig_max * sigma_x(s, i);
+        double sig_hz_xx = OF_MU0 / OF_EPS0 * (sig_max * sigma_x(s, i + 0.5));
+        double sig_hz_yy = OF_MU0 / OF_EPS0 * (sig_max * sigma_y(s, j + 0.5));
+        c[0][k] = pml_coef(e[0][k], sig_ex_y);
+        c[1][k] = pml_lxy(e[0][k], sig_ex_y);
+        c[2][k] = pml_coef(e[1][k], sig_ey_x);
+        c[3][k] = pml_lxy(e[1][k], sig_ey_x);
+        c[4][k] = pml_coef(OF_MU0, sig_hz_xx);
+        c[5][k] = pml_lxy(OF_MU0, sig_hz_xx);
+        c[6][k] = pml_coef(OF_MU0, sig_hz_yy);
+        c[7][k] = pml_lxy(OF_MU0, sig_hz_yy);
+      }
+  } else if (s->solver == OF_NS_TM_2D) {              /* nsFdtdTM.c:231-307 */
+    const double sig_max = -(M + 1.0) * OF_EPS0 * OF_C / s->n_pml * log(R);
+    for (int i = 0; i < NX; i++)
+      for (int j = 0; j < NY; j++) {
+        int k = i * NY + j;
+        e[0][k] = meps(s, i, j, DXY_);
+        e[1][k] = meps(s, i, j + 0.5, DY_);
+        e[2][k] = meps(s, i + 0.5, j, DX_);
+        double sig_ez_x = sig_max * sigma_x(s, i), sig_ez_y = sig_max * sigma_y(s, j);
+        double sig_hx_y = sig_max * sigma_y(s, j + 0.5), sig_hy_x = sig_max * sigma_x(s, i + 0.5);
+        double a_hx_y = sig_hx_y / (2 * OF_EPS0), a_hy_x = sig_hy_x / (2 * OF_EPS0);
+        double a_ez_x = sig_ez_x / (2 * OF_EPS0), a_ez_y = sig_ez_y / (2 * OF_EPS0);
+        double b_hx_y = ns_beta(a_hx_y), b_hy_x = ns_beta(a_hy_x), b_ez_x = ns_beta(a_ez_x), b_ez_y = ns_beta(a_ez_y);
+        double z_ez = sqrt(OF_MU0 / e[0][k]), u_ez = ns_u(s, e[0][k]);
+        c[0][k] = ns_coef1(a_ez_x, b_ez_x);
+        c[1][k] = u_ez * z_ez / (1 + b_ez_x);
+        c[2][k] = ns_coef1(a_ez_y, b_ez_y);
+        c[3][k] = u_ez * z_ez / (1.0 + b_ez_x);        /* nsFdtdTM.c:287: b_ez_x, as written */
+        double z_hx = sqrt(OF_MU0 / e[1][k]), u_hx = ns_u(s, e[1][k]);
+        c[4][k] = ns_coef1(a_hx_y, b_hx_y);
+        c[5][k] = u_hx / z_hx / (1.0 + b_hx_y);
+        double z_hy = sqrt(OF_MU0 / e[2][k]), u_hy = ns_u(s, e[2][k]);
+        c[6][k] = ns_coef1(a_hy_x, b_hy_x);
+        c[7][k] = u_hy / z_hy / (1.0 + b_hy_x);
+      }
+  } else {                                            /* nsFdtdTE.c:100-181, inner cells only */
+    const double sig_max = -(M + 1.0) * OF_EPS0 * OF_C / s->n_pml * log(R);
+    for (int i = 1; i < NX - 1; i++)
+      for (int j = 1; j < NY - 1; j++) {
+        int k = i * NY + j;
+        e[0][k] = meps(s, i + 0.5, j, DY_);
+        e[1][k] = meps(s, i, j + 0.5, DX_);
+        e[2][k] = meps(s, i + 0.5, j + 0.5, DXY_);
+        double sig_ex_y = sig_max * sigma_y(s, j), sig_ey_x = sig_max * sigma_x(s, i);
+        double sig_hz_x = sig_max * sigma_x(s, i + 0.5), sig_hz_y = sig_max * sigma_y(s, j + 0.5);
+        double a_ex_y = sig_ex_y / (2 * e[0][k]), a_ey_x = sig_ey_x / (2 * e[1][k]);
+        double a_hz_x = sig_hz_x / (2 * e[2][k]), a_hz_y = sig_hz_y / (2 * e[2][k]);
+        double b_ex_y = ns_beta(a_ex_y), b_ey_x = ns_beta(a_ey_x), b_hz_x = ns_beta(a_hz_x), b_hz_y = ns_beta(a_hz_y);
+        double z_hz = sqrt(OF_MU0 / e[2][k]), u_hz = ns_u(s, e[2][k]);
+        c[4][k] = ns_coef1(a_hz_x, b_hz_x);
+        c[5][k] = u_hz / z_hz / (1.0 + b_hz_x);
+        c[6][k] = ns_coef1(a_hz_y, b_hz_y);
+        c[7][k] = u_hz / z_hz / (1.0 + b_hz_y);
+        double z_ex = sqrt(OF_MU0 / e[0][k]), u_ex = ns_u(s, e[0][k]);
+        c[0][k] = ns_coef1(a_ex_y, b_ex_y);
+        c[1][k] = u_ex * z_ex / (1.0 + b_ex_y);
+        double z_ey = sqrt(OF_MU0 / e[1][k]), u_ey = ns_u(s, e[1][k]);
+        c[2][k] = ns_coef1(a_ey_x, b_ey_x);
+        c[3][k] = u_ey * z_ey / (1.0 + b_ey_x);
+      }
+  }
+}
+
+/* field_scatteredWaveNotUPML (field.c:179-196) and field_nsScatteredWaveNotUPML
+ * (field.c:155-177): the CW source of the split-field / NS solvers on cells
+ * 1..N-2 of the global frame */
+static void wave_not_upml(of_sim *s, cplx *p, const double *eps, double gx, double gy)
+{
+  double rad = s->fi.angle_deg * M_PI / 180.0;
+  double ks_cos = cos(rad) * s->k_s, ks_sin = sin(rad) * s->k_s;
+  for (int i = 1; i < s->n_px - 1; i++)
+    for (int j = 1; j < s->n_py - 1; j++) {
+      int k = i * s->n_py + j;
+      double kr = (i + gx) * ks_cos + (j + gy) * ks_sin;
+      p[k] += s->ray_coef * (OF_EPS0 / eps[k] - 1.0) *
+              (cexp(I * (kr - s->w_s * (s->time + 0.5))) - cexp(I * (kr - s->w_s * (s->time - 0.5))));
+    }
+}
+static void ns_wave_not_upml(of_sim *s, cplx *p, const double *eps, double gx, double gy, double dot)
+{
+  double ray_coef = s->ray_coef * dot;
+  double rad = s->fi.angle_deg * M_PI / 180.0;
+  double ks_cos = cos(rad) * s->k_s, ks_sin = sin(rad) * s->k_s;
+  for (int i = 1; i < s->n_px - 1; i++)
+    for (int j = 1; j < s->n_py - 1; j++) {
+      int k = i * s->n_py + j;
+      double kr = (i + gx) * ks_cos + (j + gy) * ks_sin;
+      double n = sqrt(eps[k] / OF_EPS0);
+      double u0 = sin(s->w_s * 0.5) / sin(s->k_s * 0.5);
+      double u1 = sin(s->w_s * 0.5) / sin(n * s->k_s * 0.5);
+      double _n = u0 / u1;
+      p[k] += ray_coef * (1.0 / (_n * n) - 1.0) *
+              (cexp(I * (kr - s->w_s * (s->time + 1.0))) - cexp(I * (kr - s->w_s * (s->time))));
+    }
+}
+
+#define SPLIT_FOR for (int i = 1; i < s->n_px - 1; i++) for (int j = 1; j < s->n_py - 1; j++)
+
+static void update_split(of_sim *s)
+{
+  const int NY = s->n_py, dx = NY, dy = 1;
+  cplx **f = s->f;
+  double **c = s->c;
+  if (s->solver == OF_TM_2D) {                       /* fdtdTM.c:290-327 */
+    cplx *Ez = f[0], *Ezx = f[1], *Ezy = f[2], *Hx = f[3], *Hy = f[4];
+    SPLIT_FOR { int k = i * NY + j; Hx[k] = c[4][k] * Hx[k] - c[5][k] * (Ezx[k + 1] - Ezx[k] + Ezy[k + 1] - Ezy[k]); }
+    SPLIT_FOR { int k = i * NY + j; Hy[k] = c[6][k] * Hy[k] + c[7][k] * (Ezx[k + dx] - Ezx[k] + Ezy[k + dx] - Ezy[k]); }
+    SPLIT_FOR { int k = i * NY + j; Ezx[k] = c[0][k] * Ezx[k] + c[1][k] * (Hy[k] - Hy[k - dx]); }
+    SPLIT_FOR { int k = i * NY + j; Ezy[k] = c[2][k] * Ezy[k] - c[3][k] * (Hx[k] - Hx[k - 1]); }
+    SPLIT_FOR { int k = i * NY + j; Ez[k] = Ezx[k] + Ezy[k]; }
+    wave_not_upml(s, Ezx, s->eps[0], 0.0, 0.0);
+  } else if (s->solver == OF_TE_2D) {                /* fdtdTE.c:283-321 */
+    cplx *Ex = f[0], *Ey = f[1], *Hz = f[2], *Hzx = f[3], *Hzy = f[4];
+    SPLIT_FOR { int k = i * NY + j; Ex[k] = c[0][k] * Ex[k] + c[1][k] * (Hzx[k] - Hzx[k - 1] + Hzy[k] - Hzy[k - 1]); }
+    SPLIT_FOR { int k = i * NY + j; Ey[k] = c[2][k] * Ey[k] - c[3][k] * (Hzx[k] - Hzx[k - dx] + Hzy[k] - Hzy[k - dx]); }
+    wave_not_upml(s, Ey, s->eps[1], 0.0, 0.5);
+    SPLIT_FOR { int k = i * NY + j; Hzx[k] = c[4][k] * Hzx[k] - c[5][k] * (Ey[k + dx] - Ey[k]); }
+    SPLIT_FOR { int k = i * NY + j; Hzy[k] = c[6][k] * Hzy[k] + c[7][k] * (Ex[k + 1] - Ex[k]); }
+    SPLIT_FOR { int k = i * NY + j; Hz[k] = Hzx[k] + Hzy[k]; }
+  } else if (s->solver == OF_NS_TM_2D) {             /* nsFdtdTM.c:68-151 */
+    cplx *Ez = f[0], *Ezx = f[1], *Ezy = f[2], *Hx = f[3], *Hy = f[4];
+    double k_s = s->k_s;
+    double r = 1.0 / 6.0 + k_s * k_s / 180.0 - pow(k_s, 4) / 23040, r_2 = r / 2.0;
+    SPLIT_FOR {
+      int k = i * NY + j;
+      cplx ns = r_2 * ((Ez[k + dy + dx] + Ez[k + dy - dx] - 2 * Ez[k + dy]) - (Ez[k + dx] + Ez[k - dx] - 2 * Ez[k]));
+      Hx[k] = c[4][k] * Hx[k] - c[5][k] * (Ez[k + dy] - Ez[k] + ns);
+    }
+    SPLIT_FOR {
+      int k = i * NY + j;
+      cplx ns = r_2 * ((Ez[k + dx + dy] + Ez[k + dx - dy] - 2 * Ez[k + dx]) - (Ez[k + dy] + Ez[k - dy] - 2 * Ez[k]));
+      Hy[k] = c[6][k] * Hy[k] + c[7][k] * (Ez[k + dx] - Ez[k] + ns);
+    }
+    SPLIT_FOR { int k = i * NY + j; Ezx[k] = c[0][k] * Ezx[k] + c[1][k] * (Hy[k] - Hy[k - dx]); }
+    SPLIT_FOR { int k = i * NY + j; Ezy[k] = c[2][k] * Ezy[k] - c[3][k] * (Hx[k] - Hx[k - dy]); }
+    ns_wave_not_upml(s, Ezy, s->eps[0], 0, 0, 1.0);
+    SPLIT_FOR { int k = i * NY + j; Ez[k] = Ezx[k] + Ezy[k]; }
+  } else {                                           /* nsFdtdTE.c:233-308 */
+    cplx *Ex = f[0], *Ey = f[1], *Hz = f[2], *Hzx = f[3], *Hzy = f[4];
+    SPLIT_FOR { int k = i * NY + j; Hzx[k] = c[4][k] * Hzx[k] - c[5][k] * (Ey[k + dx] - Ey[k]); }
+    SPLIT_FOR { int k = i * NY + j; Hzy[k] = c[6][k] * Hzy[k] + c[7][k] * (Ex[k + dy] - Ex[k]); }
+    SPLIT_FOR { int k = i * NY + j; Hz[k] = Hzx[k] + Hzy[k]; }
+    double k_s = s->k_s;
+    double r = 1.0 / 6.0 + k_s * k_s / 180.0 - pow(k_s, 4) / 23040, r_2 = r / 2.0;
+    SPLIT_FOR {
+      int k = i * NY + j;
+      cplx ns = r_2 * ((Hz[k + dx] + Hz[k - dx] - 2 * Hz[k]) - (Hz[k - dy + dx] + Hz[k - dy - dx] - 2 * Hz[k - dy]));
+      Ex[k] = c[0][k] * Ex[k] + c[1][k] * (Hz[k] - Hz[k - dy] + ns);
+    }
+    SPLIT_FOR {
+      int k = i * NY + j;
+      cplx ns = r_2 * ((Hz[k + dy] + Hz[k - dy] - 2 * Hz[k]) - (Hz[k - dx + dy] + Hz[k - dx - dy] - 2 * Hz[k - dx]));
+      Ey[k] = c[2][k] * Ey[k] - c[3][k] * (Hz[k] - Hz[k - dx] + ns);
+    }
+    double co = cos((s->fi.angle_deg + 90) * M_PI / 180.0);
+    double si = sin((s->fi.angle_deg + 90) * M_PI / 180.0);
+    if (co != 0.0) ns_wave_not_upml(s, Ex, s->eps[0], 0, 0.5, co);
+    if (si != 0.0) ns_wave_not_upml(s, Ey, s->eps[1], 0, 0.5, si);
+  }
+}
+#undef SPLIT_FOR
+
 /* ------------------------------------------------------------------ step */
 
 static void update(of_sim *s)
 {
+  if (s->family) {
+    update_split(s);
+    return;
+  }
   if (s->mpi) {
     /* mpiTM_UPML.c:196-217 / mpiTE_UPML.c:290-304 (halo exchange is a no-op
      * for one rank; the halos stay zero) */
@@ -773,8 +1004,9 @@ void of_dims(const of_sim *s, int *nx, int *ny, int *n_px, int *n_py)
 { *nx = s->nx; *ny = s->ny; *n_px = s->n_px; *n_py = s->n_py; }
 double *of_field(of_sim *s, int which)
 {
-  static const int tm_slot[3] = {0, 3, 6}, te_slot[3] = {0, 1, 2};
+  static const int tm_slot[3] = {0, 3, 6}, te_slot[3] = {0, 1, 2}, split_tm_slot[3] = {0, 3, 4};
   if (which < 0 || which > 2) return NULL;
+  if (s->family) return (double *)s->f[s->tm ? split_tm_slot[which] : te_slot[which]];
   return (double *)s->f[s->tm ? tm_slot[which] : te_slot[which]];
 }
 double *of_eps(of_sim *s, int which) { return (which >= 0 && which < 3) ? s->eps[which] : NULL; }
@@ -785,7 +1017,7 @@ int of_ntff_info(const of_sim *s, int *top, int *bottom, int *left, int *right, 
 }
 int of_array_size(const of_sim *s) { return s->array_size; }
 int of_ntff_guard(void) { return OF_GUARD; }
-double *of_ntff(of_sim *s, int which) { return (which >= 0 && which < 3) ? (double *)s->nt_base[which] : NULL; }
+double *of_ntff(of_sim *s, int which) { return (which >= 0 && which < 3 && !s->family) ? (double *)s->nt_base[which] : NULL; }
 
 /* ------------------------------------------------------- spectrum output */
 
@@ -815,6 +1047,7 @@ static void fft_pos(cplx *a, int n)
 /* ntffTM.c:161-275 / ntffTE.c:20-55,160-238.  TM transforms E_theta, TE E_phi. */
 int of_time_output(of_sim *s, double *out)
 {
+  if (s->family) return -1;  /* no NTFF */
   const int maxTime = (int)s->max_time;
   if (maxTime > OF_NFFT) return -1;
   const double complex coef = 1.0 / (4 * M_PI * OF_C) * csqrt(2 * M_PI * OF_C / (I * s->w_s));
@@ -899,6 +1132,7 @@ static void frequency_te(const of_sim *s, const cplx *Ex, const cplx *Ey, const 
  * gathered to global x = i-1 first). */
 int of_frequency(of_sim *s, double *out)
 {
+  if (s->family) return -1;  /* no NTFF */
   const int NX = s->n_px, NY = s->n_py;
   cplx *g[3];
   for (int q = 0; q < 3; q++) {

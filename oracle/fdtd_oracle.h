@@ -14,8 +14,10 @@
 extern "C" {
 #endif
 
-/* Solver selection, numbered like enum SOLVER in simulator.h:8-18. */
-enum { OF_TM_UPML = 2, OF_TE_UPML = 3, OF_MPI_TM_UPML = 4, OF_MPI_TE_UPML = 5 };
+/* Solver selection, numbered like enum SOLVER in simulator.h:8-18 (0, 1, 6, 7:
+ * the split-field PML and NS-FDTD solvers, no NTFF). */
+enum { OF_TM_2D = 0, OF_TE_2D = 1, OF_TM_UPML = 2, OF_TE_UPML = 3, OF_MPI_TM_UPML = 4, OF_MPI_TE_UPML = 5,
+       OF_NS_TM_2D = 6, OF_NS_TE_2D = 7 };
 
 /* Models: the reference's noModel.c / circleModel.c / morphoScaleModel.c /
  * zigzagModel.c, plus

@@ -32,7 +32,6 @@ TM_UPML_2D, TE_UPML_2D, MPI_TM_UPML_2D, MPI_TE_UPML_2D = 2, 3, 4, 5
 TM_2D, TE_2D, NS_TM_2D, NS_TE_2D = 0, 1, 6, 7
 SOLVERS = {"TM_UPML": TM_UPML_2D, "TE_UPML": TE_UPML_2D,
            "MPI_TM_UPML": MPI_TM_UPML_2D, "MPI_TE_UPML": MPI_TE_UPML_2D,
-           # run by RefSim only (the C restatement covers the UPML solvers)
            "TM_2D": TM_2D, "TE_2D": TE_2D, "NS_TM_2D": NS_TM_2D, "NS_TE_2D": NS_TE_2D}
 MODEL_NONE, MODEL_CIRCLE, MODEL_MORPHO, MODEL_DISCS, MODEL_ZIGZAG = 0, 1, 2, 3, 4
 NFFT = 8192

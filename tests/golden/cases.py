@@ -44,18 +44,17 @@ CASES = {
     "ser_te_circle": dict(solver="TE_UPML", fi=(300, 300, 5, 8, 100, 20, 700),
                           model=("circle", 60, 0.0), steps=700, kind="full", rows="few",
                           extras=("spectrum",)),
-    # The split-field PML and NS-FDTD solvers (no NTFF; pinned to the reference
-    # directly, the C restatement covers the UPML path only: ref_only).
+    # The split-field PML and NS-FDTD solvers (they have no NTFF: no_ntff).
     "split_tm_circle": dict(solver="TM_2D", fi=(300, 320, 5, 10, 100, 0, 200),
-                            model=("circle", 60, 0.0), steps=200, kind="full", ref_only=True, extras=("elliptic",)),
+                            model=("circle", 60, 0.0), steps=200, kind="full", no_ntff=True, extras=("elliptic",)),
     "split_te_circle_30deg": dict(solver="TE_2D", fi=(320, 300, 5, 10, 100, 30, 200),
-                                  model=("circle", 60, 2.25), steps=200, kind="full", ref_only=True,
+                                  model=("circle", 60, 2.25), steps=200, kind="full", no_ntff=True,
                                   extras=("elliptic",)),
     "ns_tm_morpho": dict(solver="NS_TM_2D", fi=(330, 340, 5, 10, 90, 0, 180),
-                         model=("morpho", 150, 20, 25, 3, 10, 0.5, 0.0), steps=180, kind="full", ref_only=True,
+                         model=("morpho", 150, 20, 25, 3, 10, 0.5, 0.0), steps=180, kind="full", no_ntff=True,
                          extras=("elliptic",)),
     "ns_te_circle_20deg": dict(solver="NS_TE_2D", fi=(300, 320, 5, 10, 100, 20, 200),
-                               model=("circle", 60, 0.0), steps=200, kind="full", ref_only=True,
+                               model=("circle", 60, 0.0), steps=200, kind="full", no_ntff=True,
                                extras=("elliptic",)),
     # The 1044^2 Mie grid (r 500 nm, eps 2.25 override) for the first 40 of 4000 steps.
     "mpi_tm_c2_head": dict(solver="MPI_TM_UPML", fi=(5220, 5220, 5, 10, 500, 0, 4000),

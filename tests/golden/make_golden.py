@@ -59,7 +59,7 @@ def run_case(name, c):
     mpi = c["solver"].startswith("MPI")
     fields = [crop(sim.field(w), mpi) for w in range(3)]
     eps = [crop(sim.eps(w), mpi) for w in range(3)]
-    ntff = [] if c.get("ref_only") else [sim.ntff(w) for w in range(3)]   # split-field / NS: no NTFF
+    ntff = [] if c.get("no_ntff") else [sim.ntff(w) for w in range(3)]   # split-field / NS: no NTFF
     out = capture(fields, eps, ntff, sim.array_size, c["kind"], c.get("rows", "all"))
     extras = c.get("extras", ())
     if "spectrum" in extras:

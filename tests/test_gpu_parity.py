@@ -39,7 +39,7 @@ def run_gpu(name, precision="f64"):
     sim.run(c["steps"])
     fields = [sim.field(w) for w in range(3)]
     eps = [sim.eps(w) for w in range(3)]
-    ntff = [] if c.get("ref_only") else [sim.ntff(w) for w in range(3)]   # split-field / NS: no NTFF
+    ntff = [] if c.get("no_ntff") else [sim.ntff(w) for w in range(3)]   # split-field / NS: no NTFF
     out = capture(fields, eps, ntff, sim.array_size, c["kind"], c.get("rows", "all"))
     extras = c.get("extras", ())
     if "spectrum" in extras:

@@ -23,7 +23,7 @@ def run_oracle(name):
     mpi = c["solver"].startswith("MPI")
     fields = [crop(sim.field(w), mpi) for w in range(3)]
     eps = [crop(sim.eps(w), mpi) for w in range(3)]
-    ntff = [sim.ntff(w) for w in range(3)]
+    ntff = [] if c.get("no_ntff") else [sim.ntff(w) for w in range(3)]   # split-field / NS solvers
     out = capture(fields, eps, ntff, sim.array_size, c["kind"], c.get("rows", "all"))
     extras = c.get("extras", ())
     if "spectrum" in extras:
@@ -34,7 +34,7 @@ def run_oracle(name):
     return sim, out
 
 
-@pytest.mark.parametrize("name", sorted(n for n, c in CASES.items() if not c.get("ref_only")))
+@pytest.mark.parametrize("name", sorted(CASES))
 def test_oracle_matches_reference_golden(oracle_built, name):
     ref = dict(np.load(GOLDEN / f"{name}.npz"))
     sim, got = run_oracle(name)
