@@ -249,7 +249,9 @@ static int batch_cols(const fdtd_batch *b) { return b->cols == 2 && b->f32 && (b
 static int batch_rows(const fdtd_batch *b, const fdtd_sim *s)
 {
   if (b->L > 0) return b->L;
-  return std::max(16, std::min(48, s->ni / 4 + 1));  // 48: fastest on the 256-cylinder sweep
+  // 96: fastest on the 256-cylinder sweep (236^2..643^2) once the tiles prefetch
+  // their rows (32: 242, 48: 259, 64: 266, 96: 271 structures/s)
+  return std::max(16, std::min(96, s->ni));
 }
 
 // Instance descriptors from the current field sets (fdtd_batch_run swaps an

@@ -2,7 +2,7 @@
 
     python -m mpifdtd_gb300.profile_case tblock --grid 4096 --k 4 --rows 128 --steps 16 [--precision f32]
     python -m mpifdtd_gb300.profile_case gemm --m 8192 --n 8192 --kdim 8192
-    python -m mpifdtd_gb300.profile_case sweep --structures 64 [--k 4 --cols 1]
+    python -m mpifdtd_gb300.profile_case sweep --structures 64 [--k 4 --cols 1 --batch-rows 0]
     python -m mpifdtd_gb300.profile_case all ...    (tblock and gemm, the blocked case first)
 
 tblock: the morpho ridge on a (grid + 32)^2 MPI_TM_UPML grid with temporal
@@ -74,8 +74,9 @@ def sweep(a):
     from mpifdtd_gb300.sweep import mie_sweep, run_batch
     cases = mie_sweep(a.structures)
     cell_steps = sum(c.cells * c.fi.step_num for c in cases)
-    _, t, _, launches = run_batch(cases, "f32", tblock=a.k, cols=a.cols)
-    print(json.dumps({"case": "sweep", "structures": a.structures, "k": a.k, "cols": a.cols, "seconds": t,
+    _, t, _, launches = run_batch(cases, "f32", tblock=a.k, cols=a.cols, rows=a.batch_rows)
+    print(json.dumps({"case": "sweep", "structures": a.structures, "k": a.k, "cols": a.cols, "rows": a.batch_rows,
+                      "seconds": t,
                       "structures_per_s": a.structures / t, "gcell_per_s": cell_steps / t / 1e9, "launches": launches}),
           flush=True)
 
@@ -85,6 +86,7 @@ def main(argv=None):
     ap.add_argument("case", choices=["tblock", "gemm", "sweep", "all"])
     ap.add_argument("--structures", type=int, default=64)
     ap.add_argument("--cols", type=int, default=1)
+    ap.add_argument("--batch-rows", type=int, default=0, help="sweep: tile rows (0: the engine's choice)")
     ap.add_argument("--grid", type=int, default=4096)
     ap.add_argument("--k", type=int, default=4)
     ap.add_argument("--rows", type=int, default=128)

@@ -21,7 +21,8 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from .engine import MODEL_CIRCLE, OPT_NTFF_MODE, OPT_TBLOCK, OPT_TBLOCK_COLS, Batch, FieldInfo, Simulation
+from .engine import (MODEL_CIRCLE, OPT_NTFF_MODE, OPT_TBLOCK, OPT_TBLOCK_COLS, OPT_TBLOCK_ROWS, Batch, FieldInfo,
+                     Simulation)
 
 H_U = 5
 PML = 10
@@ -56,14 +57,17 @@ def mie_sweep(n: int = 256, seed: int = 20261203 + 2, periods: float = 12.0):
     return cases
 
 
-def run_batch(cases, precision="f32", tblock=4, cols=1):
-    """All cases in one batched engine; returns (far fields [n, 360] complex,
-    stepping seconds, end-to-end seconds, kernel launches)."""
+def run_batch(cases, precision="f32", tblock=4, cols=1, rows=0):
+    """All cases in one batched engine (rows: tile height, 0 = the engine's
+    choice per instance); returns (far fields [n, 360] complex, stepping
+    seconds, end-to-end seconds, kernel launches)."""
     t0 = time.perf_counter()
     b = Batch("MPI_TM_UPML", [c.fi for c in cases], precision)
     b.set_option(OPT_TBLOCK, tblock)
     if cols != 1:
         b.set_option(OPT_TBLOCK_COLS, cols)
+    if rows:
+        b.set_option(OPT_TBLOCK_ROWS, rows)
     for s, c in zip(b.instances, cases):
         s.fill_model(MODEL_CIRCLE, [c.radius_nm, c.eps])
     for s in b.instances:
