@@ -6,7 +6,10 @@
  * mpiTM_UPML.c / mpiTE_UPML.c (and of the serial fdtdTM_upml.c /
  * fdtdTE_upml.c), the scattered-field sources of field.c, and the
  * time-domain near-to-far-field (NTFF) accumulation into the flat
- * [360][arraySize] U/W arrays.  Plain C types only: no CUDA or torch types.
+ * [360][arraySize] U/W arrays; besides those, the split-field PML and
+ * non-standard FDTD solvers (fdtdTM.c, fdtdTE.c, nsFdtdTM.c, nsFdtdTE.c),
+ * batched sweeps, the running-DFT NTFF and the reference's file outputs.
+ * Plain C types only: no CUDA or torch types.
  *
  * The reference's own entry points (mpi_fdtdTM_upml_getUpdate() ... ) are
  * provided on top of this ABI by libmpifdtd_upml.so, see mpifdtd_upml.h.
