@@ -1,4 +1,5 @@
-"""Mie series of a dielectric circular cylinder: the known-answer far field.
+"""Mie series of a dielectric circular cylinder: the known-answer far field
+and near-field ring.
 
 TEST INFRASTRUCTURE (the oracle's physics check).  The CW path of the
 reference (scatteredWave, mpiTM_UPML.c:337-374 / mpiTE_UPML.c:250-281, and
@@ -65,3 +66,29 @@ def pattern_error(intensity: np.ndarray, reference: np.ndarray) -> tuple[float, 
     reference = np.asarray(reference, dtype=float)
     s = float(intensity @ reference / (reference @ reference))
     return float(np.linalg.norm(intensity - s * reference) / np.linalg.norm(intensity)), s
+
+
+def near_field_ring(radius: float, wavelength: float, eps: float, pol: str, ring_radius: float,
+                    angles_deg=None) -> np.ndarray:
+    """|E|^2 of the scattered field on a circle about the cylinder's axis
+    (same length unit throughout): the axial E_z (TM) or, for H polarisation
+    with the plane wave along +x, E_y obtained from H_z = sum i^n b_n H_n(kr)
+    e^{in phi} through E_y ~ (1/k) dH_z/dx (unit incident E_y):
+
+      TM: |sum_n i^n b_n H_n(kr) e^{in phi}|^2
+      TE: |sum_n i^n b_n (cos(phi) H_n'(kr) - i n sin(phi) H_n(kr) / (kr)) e^{in phi}|^2
+
+    The default angles are those of field_outputElliptic's ring (field.c:322-343),
+    180 down to 0 degrees, i.e. entry q is the angle 180 - q."""
+    from scipy.special import h1vp, hankel1
+    if angles_deg is None:
+        angles_deg = np.arange(180, -1, -1)
+    phi = np.deg2rad(np.asarray(angles_deg, dtype=float))[:, None]
+    n, b = coefficients(2.0 * np.pi * radius / wavelength, float(np.sqrt(eps)), pol)
+    kr = 2.0 * np.pi * ring_radius / wavelength
+    H = hankel1(n, kr)[None, :]
+    w = ((1j ** n) * b)[None, :] * np.exp(1j * phi * n[None, :])
+    if pol == "TM":
+        return np.abs((w * H).sum(axis=1)) ** 2
+    Hp = h1vp(n, kr)[None, :]
+    return np.abs((w * (np.cos(phi) * Hp - 1j * n[None, :] * np.sin(phi) / kr * H)).sum(axis=1)) ** 2

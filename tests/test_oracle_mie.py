@@ -1,5 +1,6 @@
-"""Known-answer physics check of the oracle's CW path: the far field of a
-dielectric cylinder against the Mie series (oracle/mie.py).
+"""Known-answer physics check of the oracle's CW path: the far field and the
+1.2-lambda near-field ring of a dielectric cylinder against the Mie series
+(oracle/mie.py).
 
 The MPI UPML solvers (scatteredWave source, mpiTM_UPML.c:337-374 /
 mpiTE_UPML.c:250-281) run a cylinder to steady state and the frequency-domain
@@ -43,3 +44,22 @@ def test_oracle_far_field_matches_mie_series(solver, pol):
     err, _ = mie.pattern_error(inten, ref)
     assert err < 0.02, err
     assert abs(int(np.argmax(inten)) - 180) <= 2   # forward scattering of the +x plane wave
+
+
+@pytest.mark.parametrize("solver,pol", [("TM_2D", "TM"), ("NS_TM_2D", "TM"), ("TE_2D", "TE"), ("NS_TE_2D", "TE"),
+                                        ("MPI_TM_UPML", "TM")])
+def test_oracle_elliptic_ring_matches_mie_near_field(solver, pol):
+    """field_outputElliptic's ring (|E|^2 of the scattered field at 1.2 lambda,
+    Ez for TM, Ey for TE) of every solver family against the series, in
+    absolute amplitude: r = 150 nm, eps = 2.25, lambda = 300 nm, 1000 steps."""
+    from oracle import outputs
+    r, lam, eps = 150, 300, 2.25
+    sim = po.OracleSim(solver, po.FieldInfo(1200, 1200, 5, 10, lam, 0, 1000), po.Model.circle(r, eps))
+    sim.step(1000)
+    f = sim.field(0 if pol == "TM" else 1)
+    if sim.mpi:
+        f = f[1:-1, 1:-1]
+    ring = outputs.elliptic_ring(f, lam / 5)
+    ref = mie.near_field_ring(r, lam, eps, pol, 1.2 * lam)
+    err = float(np.linalg.norm(ring - ref) / np.linalg.norm(ref))
+    assert err < (0.02 if pol == "TM" else 0.04), err
