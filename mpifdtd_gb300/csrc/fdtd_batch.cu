@@ -8,12 +8,14 @@
 // batch adds each instance's spare field set, a device clock, and two packed
 // work-lists of (instance, strip, segment) tiles over all instances -- the
 // PML-free interior tiles and the others -- for the temporally blocked tile
-// code (tblock_tile.cuh).  One K-step block is four launches:
+// code (tblock_tile.cuh), each sorted by tile height (largest first).  One
+// K-step block is four launches:
 //   source  : ray_coef e^{-i w t} of every instance at the block's K times
-//   interior: persistent kernel striding over the interior work-list
-//   general : persistent kernel striding over the other tiles (on a second
-//             stream forked and joined inside the graph: runs beside interior)
-//   clock   : t += K, set parity flips
+//   interior: persistent kernel whose warps claim interior tiles one by one
+//             (an atomic counter in the clock record)
+//   general : the same over the other tiles (on a second stream forked and
+//             joined inside the graph: runs beside interior)
+//   clock   : t += K, set parity flips, tile counters reset
 // captured once in a CUDA graph and replayed until the instance with the
 // largest step_num has finished.  An instance whose step_num ends inside a
 // block freezes its remaining levels; a finished one is skipped, so its
