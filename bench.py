@@ -262,6 +262,7 @@ def run_gpu_arm(args):
     with ClockSampler(dev) as clk:
         e0.record(stream)
         sim.run(args.steps)
+        sim.flush()                     # the NTFF deposit of every timed step lands before e1
         e1.record(stream)
         e1.synchronize()
     torch.cuda.synchronize()
@@ -338,6 +339,7 @@ def run_variants(m, args, torch, cells, ms_f64):
     torch.cuda.synchronize()
     e0.record(stream)
     sim.run(args.steps)
+    sim.flush()
     e1.record(stream)
     e1.synchronize()
     ms = e0.elapsed_time(e1) / args.steps

@@ -128,6 +128,14 @@ int fdtd_run(fdtd_sim *sim, int n_steps);
 int fdtd_get_time(const fdtd_sim *sim, double *time);
 int fdtd_set_time(fdtd_sim *sim, double time);
 int fdtd_synchronize(fdtd_sim *sim);
+/* Enqueues the deposit of every buffered NTFF step (NTFF mode 2) on the
+ * engine's stream and returns without waiting: after it, work recorded on
+ * that stream (a CUDA event, a copy) follows the complete time-domain NTFF of
+ * every step taken so far.  The reference deposits inside each update()
+ * (mpiTM_UPML.c:196-217); the engine buffers up to FDTD_OPT_NTFF_BLOCK steps
+ * and deposits them together, so a timer that stops between steps calls this
+ * first.  A no-op when nothing is buffered. */
+int fdtd_flush(fdtd_sim *sim);
 
 /* Copy-out.  Sizes in complex elements: GLOBAL n_px*n_py, SOLVER
  * (n_px+2)*(n_py+2) for MPI solvers, n_px*n_py for serial ones. */

@@ -822,11 +822,15 @@ static void enqueue_step(fdtd_sim *s, double time, double ray_coef)
   if (s->profiling) s->prof_steps++;
 }
 
-// Deposits the buffered steps of the time-blocked NTFF (mode 2).
+// Deposits the buffered steps of the time-blocked NTFF (mode 2).  Under
+// profiling the deposit is one more 5-event group whose first four events
+// coincide, so fdtd_profile_read counts it as NTFF deposit time of no step.
 static int flush_ntff(fdtd_sim *s)
 {
   if (s->nb_pending == 0) return FDTD_OK;
+  for (int q = 0; q < 4; q++) mark(s);
   deposit_pending(s, ntff_view(s), s->stream);
+  mark(s);
   CK(cudaGetLastError());
   return FDTD_OK;
 }
@@ -1413,6 +1417,12 @@ extern "C" int fdtd_set_time(fdtd_sim *s, double t)
   s->time = t;
   s->ray_coef = t == 0 ? 0.0 : 1.0 - exp(-pow(0.01 * t, 2));
   return FDTD_OK;
+}
+
+extern "C" int fdtd_flush(fdtd_sim *s)
+{
+  if (!s) return fail(FDTD_E_ARG, "null simulation");
+  return flush_ntff(s);
 }
 
 extern "C" int fdtd_synchronize(fdtd_sim *s)

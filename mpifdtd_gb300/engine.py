@@ -92,6 +92,7 @@ def load():
         "fdtd_get_time": (I, [P, dp]),
         "fdtd_set_time": (I, [P, D]),
         "fdtd_synchronize": (I, [P]),
+        "fdtd_flush": (I, [P]),
         "fdtd_get_field": (I, [P, I, I, dp]),
         "fdtd_get_eps": (I, [P, I, I, dp]),
         "fdtd_get_ntff": (I, [P, I, dp]),
@@ -372,6 +373,10 @@ class Simulation:
 
     def synchronize(self):
         _check(self.lib.fdtd_synchronize(self.h))
+
+    def flush(self):
+        """Enqueue the deposit of the buffered NTFF steps (fdtd_flush); no wait."""
+        _check(self.lib.fdtd_flush(self.h))
 
     def reset(self):
         _check(self.lib.fdtd_reset(self.h))

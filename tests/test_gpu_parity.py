@@ -262,3 +262,30 @@ def test_gpu_split_and_ns_solvers_refuse_ntff_and_fp32():
             call()
     ez, ezx, ezy = sim.field(0), sim.field(3), sim.field(4)
     np.testing.assert_array_equal(ez, ezx + ezy)            # nsFdtdTM.c:73-76: Ez = Ezx + Ezy
+
+
+def test_gpu_flush_deposits_a_run_shorter_than_the_ntff_block():
+    """A run of fewer steps than the time-blocked NTFF buffer (32 steps)
+    leaves its deposit pending; fdtd_flush enqueues it on the engine stream,
+    the profiler counts it as NTFF deposit time, and the accumulators then
+    hold every step (mpiTM_UPML.c:196-217 deposits inside each update())."""
+    m = _engine()
+    fi = m.FieldInfo(300, 320, 5, 6, 100, 0, 150)
+    eps = _eps_for("mpi_tm_circle", CASES["mpi_tm_circle"])
+    a = m.Simulation("MPI_TM_UPML", fi)
+    b = m.Simulation("MPI_TM_UPML", fi)
+    for s in (a, b):
+        s.set_eps(*eps)
+        s.run(40)                       # past the source ramp: the path carries field
+        s.synchronize()
+    a.profile(True)
+    a.run(20)
+    a.flush()
+    prof = a.profile_read()
+    a.profile(False)
+    assert prof["steps"] == 20
+    assert prof["ntff_deposit"] > 0
+    b.set_option(m.OPT_NTFF_MODE, 0)    # direct per-step deposit as the reference does
+    b.run(20)
+    for w in range(3):
+        assert rel(a.ntff(w), b.ntff(w)) <= 1e-12
