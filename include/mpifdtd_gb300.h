@@ -290,9 +290,17 @@ long long fdtd_launch_count(const fdtd_sim *sim);
  * library until the process exits); a larger path is rejected with
  * FDTD_E_ARG.  The first call on a device looks the array up and uploads the
  * 360 direction cosines, so make that first call before any stream capture.
- * Every call reuses the same array (each call overwrites all of it before
- * reading), so calls that overlap on the GPU -- on different streams, or from
- * several host threads -- race; order them on one stream.
+ * The set-up belongs to the device's CUDA context: after a cudaDeviceReset
+ * the next call finds a new context and sets up again (it asks the driver
+ * for the context's id, cuCtxGetId; a driver without it keeps the first
+ * set-up, and calls after a reset then fail or use stale tables).
+ * Every call reuses the same array (each call writes the 2 x path entries it
+ * reads before reading them), so calls that overlap on the GPU -- on
+ * different streams, or from several host threads -- race; order them on
+ * one stream.  A tap whose flat index falls outside the block and its guard
+ * cells is skipped without an error: with time in [0, step_num-1] and
+ * accumulators sized as below none does, so a skip means the accumulators
+ * do not match cfg.
  *
  * args->e0/e1/h0/h1: device FP64 complex fields in the one-rank layout of the
  *   MPI solvers: row i, column j at (i*pitch + j), i in [0, N_PX+2), global

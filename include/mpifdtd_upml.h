@@ -12,8 +12,7 @@
  * reference solvers read them, so the host keeps owning time (field_nextStep
  * after update(), simulator.c:247-251) and the permittivity callback.
  *
- * Semantics per entry point (differences from the reference are listed in
- * INTEGRATION.md):
+ * Semantics per entry point:
  *   init()   allocates the device state, fills the permittivity through
  *            models_eps() at the solver's staggered points and modes
  *   update() one time step on the GPU at field_getTime()/field_getRayCoef()
@@ -23,6 +22,12 @@
  *   finish() releases everything (serial solvers write the spectrum first)
  *   get*()   borrowed host pointers in the reference solver's own layout,
  *            refreshed from the device on each call after an update()
+ * Differences from the reference: finish() of the MPI solvers does not run
+ * ntff*_FrequencySplit or MPI_Finalize (fdtd_frequency gives the frequency
+ * far field); update() at a time outside [0, stepNum-1] is refused, since the
+ * reference's flat NTFF index leaves its allocation there; errors print and
+ * exit(2) as the reference does, or, after mpifdtd_upml_set_error_mode(1),
+ * are stored for mpifdtd_upml_last_status() instead.
  * This header is C only (double complex), like the reference's headers.
  */
 #ifndef MPIFDTD_UPML_H

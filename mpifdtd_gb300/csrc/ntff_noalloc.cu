@@ -8,6 +8,7 @@
 // with IEEE-rounded operations in the reference's order (bit-identical to the
 // engine's host-built shift table), and the path samples live in a file-scope
 // __device__ array instead of engine-allocated memory.
+#include <cuda.h>  // CUcontext / CUresult types only: the two driver calls are looked up at run time
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -19,8 +20,8 @@ namespace fdtd {
 namespace {
 
 // Scratch: the signed, scaled E and H samples of every path cell of one step
-// ([0, ncell) E, [ncell, 2 ncell) H).  Every call overwrites the entries it
-// reads, so nothing has to be cleared between calls.
+// ([0, ncell) E, [ncell, 2 ncell) H).  Every call writes the 2 ncell entries
+// it reads before reading them, so nothing has to be cleared between calls.
 __device__ __align__(256) double2 g_noalloc_samples[2 * FDTD_NOALLOC_MAX_PATH];
 // (cos, sin) of each of the 360 observation angles, from the host libm
 // (mpiTM_UPML.c:875-876), uploaded once per device.
@@ -129,6 +130,38 @@ std::mutex g_setup_mutex;
 constexpr int kMaxDevices = 64;
 double2 *g_scratch_addr[kMaxDevices];  // device address of g_noalloc_samples per device
 bool g_ready[kMaxDevices];
+unsigned long long g_ctx_id[kMaxDevices];  // the context the set-up was made in (0: unknown)
+
+// Unique id of the calling thread's current CUDA context (cuCtxGetId), or 0
+// when the driver does not offer it.  A cudaDeviceReset destroys the primary
+// context, with it the module's __device__ / __constant__ storage; the next
+// context has another id, which tells the set-up to run again.
+unsigned long long current_context_id()
+{
+  using GetCurrent = CUresult (*)(CUcontext *);
+  using GetId = CUresult (*)(CUcontext, unsigned long long *);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {  // under g_setup_mutex
+    void *f0 = nullptr, *f1 = nullptr;
+    cudaDriverEntryPointQueryResult q0, q1;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0) == cudaSuccess &&
+        q0 == cudaDriverEntryPointSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+        q1 == cudaDriverEntryPointSuccess) {
+      get_current = (GetCurrent)f0;
+      get_id = (GetId)f1;
+    }
+    cudaGetLastError();
+    looked_up = true;
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
 
 }  // namespace
 }  // namespace fdtd
@@ -179,7 +212,9 @@ extern "C" int fdtd_ntff_step_noalloc(const fdtd_ntff_step_args *a, void *stream
   double2 *scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_ready[dev]) {  // once per device, with that device current
+    const unsigned long long ctx = current_context_id();
+    if (g_ready[dev] && ctx != 0 && ctx != g_ctx_id[dev]) g_ready[dev] = false;  // a new context: set up again
+    if (!g_ready[dev]) {  // once per device context, with that device current
       void *addr = nullptr;
       e = cudaGetSymbolAddress(&addr, g_noalloc_samples);
       if (e != cudaSuccess) return set_error(FDTD_E_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
@@ -191,6 +226,7 @@ extern "C" int fdtd_ntff_step_noalloc(const fdtd_ntff_step_args *a, void *stream
       e = cudaMemcpyToSymbol(g_noalloc_dir, dir, sizeof dir);
       if (e != cudaSuccess) return set_error(FDTD_E_CUDA, "cudaMemcpyToSymbol: %s", cudaGetErrorString(e));
       g_scratch_addr[dev] = (double2 *)addr;
+      g_ctx_id[dev] = ctx;
       g_ready[dev] = true;
     }
     scratch = g_scratch_addr[dev];

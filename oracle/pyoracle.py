@@ -25,7 +25,21 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ORACLE_SO = HERE / "_build" / "libfdtd_oracle.so"
 REF_SO = HERE / "_ref" / "libfdtdref.so"
-REF_SRC = Path(os.environ.get("MPIFDTD_REFERENCE", "/root/reference"))
+
+
+def _reference_dir() -> Path:
+    """Where the reference's sources are read from: $MPIFDTD_REFERENCE, else
+    the REF default of the recipe that compiles them (oracle/ref.mk)."""
+    env = os.environ.get("MPIFDTD_REFERENCE")
+    if env:
+        return Path(env)
+    for line in (HERE / "ref.mk").read_text().splitlines():
+        if line.startswith("REF") and "?=" in line:
+            return Path(line.split("?=", 1)[1].strip())
+    return HERE / "_ref" / "src"   # a directory that does not exist: reference absent
+
+
+REF_SRC = _reference_dir()
 
 # simulator.h:8-18
 TM_UPML_2D, TE_UPML_2D, MPI_TM_UPML_2D, MPI_TE_UPML_2D = 2, 3, 4, 5

@@ -3,7 +3,7 @@
     python tests/golden/make_golden.py [case ...]
 
 Builds oracle/_ref/libfdtdref.so from the reference sources (oracle/ref.mk;
-they must be present, default /root/reference or $MPIFDTD_REFERENCE), runs
+they must be present: $MPIFDTD_REFERENCE, else the recipe's REF), runs
 every case of cases.py through the reference exactly as simulator.c drives it,
 and writes tests/golden/<case>.npz.  The fixtures are committed; this script
 is how they were made.

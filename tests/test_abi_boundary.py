@@ -133,7 +133,7 @@ def test_dropin_without_gpu_reports_and_returns(libs):
     assert u.mpifdtd_upml_last_status() == 2   # FDTD_E_CUDA: no device, no CPU path
 
 
-REF = Path(os.environ.get("MPIFDTD_REFERENCE", "/root/reference"))
+REF = __import__("oracle.pyoracle", fromlist=["REF_SRC"]).REF_SRC   # $MPIFDTD_REFERENCE or ref.mk's REF
 REF_HOST_SOURCES = ["main.c", "simulator.c", "field.c", "models.c", "noModel.c", "circleModel.c",
                     "morphoScaleModel.c", "multiLayerModel.c", "zigzagModel.c", "traceImageModel.c",
                     "concentricCircleModel.c", "ntffTM.c",

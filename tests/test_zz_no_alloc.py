@@ -44,23 +44,44 @@ def _device_field(lib, sim, which):
     return p.value, pitch.value
 
 
-@pytest.mark.parametrize("solver", ["MPI_TM_UPML", "MPI_TE_UPML"])
-def test_noalloc_ntff_step_matches_engine(solver):
+CANARY = 64      # complex elements past each guard that no call may touch
+# an FP64 NaN payload no arithmetic produces: a write over it shows as a changed bit pattern
+CANARY_BITS = np.uint64(0x7FF4DEADBEEFCAFE)
+
+CASES = {
+    # solver, FieldInfo (width, height, h_u, pml, lambda, angle, step_num), circle radius (nm), warm-up steps
+    "tm_small": ("MPI_TM_UPML", (300, 320, 5, 6, 100, 0, 150), 60.0, 60),
+    "te_small": ("MPI_TE_UPML", (300, 320, 5, 6, 100, 0, 150), 60.0, 60),
+    # 100 x 32700 cells: a path of 65 480 cells, just under the 65 536 the static scratch holds
+    "tm_path_near_cap": ("MPI_TM_UPML", (500, 163500, 5, 10, 100, 0, 200), 150.0, 30),
+}
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_noalloc_ntff_step_matches_engine(case):
     import torch
 
     import mpifdtd_gb300 as m
 
+    solver, fi_t, radius, warm = CASES[case]
     lib = m.load()
     lib.fdtd_ntff_step_noalloc.restype = C.c_int
     lib.fdtd_ntff_step_noalloc.argtypes = [C.POINTER(_StepArgs), C.c_void_p]
-    fi = m.FieldInfo(300, 320, 5, 6, 100, 0, 150)
+    fi = m.FieldInfo(*fi_t)
     sim = m.Simulation(solver, fi)
-    sim.fill_model(m.MODEL_CIRCLE, [60.0, 0.0])
-    sim.run(60)
+    sim.fill_model(m.MODEL_CIRCLE, [radius, 0.0])
+    sim.run(warm)
     before = [sim.ntff(w) for w in range(3)]
+    before_guard = [sim.ntff_guard(w) for w in range(3)]
 
     n_block = 360 * sim.array_size
-    acc = torch.zeros((3, 2 * (n_block + 2 * GUARD)), dtype=torch.float64, device="cuda")
+    # the caller's own accumulators: [canary | guard | block | guard | canary] per array
+    n_all = n_block + 2 * GUARD + 2 * CANARY
+    acc = torch.zeros((3, 2 * n_all), dtype=torch.float64, device="cuda")
+    bits = acc.view(torch.int64)
+    canary = int(CANARY_BITS.view(np.int64))
+    bits[:, :2 * CANARY] = canary
+    bits[:, 2 * (n_all - CANARY):] = canary
     tm = solver == "MPI_TM_UPML"
     fields = [_device_field(lib, sim, w) for w in range(3)]
     args = _StepArgs()
@@ -74,7 +95,7 @@ def test_noalloc_ntff_step_matches_engine(solver):
         args.e0, args.e1, args.h0, args.h1 = fields[0][0], fields[1][0], fields[2][0], None
     args.pitch = fields[0][1]
     for w in range(3):
-        args.acc[w] = acc[w].data_ptr() + GUARD * 16
+        args.acc[w] = acc[w].data_ptr() + (CANARY + GUARD) * 16
     torch.cuda.synchronize()
 
     for call in range(2):                     # two calls in a row
@@ -86,12 +107,22 @@ def test_noalloc_ntff_step_matches_engine(solver):
         assert rc == 0, lib.fdtd_last_error().decode()
         sim.synchronize()
         torch.cuda.synchronize()
-        got = acc.cpu().numpy().view(np.complex128)[:, GUARD:GUARD + n_block]
+        host = acc.cpu().numpy()
+        got = host.view(np.complex128)
         for w in range(3):
             want = sim.ntff(w) - before[w]    # the engine's accumulation of the same steps
             assert np.abs(want).max() > 0
-            err = _rel(got[w], want)
-            assert err <= 1e-12, (solver, call, w, err)
+            err = _rel(got[w, CANARY + GUARD:CANARY + GUARD + n_block], want)
+            assert err <= 1e-12, (case, call, w, err)
+            # guard cells: what the engine's flat index spilled there over the same steps
+            g_want = sim.ntff_guard(w) - before_guard[w]
+            g_got = np.concatenate([got[w, CANARY:CANARY + GUARD],
+                                    got[w, CANARY + GUARD + n_block:CANARY + 2 * GUARD + n_block]])
+            assert np.abs(g_got - g_want).max() <= 1e-12 * max(1.0, np.abs(want).max()), (case, call, w)
+            # nothing beyond the guards is written
+            raw = host[w].view(np.uint64)
+            assert np.all(raw[:2 * CANARY] == CANARY_BITS), (case, call, w, "front canary")
+            assert np.all(raw[2 * (n_all - CANARY):] == CANARY_BITS), (case, call, w, "back canary")
     assert sim.status == 0
 
 
