@@ -19,8 +19,11 @@
 //                      (rows), bias / accumulate / GELU, stores.
 // Every mbarrier wait is bounded: on timeout the kernel sets *err and leaves
 // the loop (results are then invalid and the host reports the error).
-// Batched: grid.z runs independent products (3-D tensor maps), B may be shared.
-// Shapes: M % 128 == 0, N % 64 == 0, K % 64 == 0, leading dims % 8 == 0.
+// Batched: grid.z runs independent products (3-D tensor maps); A or B may be
+// shared by every batch entry.
+// Shapes: M % 64 == 0, N % 64 == 0, K % 64 == 0, leading dims % 8 == 0.  A row
+// tile reaching past M (M = 64, or M % 128 == 64) is loaded with the tensor
+// map's zero fill and its rows past M are not stored.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -140,6 +143,7 @@ __device__ __forceinline__ float gelu(float x)
 
 struct Epilogue {
   void *c;            // output
+  int M;              // rows of C: accumulator lanes at or past M are not stored
   long long c_bstride;  // elements between batch entries of C (and pre)
   int ldc;
   int c_bf16;         // 1: BF16 output, 0: FP32
@@ -152,7 +156,7 @@ struct Epilogue {
 template <int BN>
 __global__ void __launch_bounds__(128, 2)
     gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tA, const __grid_constant__ CUtensorMap tB, Epilogue ep,
-                        int K, int b_batched, unsigned *err)
+                        int K, int a_batched, int b_batched, unsigned *err)
 {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -199,7 +203,7 @@ __global__ void __launch_bounds__(128, 2)
       const int s = kb % STAGES;
       if (kb >= STAGES && !mbar_wait(&empty[s], ((kb / STAGES) - 1) & 1, err, 1u)) break;
       mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
-      tma_load_3d(sA + s * A_BYTES, &tA, kb * BK, m0, z, &full[s]);
+      tma_load_3d(sA + s * A_BYTES, &tA, kb * BK, m0, a_batched ? z : 0, &full[s]);
       tma_load_3d(sB + s * B_BYTES, &tB, kb * BK, n0, b_batched ? z : 0, &full[s]);
     }
   } else if (threadIdx.x == 32) {  // MMA issuer
@@ -223,8 +227,8 @@ __global__ void __launch_bounds__(128, 2)
   // epilogue
   const bool have = __all_sync(0xffffffffu, mbar_wait(done, 0, err, 4u));  // tcgen05.ld is warp-aligned
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (have) {
-    const int row = m0 + warp * 32 + lane;
+  const int row = m0 + warp * 32 + lane;
+  if (have && m0 + warp * 32 < ep.M) {  // tcgen05.ld stays warp-uniform; lanes past M skip their stores
 #pragma unroll 1
     for (int c = 0; c < BN; c += 32) {
       float v[32];
@@ -344,7 +348,7 @@ extern "C" int sg_gemm_bf16_tn_batched(const void *A, int lda, long long a_bstri
                                        float *pre, unsigned *err, void *stream)
 {
   if (!A || !B || !C || !err) return set_err(1, "null pointer");
-  if (M <= 0 || N <= 0 || K <= 0 || M % BM || K % BK || N % 64) return set_err(1, "shape: M%128, N%64, K%64");
+  if (M <= 0 || N <= 0 || K <= 0 || M % 64 || K % BK || N % 64) return set_err(1, "shape: M%64, N%64, K%64");
   if (batch < 1 || batch > 65535) return set_err(1, "batch must be in [1, 65535]");
   if (lda % 8 || ldb % 8 || ldc % 8 || a_bstride % 8 || b_bstride % 8 || c_bstride % 8 || ((uintptr_t)A & 15) ||
       ((uintptr_t)B & 15) || ((uintptr_t)C & 15))
@@ -353,14 +357,13 @@ extern "C" int sg_gemm_bf16_tn_batched(const void *A, int lda, long long a_bstri
   if (int rc = encoder()) return rc;
   const bool wide = N % 128 == 0;
   CUtensorMap ta, tb;
-  // B may be shared by every batch entry (b_bstride 0: a one-entry map always read at z = 0)
-  if (a_bstride == 0 && batch > 1) return set_err(1, "A must have a batch stride");
-  if (make_map(&ta, A, M, K, lda, BM, batch, a_bstride) ||
+  // A or B may be shared by every batch entry (bstride 0: a one-entry map always read at z = 0)
+  if (make_map(&ta, A, M, K, lda, BM, a_bstride ? batch : 1, a_bstride) ||
       make_map(&tb, B, N, K, ldb, wide ? 128 : 64, b_bstride ? batch : 1, b_bstride))
     return 1;
-  Epilogue ep{C, c_bstride, ldc, c_bf16, accumulate, bias, act, pre};
+  Epilogue ep{C, M, c_bstride, ldc, c_bf16, accumulate, bias, act, pre};
   cudaStream_t st = (cudaStream_t)stream;
-  const dim3 grid((unsigned)(N / (wide ? 128 : 64)), (unsigned)(M / BM), (unsigned)batch);
+  const dim3 grid((unsigned)(N / (wide ? 128 : 64)), (unsigned)((M + BM - 1) / BM), (unsigned)batch);
   if (wide) {
     static bool cfg = false;
     if (!cfg) {
@@ -368,7 +371,8 @@ extern "C" int sg_gemm_bf16_tn_batched(const void *A, int lda, long long a_bstri
                            (int)smem_bytes<128>());
       cfg = true;
     }
-    gemm_bf16_tn_kernel<128><<<grid, 128, smem_bytes<128>(), st>>>(ta, tb, ep, K, b_bstride ? 1 : 0, err);
+    gemm_bf16_tn_kernel<128><<<grid, 128, smem_bytes<128>(), st>>>(ta, tb, ep, K, a_bstride ? 1 : 0,
+                                                                   b_bstride ? 1 : 0, err);
   } else {
     static bool cfg = false;
     if (!cfg) {
@@ -376,7 +380,8 @@ extern "C" int sg_gemm_bf16_tn_batched(const void *A, int lda, long long a_bstri
                            (int)smem_bytes<64>());
       cfg = true;
     }
-    gemm_bf16_tn_kernel<64><<<grid, 128, smem_bytes<64>(), st>>>(ta, tb, ep, K, b_bstride ? 1 : 0, err);
+    gemm_bf16_tn_kernel<64><<<grid, 128, smem_bytes<64>(), st>>>(ta, tb, ep, K, a_bstride ? 1 : 0,
+                                                                 b_bstride ? 1 : 0, err);
   }
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_err(2, cudaGetErrorString(e));

@@ -1,11 +1,14 @@
 // surrogate_ops.cu -- the far-field surrogate's non-GEMM kernels (forward,
-// backward, optimizer).  Every contraction of the model runs in the tcgen05
-// GEMM (surrogate_gemm.cu); these kernels do the layout permutations,
-// pooling, the point-wise channel mixing, activations, reductions, the loss
-// and the Adam update.  Tensors are row-major; shapes are given per call.
+// backward, optimizer).  Every contraction of the model, the point-wise
+// channel mixing included, runs in the tcgen05 GEMM (surrogate_gemm.cu); these
+// kernels do the layout permutations, pooling, activations, reductions, the
+// loss and the Adam update.  Tensors are row-major; shapes are given per call.
 //
 // Notation: B structures, C = 64 channels, S = 1024 points of the 32 x 32 grid,
 // Q = 256 retained Fourier modes (2 real components each: 2Q = 512).
+// Activations exist in two layouts: channels-first [B][C][S] (rows of S points,
+// the operand of the truncated-DFT GEMMs) and channels-last [B][S][C] (rows of
+// C channels, the operand and output of the point-wise mixing GEMM).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -42,40 +45,42 @@ __global__ void pool_map_kernel(const uint8_t *map, float *x, int B)
   x[i] = s * (1.0f / 64.0f);
 }
 
-// h0[b][c][s] = x[b][s] wl[c] + bl[c]
-__global__ void lift_kernel(const float *x, const float *wl, const float *bl, bf16 *h, int B, int C)
+// h0[b][c][s] = x[b][s] wl[c] + bl[c] in both layouts: i < n writes the
+// channels-first copy, n <= i < 2n the channels-last one (each coalesced)
+__global__ void lift_kernel(const float *x, const float *wl, const float *bl, bf16 *h_cf, bf16 *h_cl, int B, int C)
 {
+  const size_t n = (size_t)B * C * 1024;
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (size_t)B * C * 1024) return;
-  const int s = i % 1024, c = (i / 1024) % C, b = (int)(i / (1024 * (size_t)C));
-  h[i] = __float2bfloat16(x[(size_t)b * 1024 + s] * wl[c] + bl[c]);
+  if (i >= 2 * n) return;
+  if (i < n) {
+    const int s = i % 1024, c = (i / 1024) % C, b = (int)(i / (1024 * (size_t)C));
+    h_cf[i] = __float2bfloat16(x[(size_t)b * 1024 + s] * wl[c] + bl[c]);
+  } else {
+    const size_t k = i - n;
+    const int c = k % C, s = (k / C) % 1024, b = (int)(k / ((size_t)C * 1024));
+    h_cl[k] = __float2bfloat16(x[(size_t)b * 1024 + s] * wl[c] + bl[c]);
+  }
 }
 
-// lift backward: dwl[c] = sum_{b,s} dh x, dbl[c] = sum dh (one block per c)
-__global__ void lift_bwd_kernel(const float *x, const float *dh, float *dwl, float *dbl, int B, int C)
+// column sums of a tall FP32 [R][64] matrix, plain and weighted by w[r]:
+// out[c] += sum_r a[r][c], out_w[c] += sum_r a[r][c] w[r] (both zeroed by the
+// caller); 4 row lanes x 64 columns per block, one atomic per column and block
+__global__ void colsum_tall_kernel(const float *a, const float *w, float *out, float *out_w, long long R)
 {
-  const int c = blockIdx.x;
-  float sw = 0, sb = 0;
-  for (int i = threadIdx.x; i < B * 1024; i += blockDim.x) {
-    const int b = i / 1024, s = i % 1024;
-    const float g = dh[((size_t)b * C + c) * 1024 + s];
-    sw += g * x[(size_t)b * 1024 + s];
-    sb += g;
+  const int c = threadIdx.x & 63, rl = threadIdx.x >> 6;
+  float s = 0, sw = 0;
+  for (long long r = (long long)blockIdx.x * 4 + rl; r < R; r += (long long)gridDim.x * 4) {
+    const float v = a[r * 64 + c];
+    s += v;
+    if (w) sw += v * w[r];
   }
-  __shared__ float rw[256], rb[256];
-  rw[threadIdx.x] = sw;
-  rb[threadIdx.x] = sb;
+  __shared__ float rs[4][64], rw[4][64];
+  rs[rl][c] = s;
+  rw[rl][c] = sw;
   __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if ((int)threadIdx.x < w) {
-      rw[threadIdx.x] += rw[threadIdx.x + w];
-      rb[threadIdx.x] += rb[threadIdx.x + w];
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    dwl[c] = rw[0];
-    dbl[c] = rb[0];
+  if (rl == 0) {
+    atomicAdd(&out[c], rs[0][c] + rs[1][c] + rs[2][c] + rs[3][c]);
+    if (w) atomicAdd(&out_w[c], rw[0][c] + rw[1][c] + rw[2][c] + rw[3][c]);
   }
 }
 
@@ -97,81 +102,52 @@ __global__ void mode_permute_kernel(const bf16 *in, bf16 *out, int B, int C, int
   }
 }
 
-// z[b][c][s] = hs[b][c][s] + sum_c' wp[c][c'] h[b][c'][s] + bp[c]; hn = act(z)
-// block: one (b, 32 points); thread: point s, all C outputs
-__global__ void pointwise_fwd_kernel(const bf16 *h, const float *hs, const float *wp, const float *bp, float *z,
-                                     bf16 *hn, int B, int C, int act)
+// Activation of the mixed layer, one tile of 32 points x 64 channels of one
+// structure per block: z (FP32, channels-last, the pre-activation the backward
+// keeps) -> hn = act(z) in BF16, channels-last (next point-wise GEMM) and
+// channels-first (next DFT GEMM, transposed through shared memory).
+__global__ void __launch_bounds__(256) act_fwd_kernel(const float *z, bf16 *hn_cf, bf16 *hn_cl, int act)
 {
-  __shared__ float w[64 * 64];
-  for (int q = threadIdx.x; q < C * C; q += blockDim.x) w[q] = wp[q];
+  __shared__ bf16 t[64][34];
+  const int b = blockIdx.y, s0 = blockIdx.x * 32;
+  const size_t base = ((size_t)b * 1024 + s0) * 64;
+  for (int e = threadIdx.x; e < 32 * 64; e += 256) {
+    const float v = z[base + e];
+    const bf16 h = __float2bfloat16(act ? gelu_f(v) : v);
+    hn_cl[base + e] = h;
+    t[e & 63][e >> 6] = h;
+  }
   __syncthreads();
-  const int b = blockIdx.y, s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= 1024) return;
-  float hv[64];
-  for (int c = 0; c < C; c++) hv[c] = __bfloat162float(h[((size_t)b * C + c) * 1024 + s]);
-  for (int c = 0; c < C; c++) {
-    float acc = bp[c];
-    for (int k = 0; k < C; k++) acc += w[c * C + k] * hv[k];
-    const size_t o = ((size_t)b * C + c) * 1024 + s;
-    const float zz = hs[o] + acc;
-    z[o] = zz;
-    hn[o] = __float2bfloat16(act ? gelu_f(zz) : zz);
+  for (int e = threadIdx.x; e < 32 * 64; e += 256) {
+    const int c = e >> 5, r = e & 31;
+    hn_cf[((size_t)b * 64 + c) * 1024 + s0 + r] = t[c][r];
   }
 }
 
-// dz = dh * act'(z) (FP32, in place in dz); dhs_bf = bf16(dz) for the spectral GEMMs
-__global__ void act_bwd_kernel(const float *dh, const float *z, float *dz, bf16 *dz_bf, size_t n, int act)
+// Backward of the activation on the same tiles: dz = dh act'(z) from
+// channels-last dh and z; writes BF16 dz channels-last (point-wise GEMMs) and
+// channels-first (DFT GEMMs), and adds the column sums of the FP32 dz into
+// dbp[c] (the bias gradient, zeroed by the caller).
+__global__ void __launch_bounds__(256) act_bwd_kernel(const float *dh, const float *z, bf16 *dz_cl, bf16 *dz_cf,
+                                                      float *dbp, int act)
 {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float g = act ? dh[i] * gelu_grad(z[i]) : dh[i];
-  dz[i] = g;
-  dz_bf[i] = __float2bfloat16(g);
-}
-
-// dh_prev[b][c'][s] = sum_c wp[c][c'] dz[b][c][s] + dspec[b][c'][s]
-__global__ void pointwise_bwd_x_kernel(const float *dz, const float *wp, const float *dspec, float *dh, int B, int C)
-{
-  __shared__ float w[64 * 64];
-  for (int q = threadIdx.x; q < C * C; q += blockDim.x) w[q] = wp[q];
+  __shared__ float t[64][33];
+  const int b = blockIdx.y, s0 = blockIdx.x * 32;
+  const size_t base = ((size_t)b * 1024 + s0) * 64;
+  for (int e = threadIdx.x; e < 32 * 64; e += 256) {
+    const float g = act ? dh[base + e] * gelu_grad(z[base + e]) : dh[base + e];
+    dz_cl[base + e] = __float2bfloat16(g);
+    t[e & 63][e >> 6] = g;
+  }
   __syncthreads();
-  const int b = blockIdx.y, s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= 1024) return;
-  float g[64];
-  for (int c = 0; c < C; c++) g[c] = dz[((size_t)b * C + c) * 1024 + s];
-  for (int k = 0; k < C; k++) {
-    float acc = 0;
-    for (int c = 0; c < C; c++) acc += w[c * C + k] * g[c];
-    const size_t o = ((size_t)b * C + k) * 1024 + s;
-    dh[o] = acc + dspec[o];
+  for (int e = threadIdx.x; e < 32 * 64; e += 256) {
+    const int c = e >> 5, r = e & 31;
+    dz_cf[((size_t)b * 64 + c) * 1024 + s0 + r] = __float2bfloat16(t[c][r]);
   }
-}
-
-// dwp[c][c'] = sum_{b,s} dz[b][c][s] h[b][c'][s]; dbp[c] = sum dz  (one block per (c, c'))
-__global__ void pointwise_bwd_w_kernel(const float *dz, const bf16 *h, float *dwp, float *dbp, int B, int C)
-{
-  const int c = blockIdx.x / C, k = blockIdx.x % C;
-  float acc = 0, accb = 0;
-  for (int i = threadIdx.x; i < B * 1024; i += blockDim.x) {
-    const int b = i / 1024, s = i % 1024;
-    const float g = dz[((size_t)b * C + c) * 1024 + s];
-    acc += g * __bfloat162float(h[((size_t)b * C + k) * 1024 + s]);
-    if (k == 0) accb += g;
-  }
-  __shared__ float r[256], rb[256];
-  r[threadIdx.x] = acc;
-  rb[threadIdx.x] = accb;
-  __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if ((int)threadIdx.x < w) {
-      r[threadIdx.x] += r[threadIdx.x + w];
-      rb[threadIdx.x] += rb[threadIdx.x + w];
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    dwp[c * C + k] = r[0];
-    if (k == 0) dbp[c] = rb[0];
+  if (threadIdx.x < 64) {
+    float sum = 0;
+    for (int r = 0; r < 32; r++) sum += t[threadIdx.x][r];
+    atomicAdd(&dbp[threadIdx.x], sum);
   }
 }
 
@@ -189,11 +165,12 @@ __global__ void head_pool_kernel(const bf16 *h, bf16 *flat, int B, int C)
   flat[i] = __float2bfloat16(s * (1.0f / 16.0f));
 }
 
+// the backward of head_pool into channels-last dh [B][S][C]
 __global__ void head_unpool_kernel(const float *dflat, float *dh, int B, int C)
 {
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (size_t)B * C * 1024) return;
-  const int s = i % 1024, c = (i / 1024) % C, b = (int)(i / (1024 * (size_t)C));
+  const int c = i % C, s = (i / C) % 1024, b = (int)(i / ((size_t)C * 1024));
   const int px = (s / 32) / 4, py = (s % 32) / 4;
   dh[i] = dflat[((size_t)b * C + c) * 64 + px * 8 + py] * (1.0f / 16.0f);
 }
@@ -237,6 +214,16 @@ __global__ void colsum_kernel(const bf16 *a, float *out, int R, int N)
   if (j >= N) return;
   float s = 0;
   for (int r = 0; r < R; r++) s += __bfloat162float(a[(size_t)r * N + j]);
+  out[j] = s;
+}
+
+// column sums of an FP32 [R][N] matrix -> [N] (the dW partials of the point-wise GEMM, R = B)
+__global__ void colsum_f32_kernel(const float *a, float *out, int R, int N)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= N) return;
+  float s = 0;
+  for (int r = 0; r < R; r++) s += a[(size_t)r * N + j];
   out[j] = s;
 }
 
@@ -295,14 +282,19 @@ int sg_pool_map(const void *map, float *x, int B, void *stream)
   pool_map_kernel<<<nb((size_t)B * 1024, 256), 256, 0, ST>>>((const uint8_t *)map, x, B);
   RET;
 }
-int sg_lift(const float *x, const float *wl, const float *bl, void *h, int B, int C, void *stream)
+int sg_lift(const float *x, const float *wl, const float *bl, void *h_cf, void *h_cl, int B, int C, void *stream)
 {
-  lift_kernel<<<nb((size_t)B * C * 1024, 256), 256, 0, ST>>>(x, wl, bl, (bf16 *)h, B, C);
+  lift_kernel<<<nb(2 * (size_t)B * C * 1024, 256), 256, 0, ST>>>(x, wl, bl, (bf16 *)h_cf, (bf16 *)h_cl, B, C);
   RET;
 }
+// dwl[c] = sum_{b,s} dh[b][s][c] x[b][s], dbl[c] = sum dh[b][s][c]  (dh channels-last)
 int sg_lift_bwd(const float *x, const float *dh, float *dwl, float *dbl, int B, int C, void *stream)
 {
-  lift_bwd_kernel<<<C, 256, 0, ST>>>(x, dh, dwl, dbl, B, C);
+  if (C != 64) return 1;
+  if (cudaMemsetAsync(dwl, 0, 64 * sizeof(float), ST) != cudaSuccess ||
+      cudaMemsetAsync(dbl, 0, 64 * sizeof(float), ST) != cudaSuccess)
+    return 2;
+  colsum_tall_kernel<<<304, 256, 0, ST>>>(dh, x, dbl, dwl, (long long)B * 1024);
   RET;
 }
 int sg_mode_permute(const void *in, void *out, int B, int C, int Q, int dir, void *stream)
@@ -310,27 +302,18 @@ int sg_mode_permute(const void *in, void *out, int B, int C, int Q, int dir, voi
   mode_permute_kernel<<<nb((size_t)B * C * 2 * Q, 256), 256, 0, ST>>>((const bf16 *)in, (bf16 *)out, B, C, Q, dir);
   RET;
 }
-int sg_pointwise_fwd(const void *h, const float *hs, const float *wp, const float *bp, float *z, void *hn, int B,
-                     int C, int act, void *stream)
+int sg_act_fwd(const float *z, void *hn_cf, void *hn_cl, int B, int C, int act, void *stream)
 {
-  if (C > 64) return 1;
-  pointwise_fwd_kernel<<<dim3(32, B), 32, 0, ST>>>((const bf16 *)h, hs, wp, bp, z, (bf16 *)hn, B, C, act);
+  if (C != 64) return 1;
+  act_fwd_kernel<<<dim3(32, B), 256, 0, ST>>>(z, (bf16 *)hn_cf, (bf16 *)hn_cl, act);
   RET;
 }
-int sg_act_bwd(const float *dh, const float *z, float *dz, void *dz_bf, long long n, int act, void *stream)
+int sg_act_bwd(const float *dh, const float *z, void *dz_cl, void *dz_cf, float *dbp, int B, int C, int act,
+               void *stream)
 {
-  act_bwd_kernel<<<nb((size_t)n, 256), 256, 0, ST>>>(dh, z, dz, (bf16 *)dz_bf, (size_t)n, act);
-  RET;
-}
-int sg_pointwise_bwd_x(const float *dz, const float *wp, const float *dspec, float *dh, int B, int C, void *stream)
-{
-  if (C > 64) return 1;
-  pointwise_bwd_x_kernel<<<dim3(32, B), 32, 0, ST>>>(dz, wp, dspec, dh, B, C);
-  RET;
-}
-int sg_pointwise_bwd_w(const float *dz, const void *h, float *dwp, float *dbp, int B, int C, void *stream)
-{
-  pointwise_bwd_w_kernel<<<C * C, 256, 0, ST>>>(dz, (const bf16 *)h, dwp, dbp, B, C);
+  if (C != 64) return 1;
+  if (cudaMemsetAsync(dbp, 0, 64 * sizeof(float), ST) != cudaSuccess) return 2;
+  act_bwd_kernel<<<dim3(32, B), 256, 0, ST>>>(dh, z, (bf16 *)dz_cl, (bf16 *)dz_cf, dbp, act);
   RET;
 }
 int sg_head_pool(const void *h, void *flat, int B, int C, void *stream)
@@ -356,6 +339,11 @@ int sg_gelu_bwd(const float *du, const float *pre, void *dpre, long long n, void
 int sg_colsum(const void *a, float *out, int R, int N, void *stream)
 {
   colsum_kernel<<<nb((size_t)N, 256), 256, 0, ST>>>((const bf16 *)a, out, R, N);
+  RET;
+}
+int sg_colsum_f32(const float *a, float *out, int R, int N, void *stream)
+{
+  colsum_f32_kernel<<<nb((size_t)N, 256), 256, 0, ST>>>(a, out, R, N);
   RET;
 }
 int sg_transpose(const void *in, void *out, int Z, int R, int Cc, void *stream)

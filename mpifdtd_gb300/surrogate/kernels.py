@@ -41,13 +41,12 @@ def load():
 L_ = C.c_longlong
 _OPS: dict = {
     "sg_pool_map": [P, P, I, P],
-    "sg_lift": [P, P, P, P, I, I, P],
+    "sg_lift": [P, P, P, P, P, I, I, P],
     "sg_lift_bwd": [P, P, P, P, I, I, P],
     "sg_mode_permute": [P, P, I, I, I, I, P],
-    "sg_pointwise_fwd": [P, P, P, P, P, P, I, I, I, P],
-    "sg_act_bwd": [P, P, P, P, L_, I, P],
-    "sg_pointwise_bwd_x": [P, P, P, P, I, I, P],
-    "sg_pointwise_bwd_w": [P, P, P, P, I, I, P],
+    "sg_act_fwd": [P, P, P, I, I, I, P],
+    "sg_act_bwd": [P, P, P, P, P, I, I, I, P],
+    "sg_colsum_f32": [P, P, I, I, P],
     "sg_head_pool": [P, P, I, I, P],
     "sg_head_unpool": [P, P, I, I, P],
     "sg_mse": [P, P, P, P, I, I, I, P],
@@ -108,11 +107,12 @@ def gemm(a, b, out, bias=None, act=0, accumulate=False, pre=None):
     """out[M,N] = a[M,K] . b[N,K]^T (+bias) (+out) (GELU if act=1); a, b BF16
     row-major (last dim contiguous, leading dims may be strided views of
     rows), out FP32 or BF16; pre: FP32 [M,N] copy of the pre-activation.
-    Batched when a is 3-D: a[Z,M,K], b[Z,N,K] or shared b[N,K], out[Z,M,N]."""
+    Batched when out is 3-D: out[Z,M,N] with a[Z,M,K] or a shared a[M,K], and
+    b[Z,N,K] or a shared b[N,K] (at least one of a, b per batch entry)."""
     import torch
     assert a.dtype == torch.bfloat16 and b.dtype == torch.bfloat16
     assert a.stride(-1) == 1 and b.stride(-1) == 1 and out.stride(-1) == 1
-    z = a.shape[0] if a.dim() == 3 else 1
+    z = out.shape[0] if out.dim() == 3 else 1
     m, k = a.shape[-2:]
     n, k2 = b.shape[-2:]
     assert k == k2 and tuple(out.shape[-2:]) == (m, n)

@@ -11,8 +11,11 @@ Architecture (B structures, C = 64 channels, 32 x 32 grid, Q = 256 modes):
                       rows of D, fixed)                         [B*C, 512]
     Fm   = permute(F)                                           [Q, B, 2C]
     Y[q] = Fm[q] M_l[q]^T   per-mode real 2C x 2C mixing        [Q, B, 2C]
-    Hs   = permute(Y) E^T   inverse transform (fixed E)         [B*C, 1024]
-    z    = Hs + wp_l h + bp_l ;  h = GELU(z) (no GELU after the last layer)
+    Yt   = permute(Y)                                           [B*C, 512]
+    z[b] = E Yt[b]^T        inverse transform (fixed E), channels-last [B, 1024, C]
+    z   += h_cl wp_l^T + bp_l   point-wise channel mixing, same GEMM kernel
+    h    = GELU(z) (no GELU after the last layer), kept channels-first [B, C, 1024]
+           for the DFT GEMM and channels-last [B*1024, C] for the mixing GEMM
   flat   = 4 x 4 mean pool of h                                 [B, C*64]
   u      = GELU(flat W1^T + b1)                                 [B, 512]
   out    = u W2^T + b2                                          [B, 11264]
@@ -79,8 +82,10 @@ class FNO:
         dev = "cuda"
         p = params if params is not None else init_params(seed)
         self.p = {k: torch.tensor(v, device=dev, dtype=torch.float32) for k, v in p.items()}
-        # BF16 copies of the GEMM weights (mode mixing M0..M3, head W1, W2), refreshed by adam_step
-        self.bf = {k: self.p[k].to(torch.bfloat16) for k in [f"M{l}" for l in range(NL)] + ["W1", "W2"]}
+        # BF16 copies of the GEMM weights (mode mixing M0..M3, point-wise wp0..wp3, head W1, W2),
+        # refreshed by adam_step
+        self.bf = {k: self.p[k].to(torch.bfloat16)
+                   for k in [f"M{l}" for l in range(NL)] + [f"wp{l}" for l in range(NL)] + ["W1", "W2"]}
         D, E = basis()
         self.D = torch.tensor(D, device=dev, dtype=torch.bfloat16)        # [512, 1024]
         self.E = torch.tensor(E, device=dev, dtype=torch.bfloat16)        # [1024, 512]
@@ -109,28 +114,31 @@ class FNO:
         B = x.shape[0]
         assert B % 128 == 0
         bf = t.bfloat16
-        h = self._e((B, C, NS), bf)
-        K.op("sg_lift", x, self.p["wl"], self.p["bl"], h, B, C)
+        h = self._e((B, C, NS), bf)                 # channels-first
+        h_cl = self._e((B, NS, C), bf)              # channels-last
+        K.op("sg_lift", x, self.p["wl"], self.p["bl"], h, h_cl, B, C)
         acts = {"x": x, "h": [], "Fm": [], "z": []}
         F = self._e((B * C, 2 * Q), bf)
         Fm = self._e((Q, B, 2 * C), bf)
         Y = self._e((Q, B, 2 * C), bf)
         Yt = self._e((B * C, 2 * Q), bf)
-        Hs = self._e((B * C, NS))
         for l in range(NL):
             K.gemm(h.view(B * C, NS), self.D, F)
             K.op("sg_mode_permute", F, Fm, B, C, Q, 0)
             K.gemm(Fm, self.bf[f"M{l}"], Y)
             K.op("sg_mode_permute", Y, Yt, B, C, Q, 1)
-            K.gemm(Yt, self.E, Hs)
-            z = self._e((B, C, NS))
+            z = self._e((B, NS, C))
+            K.gemm(self.E, Yt.view(B, C, 2 * Q), z)                     # inverse DFT, channels-last
+            K.gemm(h_cl.view(B * NS, C), self.bf[f"wp{l}"], z.view(B * NS, C),
+                   bias=self.p[f"bp{l}"], accumulate=True)             # + point-wise mixing
             hn = self._e((B, C, NS), bf)
-            K.op("sg_pointwise_fwd", h, Hs, self.p[f"wp{l}"], self.p[f"bp{l}"], z, hn, B, C, 1 if l < NL - 1 else 0)
+            hn_cl = self._e((B, NS, C), bf)
+            K.op("sg_act_fwd", z, hn, hn_cl, B, C, 1 if l < NL - 1 else 0)
             if save:
                 acts["h"].append(h)
                 acts["Fm"].append(Fm.clone())
                 acts["z"].append(z)
-            h = hn
+            h, h_cl = hn, hn_cl
         flat = self._e((B, C * 64), bf)
         K.op("sg_head_pool", h, flat, B, C)
         u = self._e((B, H1), bf)
@@ -170,29 +178,32 @@ class FNO:
         K.op("sg_colsum", dpre1, g["b1"], B, H1)
         dflat = self._e((B, C * 64))
         K.gemm(dpre1, K.transpose(self.bf["W1"]), dflat)
-        dh = self._e((B, C, NS))
+        dh = self._e((B, NS, C))                                       # channels-last
         K.op("sg_head_unpool", dflat, dh, B, C)
-        dz = self._e((B, C, NS))
-        dz_bf = self._e((B, C, NS), bf)
+        dz_cl = self._e((B, NS, C), bf)
+        dz_cf = self._e((B, C, NS), bf)
         dYt = self._e((B * C, 2 * Q), bf)
         dY = self._e((Q, B, 2 * C), bf)
         dFm = self._e((Q, B, 2 * C), bf)
         dF = self._e((B * C, 2 * Q), bf)
-        dspec = self._e((B * C, NS))
+        dw_part = self._e((B, C, C))
         for l in reversed(range(NL)):
-            K.op("sg_act_bwd", dh, a["z"][l], dz, dz_bf, B * C * NS, 1 if l < NL - 1 else 0)
-            g[f"wp{l}"] = self._e((C, C))
             g[f"bp{l}"] = self._e((C,))
-            K.op("sg_pointwise_bwd_w", dz, a["h"][l], g[f"wp{l}"], g[f"bp{l}"], B, C)
-            K.gemm(dz_bf.view(B * C, NS), self.Et, dYt)
+            K.op("sg_act_bwd", dh, a["z"][l], dz_cl, dz_cf, g[f"bp{l}"], B, C, 1 if l < NL - 1 else 0)
+            # dwp[c][c'] = sum_{b,s} dz[b][c][s] h[b][c'][s]: per-structure partials, then summed
+            K.gemm(dz_cf, a["h"][l], dw_part)
+            g[f"wp{l}"] = self._e((C, C))
+            K.op("sg_colsum_f32", dw_part, g[f"wp{l}"], B, C * C)
+            K.gemm(dz_cf.view(B * C, NS), self.Et, dYt)
             K.op("sg_mode_permute", dYt, dY, B, C, Q, 0)
             g[f"M{l}"] = self._e((Q, 2 * C, 2 * C))
             K.gemm(K.transpose(dY), K.transpose(a["Fm"][l]), g[f"M{l}"])
             K.gemm(dY, K.transpose(self.bf[f"M{l}"]), dFm)
             K.op("sg_mode_permute", dFm, dF, B, C, Q, 1)
-            K.gemm(dF, self.Dt, dspec)
-            dh_prev = self._e((B, C, NS))
-            K.op("sg_pointwise_bwd_x", dz, self.p[f"wp{l}"], dspec, dh_prev, B, C)
+            dh_prev = self._e((B, NS, C))
+            K.gemm(self.Dt, dF.view(B, C, 2 * Q), dh_prev)             # spectral part, channels-last
+            K.gemm(dz_cl.view(B * NS, C), K.transpose(self.bf[f"wp{l}"]), dh_prev.view(B * NS, C),
+                   accumulate=True)                                    # + point-wise part
             dh = dh_prev
         g["wl"] = self._e((C,))
         g["bl"] = self._e((C,))

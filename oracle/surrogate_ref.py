@@ -61,6 +61,7 @@ def loss_and_grads(p, x, y, D, E):
     Db, Eb = bf16(D), bf16(E)
     Mb = [bf16(p[f"M{l}"]) for l in range(NL)]
     W1b, W2b = bf16(p["W1"]), bf16(p["W2"])
+    Wpb = [bf16(p[f"wp{l}"]) for l in range(NL)]   # the point-wise mixing runs in the BF16 GEMM
     h = bf16(x[:, None, :] * p["wl"][None, :, None] + p["bl"][None, :, None])
     hs, Fms, zs = [], [], []
     for l in range(NL):
@@ -68,7 +69,7 @@ def loss_and_grads(p, x, y, D, E):
         Fm = to_modes(F, B)
         Y = bf16(np.einsum("qbk,qnk->qbn", Fm, Mb[l]))
         Hs = from_modes(Y, B) @ Eb.T
-        z = Hs.reshape(B, C, NS) + np.einsum("ck,bks->bcs", p[f"wp{l}"], h) + p[f"bp{l}"][None, :, None]
+        z = Hs.reshape(B, C, NS) + np.einsum("ck,bks->bcs", Wpb[l], h) + p[f"bp{l}"][None, :, None]
         hs.append(h)
         Fms.append(Fm)
         zs.append(z)
@@ -91,14 +92,15 @@ def loss_and_grads(p, x, y, D, E):
     dh = head_unpool(dflat, B)
     for l in reversed(range(NL)):
         dz = dh * (gelu_grad(zs[l]) if l < NL - 1 else 1.0)
-        g[f"wp{l}"] = np.einsum("bcs,bks->ck", dz, hs[l])
+        dzb = bf16(dz)                                # GEMM operand
+        g[f"wp{l}"] = np.einsum("bcs,bks->ck", dzb, hs[l])
         g[f"bp{l}"] = dz.sum(axis=(0, 2))
-        dYt = bf16(bf16(dz).reshape(B * C, NS) @ Eb)
+        dYt = bf16(dzb.reshape(B * C, NS) @ Eb)
         dY = to_modes(dYt, B)
         g[f"M{l}"] = np.einsum("qbn,qbk->qnk", dY, Fms[l])
         dFm = bf16(np.einsum("qbn,qnk->qbk", dY, Mb[l]))
         dspec = from_modes(dFm, B) @ Db
-        dh = np.einsum("ck,bcs->bks", p[f"wp{l}"], dz) + dspec.reshape(B, C, NS)
+        dh = np.einsum("ck,bcs->bks", Wpb[l], dzb) + dspec.reshape(B, C, NS)
     g["wl"] = (dh * x[:, None, :]).sum(axis=(0, 2))
     g["bl"] = dh.sum(axis=(0, 2))
     return loss, g

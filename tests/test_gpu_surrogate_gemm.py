@@ -77,3 +77,42 @@ def test_gemm_batched(shared_b):
     bt = b.float().t() if shared_b else b.float().transpose(1, 2)
     ref = a.float() @ bt
     assert float((out.float() - ref).norm() / ref.norm()) < 1e-2
+
+
+def test_gemm_batched_shared_a():
+    """A shared by every batch entry, B per entry (the inverse DFT into the
+    channels-last layout: out[z] = E . Yt[z]^T)."""
+    import torch
+    from mpifdtd_gb300.surrogate import kernels as K
+    g = torch.Generator(device="cuda").manual_seed(13)
+    z, m, n, k = 19, 1024, 64, 512
+    a = torch.randn(m, k, device="cuda", generator=g).to(torch.bfloat16)
+    b = torch.randn(z, n, k, device="cuda", generator=g).to(torch.bfloat16)
+    out = torch.empty(z, m, n, device="cuda", dtype=torch.float32)
+    K.gemm(a, b, out)
+    torch.cuda.synchronize()
+    assert int(K.err_word().item()) == 0
+    ref = a.float() @ b.float().transpose(1, 2)
+    assert float((out - ref).norm() / ref.norm()) < 1e-5
+
+
+@pytest.mark.parametrize("m", [64, 192])
+def test_gemm_rows_not_a_multiple_of_the_tile(m):
+    """M = 64 (and 192): the last row tile reads zeros past M through the
+    tensor map's fill and stores only rows below M; the rows after the output
+    (a sentinel) stay untouched.  Batched, as the point-wise mixing's weight
+    gradient uses it."""
+    import torch
+    from mpifdtd_gb300.surrogate import kernels as K
+    g = torch.Generator(device="cuda").manual_seed(m)
+    z, n, k = 5, 64, 1024
+    a = torch.randn(z, m, k, device="cuda", generator=g).to(torch.bfloat16)
+    b = torch.randn(z, n, k, device="cuda", generator=g).to(torch.bfloat16)
+    big = torch.full((z + 1, m, n), 7.0, device="cuda", dtype=torch.float32)
+    out = big[:z]
+    K.gemm(a, b, out)
+    torch.cuda.synchronize()
+    assert int(K.err_word().item()) == 0
+    ref = a.float() @ b.float().transpose(1, 2)
+    assert float((out - ref).norm() / ref.norm()) < 1e-5
+    assert bool((big[z] == 7.0).all())
