@@ -159,17 +159,58 @@ def ncu_traffic_per_cell():
 
 # ---------------------------------------------------------------- CPU arms
 
-def cpu_sample_run(steps, threads):
-    """Oracle restatement on `threads` cores, one independent instance each."""
+def cpu_sample_run(steps, threads, ntff=True):
+    """Oracle restatement on `threads` cores, one independent instance each
+    (ntff=False: without the time-domain NTFF, to split a step's time)."""
     from oracle.pyoracle import FieldInfo, Model, oracle_bench
     p = morpho_params()
     model = Model(2, p)  # MODEL_MORPHO with the same parameter vector layout
     fi = FieldInfo(*SAMPLE_FIELD)
-    dt = oracle_bench("MPI_TM_UPML", fi, model, steps, threads)
+    dt = oracle_bench("MPI_TM_UPML", fi, model, steps, threads, ntff=ntff)
     if dt <= 0:
         raise RuntimeError("oracle sample failed")
     n = (SAMPLE_FIELD[0] // SAMPLE_FIELD[2]) * (SAMPLE_FIELD[1] // SAMPLE_FIELD[2])
     return n * steps * threads / dt / 1e9, dt, n
+
+
+def grid_cells_and_path(field):
+    """Cells per step and NTFF path cells (field.c:132-142: 5 cells inside the PML) of a FieldInfo."""
+    n_px, n_py, pml = field[0] // field[2], field[1] // field[2], field[3]
+    return n_px * n_py, 2 * ((n_px - pml - 5) - (pml + 5)) + 2 * ((n_py - pml - 5) - (pml + 5))
+
+
+def cpu_baseline(steps, threads):
+    """The oracle port on the down-scaled sample (the measured value), plus the
+    corrections a reader needs to compare it with the 16416^2 workload: the
+    sample timed again without the NTFF gives a per-cell stencil cost and a
+    per-path-cell NTFF cost, which project the same cores' rate to the full
+    grid, where the 360-angle NTFF is a far smaller share of a step; and the
+    port's speed against the reference's own compiled sources."""
+    value, dt, n = cpu_sample_run(steps, threads)
+    _, dt0, _ = cpu_sample_run(steps, threads, ntff=False)
+    cells_s, path_s = grid_cells_and_path(SAMPLE_FIELD)
+    cells_f, path_f = grid_cells_and_path(FIELD)
+    t_cell = dt0 / steps / cells_s                          # s per cell-update, per instance
+    t_path = max(dt - dt0, 0.0) / steps / path_s            # s per NTFF path cell and step, per instance
+    t_full = cells_f * t_cell + path_f * t_path
+    out = {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{threads} independent {SAMPLE_FIELD[0] // 2}x{SAMPLE_FIELD[1] // 2} instances of the same "
+                     f"ridge (2 nm cells, MPI_TM_UPML FP64 with NTFF), {steps} steps each, {dt:.1f} s",
+           "ntff_share_of_step": {"sample_1040": max(dt - dt0, 0.0) / dt,
+                                  "projected_16416": path_f * t_path / t_full},
+           "projected_value_16416": cells_f * threads / t_full / 1e9,
+           "projection": "per-cell stencil and per-path-cell NTFF costs of the sample (timed with and "
+                         "without the NTFF), applied to the 16416^2 grid's cells and path; cache effects of "
+                         "the larger grid are not modelled"}
+    try:
+        ps = json.loads((ROOT / "oracle" / "port_speed.json").read_text())
+        out["port_vs_compiled_reference"] = {
+            "ratio": ps["ratio_port_over_reference_median"], "range": ps["ratio_range"], "where": ps["what"],
+            "host": ps["host"], "note": "measured on the build host by oracle/time_port_vs_reference.py "
+                                        "(the reference sources are not on the GPU host)"}
+    except (OSError, KeyError, ValueError):
+        pass
+    return out
 
 
 def host_threads():
@@ -187,15 +228,15 @@ def run_reference_arm(args):
     # warm-up: W steps per instance, untimed (also builds the oracle)
     if args.warmup > 0:
         cpu_sample_run(max(1, min(args.warmup, 3)), threads)
-    value, dt, n = cpu_sample_run(args.steps, threads)
-    sample = (f"{threads} independent {SAMPLE_FIELD[0] // 2}x{SAMPLE_FIELD[1] // 2} instances of the same ridge "
-              f"(2 nm cells, MPI_TM_UPML FP64 with NTFF), {args.steps} steps each")
+    cpu = cpu_baseline(args.steps, threads)
+    value = cpu["value"]
+    dt = value and (SAMPLE_FIELD[0] // 2) * (SAMPLE_FIELD[1] // 2) * args.steps * threads / (value * 1e9)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": cpu,
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's loops restated in C (oracle/fdtd_oracle.c, bit-identical to the reference "
                 "on its golden vectors); the reference sources are not present on this host",
@@ -299,13 +340,7 @@ def run_gpu_arm(args):
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
-            threads = host_threads()
-            steps = 150
-            v, dt, n = cpu_sample_run(steps, threads)
-            cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                   "sample": f"{threads} independent {SAMPLE_FIELD[0] // 2}x{SAMPLE_FIELD[1] // 2} instances of "
-                             f"the same ridge (2 nm cells, MPI_TM_UPML FP64 with NTFF), {steps} steps each, "
-                             f"{dt:.1f} s"}
+            cpu = cpu_baseline(150, host_threads())
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,

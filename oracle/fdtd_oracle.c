@@ -80,6 +80,7 @@ struct of_sim {
   double *c[15];
   double *eps[3];
   cplx *nt_base[3], *nt[3];
+  int skip_ntff;                         /* of_bench_opts: leave the time-domain NTFF out (timing only) */
 };
 
 /* ---------------------------------------------------------------- models */
@@ -975,7 +976,7 @@ static void update(of_sim *s)
      * for one rank; the halos stay zero) */
     if (s->tm) { tm_jd_e(s); cw_source(s, s->f[0], s->eps[0]); tm_mb_h(s); }
     else       { te_jd_e(s); cw_source(s, s->f[1], s->eps[1]); te_mb_h(s); }
-    ntff_mpi(s);
+    if (!s->skip_ntff) ntff_mpi(s);
   } else if (s->tm) {      /* fdtdTM_upml.c:54-66 */
     tm_mb_h(s); tm_jd_e(s);
     pulse_source(s, s->f[0], s->eps[0], 0, 0, 1.0);
@@ -1186,7 +1187,7 @@ int of_frequency(of_sim *s, double *out)
 /* ------------------------------------------------------------ CPU bench */
 
 typedef struct {
-  int solver, steps; of_field_info fi; of_model m;
+  int solver, steps, skip_ntff; of_field_info fi; of_model m;
   pthread_barrier_t *bar; of_sim *sim;
 } bench_arg;
 
@@ -1194,6 +1195,7 @@ static void *bench_worker(void *p)
 {
   bench_arg *a = (bench_arg *)p;
   a->sim = of_create(a->solver, &a->fi, &a->m);
+  if (a->sim) a->sim->skip_ntff = a->skip_ntff;
   pthread_barrier_wait(a->bar);         /* setup done everywhere */
   if (a->sim) of_step(a->sim, a->steps);
   pthread_barrier_wait(a->bar);         /* stepping done everywhere */
@@ -1208,13 +1210,20 @@ static double now_s(void)
 
 double of_bench(int solver, const of_field_info *fi, const of_model *m, int steps, int n_threads)
 {
+  return of_bench_opts(solver, fi, m, steps, n_threads, 0);
+}
+
+/* flags bit 0: the MPI solvers skip their time-domain NTFF, so that the
+ * stencil's and the NTFF's shares of a step can be told apart. */
+double of_bench_opts(int solver, const of_field_info *fi, const of_model *m, int steps, int n_threads, int flags)
+{
   if (n_threads < 1) n_threads = 1;
   pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * n_threads);
   bench_arg *args = (bench_arg *)calloc(n_threads, sizeof(bench_arg));
   pthread_barrier_t bar;
   pthread_barrier_init(&bar, NULL, n_threads + 1);
   for (int t = 0; t < n_threads; t++) {
-    args[t].solver = solver; args[t].steps = steps; args[t].fi = *fi;
+    args[t].solver = solver; args[t].steps = steps; args[t].fi = *fi; args[t].skip_ntff = flags & 1;
     if (m) args[t].m = *m;
     args[t].bar = &bar;
     pthread_create(&th[t], NULL, bench_worker, &args[t]);

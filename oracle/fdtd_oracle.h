@@ -62,6 +62,8 @@ int     of_frequency(of_sim *s, double *out);
  * parallel, as main.c:114-138 uses ranks); returns wall seconds of the
  * stepping phase only (setup excluded). */
 double  of_bench(int solver, const of_field_info *fi, const of_model *m, int steps, int n_threads);
+double  of_bench_opts(int solver, const of_field_info *fi, const of_model *m, int steps, int n_threads,
+                      int flags);
 
 #ifdef __cplusplus
 }

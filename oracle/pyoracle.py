@@ -173,6 +173,9 @@ def oracle_lib():
         lib.of_frequency.argtypes = [P, C.POINTER(C.c_double)]
         lib.of_bench.restype = C.c_double
         lib.of_bench.argtypes = [C.c_int, C.POINTER(_OfFieldInfo), C.POINTER(_OfModel), C.c_int, C.c_int]
+        lib.of_bench_opts.restype = C.c_double
+        lib.of_bench_opts.argtypes = [C.c_int, C.POINTER(_OfFieldInfo), C.POINTER(_OfModel), C.c_int, C.c_int,
+                                      C.c_int]
         _oracle_lib = lib
     return _oracle_lib
 
@@ -260,12 +263,13 @@ class OracleSim:
         return out.view(np.complex128)
 
 
-def oracle_bench(solver, fi: FieldInfo, model: Model, steps: int, threads: int) -> float:
-    """Wall seconds for `threads` independent simulations of `steps` steps."""
+def oracle_bench(solver, fi: FieldInfo, model: Model, steps: int, threads: int, ntff: bool = True) -> float:
+    """Wall seconds for `threads` independent simulations of `steps` steps
+    (ntff=False: the MPI solvers leave out their time-domain NTFF)."""
     lib = oracle_lib()
     cfi, cm = _pack(fi, model)
     s = SOLVERS[solver] if isinstance(solver, str) else solver
-    return lib.of_bench(s, C.byref(cfi), C.byref(cm), int(steps), int(threads))
+    return lib.of_bench_opts(s, C.byref(cfi), C.byref(cm), int(steps), int(threads), 0 if ntff else 1)
 
 
 _ref_lib = None

@@ -109,9 +109,11 @@ def test_noalloc_ntff_step_matches_engine(case):
         torch.cuda.synchronize()
         host = acc.cpu().numpy()
         got = host.view(np.complex128)
+        wants = [sim.ntff(w) - before[w] for w in range(3)]   # the engine's accumulation of the same steps
+        # (on the tall grid the far top and bottom sides see no field yet: their accumulator stays zero)
+        assert max(np.abs(x).max() for x in wants) > 0
         for w in range(3):
-            want = sim.ntff(w) - before[w]    # the engine's accumulation of the same steps
-            assert np.abs(want).max() > 0
+            want = wants[w]
             err = _rel(got[w, CANARY + GUARD:CANARY + GUARD + n_block], want)
             assert err <= 1e-12, (case, call, w, err)
             # guard cells: what the engine's flat index spilled there over the same steps
