@@ -356,18 +356,19 @@ def run_gpu_arm(args):
     return 0
 
 
-def run_variants(m, args, torch, cells, ms_f64):
-    """The same workload with FP32 fields (FP64 NTFF), temporal blocking picked
-    by the engine's autotuner, and the FP32-vs-FP64 error on the 1044^2 Mie
-    cylinder (field relative L2, far-field dB)."""
-    from mpifdtd_gb300.precision import compare_precisions
-    out = {}
-    sim = m.Simulation("MPI_TM_UPML", m.FieldInfo(*FIELD), "f32")
+def time_workload(m, args, torch, solver, precision, tune):
+    """The bench workload (16416^2 morpho ridge, NTFF every step) with another
+    solver / precision: args.steps steps device-timed on the engine stream
+    after the warm-up, the buffered NTFF deposit flushed inside the timing;
+    tune: temporal blocking picked by fdtd_autotune first."""
+    sim = m.Simulation(solver, m.FieldInfo(*FIELD), precision)
     sim.fill_model(m.MODEL_MORPHO, morpho_params())
+    cells = sim.n_px * sim.n_py
     stream = torch.cuda.ExternalStream(sim.stream)
     sim.run(args.warmup)
-    tune = sim.autotune()
-    sim.run(max(args.warmup, 2 * max(1, tune["tblock"])))
+    t = sim.autotune() if tune else None
+    if t:
+        sim.run(max(args.warmup, 2 * max(1, t["tblock"])))
     sim.synchronize()
     sim.profile(True)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -382,25 +383,47 @@ def run_variants(m, args, torch, cells, ms_f64):
     sim.profile(False)
     if sim.status != 0:
         raise RuntimeError(f"engine status {sim.status:#x}")
-    stencil = (prof["e_half"] + prof["h_half"]) / max(1, prof["steps"])
-    one_step = [c[-1] for c in tune["candidates"] if c[0] == 0][0]
-    b_alg = B_ALG[("tm", "f32")]
-    out["fp32_tm"] = {
-        "value": cells / (ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms, "speedup_vs_fp64": ms_f64 / ms,
-        "tblock": tune["tblock"], "tblock_rows": tune["tblock_rows"], "tblock_cols": tune["tblock_cols"],
-        "stencil_ms_per_step": stencil,
-        "stencil_ms_per_step_one_step_kernels": one_step,
-        "stencil_alg_gbs": cells * b_alg / (stencil * 1e-3) / 1e9, "bytes_per_cell_alg": b_alg,
-        "ntff_deposit_ms_per_step": prof["ntff_deposit"] / max(1, prof["steps"]),
-        "note": "algorithmic GB/s above the HBM peak is the temporal blocking: K steps per HBM pass",
-        "autotune": [list(c) for c in tune["candidates"]],
-    }
     sim.close()
-    fi = m.FieldInfo(5220, 5220, 5, 10, 500, 0, 4000)
-    rep = compare_precisions("MPI_TM_UPML", fi, (m.MODEL_CIRCLE, [500.0, 2.25]), steps=600)
-    out["fp32_error_vs_fp64"] = {"case": "1044^2 Mie cylinder r 500 nm eps 2.25, MPI_TM_UPML, 600 steps",
-                                 "field_rel_l2": rep["field_rel_l2"], "ntff_rel_l2": rep["ntff_rel_l2"],
-                                 "farfield_db_max": rep["farfield_db_max"]}
+    stencil = (prof["e_half"] + prof["h_half"]) / max(1, prof["steps"])
+    b_alg = B_ALG[("tm" if "TM" in solver else "te", precision)]
+    out = {"solver": solver, "precision": precision, "value": cells / (ms * 1e-3) / 1e9, "unit": UNIT,
+           "ms_per_step": ms, "stencil_ms_per_step": stencil,
+           "stencil_alg_gbs": cells * b_alg / (stencil * 1e-3) / 1e9, "bytes_per_cell_alg": b_alg,
+           "ntff_deposit_ms_per_step": prof["ntff_deposit"] / max(1, prof["steps"])}
+    if t:
+        out.update(tblock=t["tblock"], tblock_rows=t["tblock_rows"], tblock_cols=t["tblock_cols"],
+                   stencil_ms_per_step_one_step_kernels=[c[-1] for c in t["candidates"] if c[0] == 0][0],
+                   autotune=[list(c) for c in t["candidates"]])
+    else:
+        out["stencil_frac_of_hbm_peak"] = out["stencil_alg_gbs"] / measured_peak_hbm()[0]
+    return out
+
+
+def run_variants(m, args, torch, cells, ms_f64):
+    """The same workload with FP32 fields (FP64 NTFF) and temporal blocking
+    picked by the engine's autotuner, the TE solver in FP64 and FP32, and the
+    FP32-vs-FP64 error on config 2 (the 1044^2 Mie cylinder, TM and TE, all
+    4000 steps, NTFF 20 cells inside the PML)."""
+    from mpifdtd_gb300.precision import compare_precisions
+    out = {}
+    r = time_workload(m, args, torch, "MPI_TM_UPML", "f32", tune=True)
+    r["speedup_vs_fp64"] = ms_f64 / r["ms_per_step"]
+    r["note"] = "algorithmic GB/s above the HBM peak is the temporal blocking: K steps per HBM pass"
+    out["fp32_tm"] = r
+    if not args.no_te:
+        te64 = time_workload(m, args, torch, "MPI_TE_UPML", "f64", tune=False)
+        te32 = time_workload(m, args, torch, "MPI_TE_UPML", "f32", tune=True)
+        te32["speedup_vs_fp64"] = te64["ms_per_step"] / te32["ms_per_step"]
+        out["te_f64"], out["fp32_te"] = te64, te32
+    fi = m.FieldInfo(5220, 5220, 5, 10, 500, 0, 4000, ntff_inset=20)
+    out["fp32_error_vs_fp64"] = {}
+    for solver in ("MPI_TM_UPML", "MPI_TE_UPML"):
+        rep = compare_precisions(solver, fi, (m.MODEL_CIRCLE, [500.0, 2.25]), steps=4000)
+        out["fp32_error_vs_fp64"][solver] = {
+            "case": "config 2: 1044^2 Mie cylinder r 500 nm eps 2.25, lambda 500 nm, 4000 steps, "
+                    "NTFF 20 cells inside the PML",
+            "field_rel_l2": rep["field_rel_l2"], "ntff_rel_l2": rep["ntff_rel_l2"],
+            "farfield_db_max": rep["farfield_db_max"], "farfield_rel_l2": rep.get("farfield_rel_l2")}
     if not args.no_sweep:
         out["sweep"] = run_sweep()
     if not args.no_surrogate:
@@ -533,6 +556,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-variants", action="store_true", help="skip the FP32 / temporal-blocking line items")
     ap.add_argument("--no-sweep", action="store_true", help="skip the batched 256-structure sweep")
+    ap.add_argument("--no-te", action="store_true", help="skip the TE lines of the 16416^2 workload")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the learned-surrogate line item")
     ap.add_argument("--grid", type=int, default=0,
                     help="interior cells per side for a smaller case of the same workload (profiling)")

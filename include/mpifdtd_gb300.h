@@ -75,7 +75,18 @@ typedef struct fdtd_config {
   int width_nm, height_nm, h_u_nm, pml, lambda_nm, angle_deg, step_num;
   int precision;       /* FDTD_F64 or FDTD_F32                                 */
   int flags;           /* FDTD_CFG_* bits                                      */
-  int reserved[7];     /* must be zero                                         */
+  /* Settings the reference hard-codes; 0 keeps the reference's value.  The
+   * UPML solvers (2-5) take any; the split-field / NS solvers only 0. */
+  int courant_e4;      /* Courant number x 10^4, 1..7071 (2-D Yee stability
+                          needs <= 1/sqrt 2); 0: C_0_S = 0.7071 (field.h:70).
+                          It sets mu0 = 1/C^2 (the H update), omega = C k, the
+                          PML's sig_max, the NTFF time shifts and coefficients,
+                          the pulse source and the spectrum bins             */
+  int pml_order;       /* exponent M of the sigma grading, 1..8; 0: 2
+                          (field.c:259-283; sig_max uses M + 1 as there)      */
+  int ntff_inset;      /* cells between the PML and the NTFF path, >= 1;
+                          0: 5 (field.c:136-139)                              */
+  int reserved[4];     /* must be zero                                         */
 } fdtd_config;
 
 /* No time-domain NTFF state (accumulators, path tables): for CW runs whose
@@ -270,6 +281,26 @@ int fdtd_batch_set_option(fdtd_batch *batch, int key, int value);
 int fdtd_batch_run(fdtd_batch *batch);
 int fdtd_batch_reset(fdtd_batch *batch);
 long long fdtd_batch_launch_count(const fdtd_batch *batch);
+
+/* Broadband batch: the far field of every instance at many wavelengths from
+ * one run.  The reference's broadband run is a serial solver driven by
+ * field_scatteredPulse (field.c:224-256) whose ntffTM_TimeOutput spectrum
+ * (ntffTM.c:197-275) covers 380..700 nm; here every instance of an
+ * MPI_TM_UPML batch at 0 degrees gets that Gaussian pulse (carrier: its own
+ * lambda_nm) instead of the CW wave, and the NTFF path samples of every step
+ * feed a running DFT at the nlam given wavelengths (exact frequencies
+ * w = C 2 pi h_u / lambda).  The instances must be created with the
+ * time-domain NTFF state (no FDTD_CFG_NO_TIME_NTFF), one cell size and
+ * Courant number for all; call before fdtd_batch_run.
+ * fdtd_batch_broadband_spectrum: out[nlam][360] = |X(w)|^2 / |A(w)|^2 of
+ * instance `index` after its run, X the far-field component the spectrum
+ * transforms (E_theta, ntffTM.c:161-194) at w from the DFT sums, A the DFT of
+ * the incident pulse at x = 0 over the same steps: the far-field intensity of
+ * the structure's response to a unit incident plane wave at each wavelength,
+ * which the CW run approaches at its steady state.  step_num must let the
+ * pulse and the structure's ringing leave the grid. */
+int fdtd_batch_broadband(fdtd_batch *batch, int nlam, const int *lambda_nm);
+int fdtd_batch_broadband_spectrum(fdtd_batch *batch, int index, double *out);
 
 /* Number of kernel launches the engine issued since creation. */
 long long fdtd_launch_count(const fdtd_sim *sim);

@@ -61,12 +61,12 @@ int family_of(int solver)
 }
 bool is_mpi(int solver) { return solver == FDTD_MPI_TM_UPML || solver == FDTD_MPI_TE_UPML; }
 
-// field.c:259-283 (M = 2)
-double sigma_axis(double x, int n_pml, int n_inner, int n_full)
+// field.c:259-283 (the reference's M = 2; config pml_order sets M)
+double sigma_axis(double x, int n_pml, int n_inner, int n_full, int M = 2)
 {
-  if (x < n_pml) return std::pow(1.0 * (n_pml - x) / n_pml, 2);
+  if (x < n_pml) return std::pow(1.0 * (n_pml - x) / n_pml, M);
   if (x < n_inner + n_pml) return 0;
-  return std::pow(1.0 * (x - (n_full - n_pml - 1)) / n_pml, 2);
+  return std::pow(1.0 * (x - (n_full - n_pml - 1)) / n_pml, M);
 }
 
 }  // namespace
@@ -92,6 +92,13 @@ extern "C" int fdtd_geometry_of(const fdtd_config *cfg, fdtd_geometry *g)
     return fail(FDTD_E_ARG, "sizes must be positive");
   if (cfg->pml <= 0) return fail(FDTD_E_ARG, "pml must be positive (field.c:259-283 divides by it)");
   if (cfg->step_num < 0) return fail(FDTD_E_ARG, "step_num must be >= 0");
+  if (cfg->courant_e4 < 0 || cfg->courant_e4 > 7071)
+    return fail(FDTD_E_ARG, "courant_e4 %d outside [0, 7071] (Courant number <= 1/sqrt 2)", cfg->courant_e4);
+  if (cfg->pml_order < 0 || cfg->pml_order > 8) return fail(FDTD_E_ARG, "pml_order %d outside [0, 8]", cfg->pml_order);
+  if (cfg->ntff_inset < 0) return fail(FDTD_E_ARG, "ntff_inset %d < 0", cfg->ntff_inset);
+  for (int r = 0; r < 4; r++)
+    if (cfg->reserved[r]) return fail(FDTD_E_ARG, "reserved fields of fdtd_config must be zero");
+  const int inset = config_ntff_inset(*cfg);
   // field.c:95-100 (field_toCellUnit divides as double, the int conversion truncates)
   g->n_px = (int)((double)cfg->width_nm / cfg->h_u_nm);
   g->n_py = (int)((double)cfg->height_nm / cfg->h_u_nm);
@@ -101,20 +108,20 @@ extern "C" int fdtd_geometry_of(const fdtd_config *cfg, fdtd_geometry *g)
   // field.c:105-109
   g->lambda_s = (double)cfg->lambda_nm / cfg->h_u_nm;
   g->k_s = 2 * M_PI / g->lambda_s;
-  g->omega_s = kC * g->k_s;
+  g->omega_s = config_courant(*cfg) * g->k_s;
   // field.c:133-142
   g->ntff_cx = g->n_px / 2;
   g->ntff_cy = g->n_py / 2;
-  g->ntff_top = g->n_py - g->n_pml - 5;
-  g->ntff_bottom = g->n_pml + 5;
-  g->ntff_left = g->n_pml + 5;
-  g->ntff_right = g->n_px - g->n_pml - 5;
+  g->ntff_top = g->n_py - g->n_pml - inset;
+  g->ntff_bottom = g->n_pml + inset;
+  g->ntff_left = g->n_pml + inset;
+  g->ntff_right = g->n_px - g->n_pml - inset;
   double len = (g->ntff_top - g->ntff_bottom) / 2;
   g->rf_per_c = len * 2;
   g->array_size = (int)(cfg->step_num + 2 * g->rf_per_c);
   if (g->ntff_right - g->ntff_left < 2 || g->ntff_top - g->ntff_bottom < 2)
-    return fail(FDTD_E_ARG, "grid %dx%d too small for pml %d plus the 5-cell NTFF inset", g->n_px, g->n_py,
-                g->n_pml);
+    return fail(FDTD_E_ARG, "grid %dx%d too small for pml %d plus the %d-cell NTFF inset", g->n_px, g->n_py,
+                g->n_pml, inset);
   return FDTD_OK;
 }
 
@@ -124,19 +131,20 @@ static int build_tables(fdtd_sim *s)
 {
   const fdtd_geometry &g = s->geo;
   const bool tm = s->tm;
-  const double R = 1.0e-8, M = 2.0;
+  const int order = config_pml_order(s->cfg);
+  const double R = 1.0e-8, M = (double)order, C0 = s->c0;
   // mpiTM_UPML.c:672 / fdtdTM_upml.c:232 (TM, with 1/cos(pi/3)); mpiTE_UPML.c:497 (TE)
-  const double sig_max = tm ? -(M + 1.0) * kEps0 * kC / 2.0 / g.n_pml / cos(M_PI / 3) * log(R)
-                            : -(M + 1.0) * kEps0 * kC / 2.0 / g.n_pml * log(R);
+  const double sig_max = tm ? -(M + 1.0) * kEps0 * C0 / 2.0 / g.n_pml / cos(M_PI / 3) * log(R)
+                            : -(M + 1.0) * kEps0 * C0 / 2.0 / g.n_pml * log(R);
   const double e2 = 2 * kEps0, sz = 0;
-  const double mu0 = 1.0 / kC / kC;  // field.h:74
+  const double mu0 = 1.0 / C0 / C0;  // field.h:74
   const double inv_mu = 1.0 / mu0;
   s->inv_mu = inv_mu;
   std::vector<Coef4<double>> txi(s->nxa), txh(s->nxa), tyi(s->ncols), tyh(s->ncols);
   for (int i = 0; i < s->nxa; i++) {
     const double x = i + s->ox;
-    const double si = sig_max * sigma_axis(x, g.n_pml, g.n_x, g.n_px);
-    const double sh = sig_max * sigma_axis(x + 0.5, g.n_pml, g.n_x, g.n_px);
+    const double si = sig_max * sigma_axis(x, g.n_pml, g.n_x, g.n_px, order);
+    const double sh = sig_max * sigma_axis(x + 0.5, g.n_pml, g.n_x, g.n_px, order);
     if (tm) {
       txi[i] = {(e2 - si) / (e2 + si), (e2) / (e2 + si), (e2 + si) / (e2 + sz), (e2 - si) / (e2 + sz)};
       txh[i] = {(e2 - sh) / (e2 + sh), 1.0 / (e2 + sh), 0, 0};
@@ -147,8 +155,8 @@ static int build_tables(fdtd_sim *s)
   }
   for (int j = 0; j < s->ncols; j++) {
     const double y = j + s->ox;
-    const double si = sig_max * sigma_axis(y, g.n_pml, g.n_y, g.n_py);
-    const double sh = sig_max * sigma_axis(y + 0.5, g.n_pml, g.n_y, g.n_py);
+    const double si = sig_max * sigma_axis(y, g.n_pml, g.n_y, g.n_py, order);
+    const double sh = sig_max * sigma_axis(y + 0.5, g.n_pml, g.n_y, g.n_py, order);
     if (tm) {
       tyi[j] = {(e2 - si) / (e2 + si), (e2 + sz) / (e2 + si), e2 + si, e2 - si};
       tyh[j] = {(e2 - sh) / (e2 + sh), (e2) / (e2 + sh) * inv_mu, 0, 0};
@@ -265,11 +273,11 @@ static int build_ntff(fdtd_sim *s)
       // mpiTM_UPML.c:875-876, :894 ; mpiTE_UPML.c:634-635, :654
       const double rad = ang * M_PI / 180.0;
       const double r1x = cos(rad), r1y = sin(rad);
-      for (int c = 0; c < n; c++) row[c] = -(r1x * r2x[c] + r1y * r2y[c]) / kC + g.rf_per_c;
+      for (int c = 0; c < n; c++) row[c] = -(r1x * r2x[c] + r1y * r2y[c]) / s->c0 + g.rf_per_c;
     } else {
       // ntffTM.c:318-368 / ntffTE.c:92-155: shift advanced incrementally along each side
       const double rad = ang * (M_PI / 180.0);
-      const double r1x = cos(rad) / kC, r1y = sin(rad) / kC;
+      const double r1x = cos(rad) / s->c0, r1y = sin(rad) / s->c0;
       int c = 0;
       for (int sd = 0; sd < 4; sd++) {
         int c0 = c;
@@ -353,9 +361,10 @@ extern "C" int fdtd_create(int solver, const fdtd_config *cfg, fdtd_sim **out)
     return fail(FDTD_E_ARG, "precision must be FDTD_F64 or FDTD_F32");
   if (family_of(solver) && cfg->precision != FDTD_F64)
     return fail(FDTD_E_UNSUPPORTED, "the split-field and NS solvers run in FP64 only");
-  for (int q = 0; q < 7; q++)
-    if (cfg->reserved[q]) return fail(FDTD_E_ARG, "reserved fields must be zero");
   if (cfg->flags & ~FDTD_CFG_NO_TIME_NTFF) return fail(FDTD_E_ARG, "unknown config flags %#x", cfg->flags);
+  if (family_of(solver) && (cfg->courant_e4 || cfg->pml_order || cfg->ntff_inset))
+    return fail(FDTD_E_UNSUPPORTED, "the split-field and NS solvers run with the reference's Courant number, "
+                                    "sigma grading and NTFF inset only");
   fdtd_geometry geo;
   int rc = fdtd_geometry_of(cfg, &geo);
   if (rc) return rc;
@@ -371,6 +380,8 @@ extern "C" int fdtd_create(int solver, const fdtd_config *cfg, fdtd_sim **out)
   s->mpi = is_mpi(solver);
   s->family = family_of(solver);
   s->cfg = *cfg;
+  s->c0 = config_courant(*cfg);
+  s->z0 = config_z0(*cfg);
   if (s->family) s->cfg.flags |= FDTD_CFG_NO_TIME_NTFF;  // these solvers have no NTFF
   s->geo = geo;
   s->f32 = cfg->precision == FDTD_F32;
@@ -696,8 +707,8 @@ static SourceStep pulse_step(const fdtd_sim *s, double time, double gap_x, doubl
   SourceStep p{};
   p.kind = 2;
   const double rad = s->cfg.angle_deg * M_PI / 180.0;
-  p.cos_per_c = cos(rad) / kC;
-  p.sin_per_c = sin(rad) / kC;
+  p.cos_per_c = cos(rad) / s->c0;
+  p.sin_per_c = sin(rad) / s->c0;
   const double center_peak =
       (s->geo.n_px / 2.0 + gap_x) * p.cos_per_c + (s->geo.n_py / 2 + gap_y) * p.sin_per_c;
   p.t0 = -center_peak + 500;
@@ -761,7 +772,7 @@ static void enqueue_step(fdtd_sim *s, double time, double ray_coef)
   const StencilView<R> v = view_of<R>(s);
   const NtffView n = ntff_view(s);
   cudaStream_t st = s->stream;
-  const double coef = s->mpi ? 1.0 / (4 * M_PI * kC * 1.0e6) : 1.0;  // mpiTM_UPML.c:852-854
+  const double coef = s->mpi ? 1.0 / (4 * M_PI * s->c0 * 1.0e6) : 1.0;  // mpiTM_UPML.c:852-854
   mark(s);
   if (s->mpi) {
     SourceStep cw{};
@@ -1003,7 +1014,7 @@ static void enqueue_block(fdtd_sim *s, int K)
     t = t + 1.0;
     rc = 1.0 - exp(-pow(0.01 * t, 2));
   }
-  const double coef = 1.0 / (4 * M_PI * kC * 1.0e6);  // mpiTM_UPML.c:852-854
+  const double coef = 1.0 / (4 * M_PI * s->c0 * 1.0e6);  // mpiTM_UPML.c:852-854
   mark(s);
   launch_tblock<R>(v, tb, K, s->tm, st);
   mark(s);
@@ -1600,11 +1611,14 @@ extern "C" int fdtd_spectrum(fdtd_sim *s, double *out)
   v.max_time = s->cfg.step_num;
   v.tm = s->tm ? 1 : 0;
   v.h_u_nm = s->cfg.h_u_nm;
+  v.c0 = s->c0;
+  v.z0 = s->z0;
   v.dir = (const double2 *)s->d_dirs;
   v.twiddle = (const double2 *)s->d_twiddle;
   // ntffTM.c:165 / ntffTE.c:25: 1/(4 pi C) * csqrt(2 pi C / (i w))
-  const std::complex<double> q = std::complex<double>(2 * M_PI * kC, 0.0) / std::complex<double>(0.0, s->geo.omega_s);
-  const std::complex<double> c = (1.0 / (4 * M_PI * kC)) * std::sqrt(q);
+  const std::complex<double> q = std::complex<double>(2 * M_PI * s->c0, 0.0) /
+                                 std::complex<double>(0.0, s->geo.omega_s);
+  const std::complex<double> c = (1.0 / (4 * M_PI * s->c0)) * std::sqrt(q);
   v.coef = make_double2(c.real(), c.imag());
   v.out = (double *)s->d_spec;
   launch_spectrum(v, s->stream);
@@ -1620,8 +1634,9 @@ extern "C" int fdtd_spectrum(fdtd_sim *s, double *out)
 static std::complex<double> spectrum_coef(const fdtd_sim *s)
 {
   // ntffTM.c:165 / ntffTE.c:25: 1/(4 pi C) * csqrt(2 pi C / (i w))
-  const std::complex<double> q = std::complex<double>(2 * M_PI * kC, 0.0) / std::complex<double>(0.0, s->geo.omega_s);
-  return (1.0 / (4 * M_PI * kC)) * std::sqrt(q);
+  const std::complex<double> q = std::complex<double>(2 * M_PI * s->c0, 0.0) /
+                                 std::complex<double>(0.0, s->geo.omega_s);
+  return (1.0 / (4 * M_PI * s->c0)) * std::sqrt(q);
 }
 
 extern "C" int fdtd_dft_enable(fdtd_sim *s, int nlam, const int *lambda_nm)
@@ -1635,7 +1650,7 @@ extern "C" int fdtd_dft_enable(fdtd_sim *s, int nlam, const int *lambda_nm)
   s->dft_frac.clear();
   for (int l : s->dft_lam) {
     if (l <= 0) return fail(FDTD_E_ARG, "wavelength %d nm", l);
-    const double p = kC * s->cfg.h_u_nm * kNfft / l;  // the spectrum's fractional bin (ntffTM.c:227)
+    const double p = s->c0 * s->cfg.h_u_nm * kNfft / l;  // the spectrum's fractional bin (ntffTM.c:227)
     const double idx = floor(p);
     s->dft_frac.push_back(p - idx);
     omega.push_back(2 * M_PI * idx / kNfft);
@@ -1656,6 +1671,22 @@ extern "C" int fdtd_dft_enable(fdtd_sim *s, int nlam, const int *lambda_nm)
   return FDTD_OK;
 }
 
+int fdtd_far_field_of_sums(fdtd_sim *s, const double *d_omega, int nfreq, const double2 *d_S, double2 *d_X)
+{
+  if (!s->d_cells) return fail(FDTD_E_STATE, "no NTFF path (FDTD_CFG_NO_TIME_NTFF)");
+  if (int rc = ensure_farfield(s)) return rc;
+  const std::complex<double> c = spectrum_coef(s);
+  DftView d{};
+  d.omega = d_omega;
+  d.nfreq = nfreq;
+  d.S = const_cast<double2 *>(d_S);
+  launch_dft_farfield(ntff_view(s), d, s->tm ? 1 : 0, s->z0, (const double2 *)s->d_dirs,
+                      make_double2(c.real(), c.imag()), d_X, s->stream);
+  s->launches += 1;
+  CK(cudaGetLastError());
+  return FDTD_OK;
+}
+
 // X[360][2 nlam]: the far-field component's Fourier sum at the two bins of each wavelength
 extern "C" int fdtd_dft_far_field(fdtd_sim *s, double *out_complex)
 {
@@ -1665,7 +1696,7 @@ extern "C" int fdtd_dft_far_field(fdtd_sim *s, double *out_complex)
   if (int rc = ensure_farfield(s)) return rc;
   const std::complex<double> c = spectrum_coef(s);
   const DftView d = dft_view(s);
-  launch_dft_farfield(ntff_view(s), d, s->tm ? 1 : 0, (const double2 *)s->d_dirs, make_double2(c.real(), c.imag()),
+  launch_dft_farfield(ntff_view(s), d, s->tm ? 1 : 0, s->z0, (const double2 *)s->d_dirs, make_double2(c.real(), c.imag()),
                       (double2 *)s->d_dft_X, s->stream);
   s->launches += 1;
   CK(cudaGetLastError());
@@ -1720,6 +1751,7 @@ extern "C" int fdtd_frequency(fdtd_sim *s, double *out)
   f.cy = s->geo.ntff_cy;
   f.k_s = s->geo.k_s;
   f.scale = s->tm ? sqrt((double)s->cfg.h_u_nm) : (double)s->cfg.h_u_nm;  // ntffTM.c:156, ntffTE.c:329
+  f.z0 = s->z0;
   f.dir = (const double2 *)s->d_dirs + 360;
   // ntffTM.c:31 R0 = 1e6 * field_toCellUnit(500); ntffTM.c:82 / ntffTE.c:256 coef
   const double R0 = 1.0e6 * (500.0 / s->cfg.h_u_nm);

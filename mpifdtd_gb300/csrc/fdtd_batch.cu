@@ -22,6 +22,18 @@
 // fields stay in the set of its last block.  The batch does no time-domain
 // NTFF: the far field of a CW instance is fdtd_frequency (ntffTM_Frequency)
 // of its final fields.
+//
+// Broadband mode (fdtd_batch_broadband, TM at 0 degrees): the source is the
+// reference's Gaussian pulse (field.c:224-256) instead of the CW wave, and the
+// far field at many wavelengths comes from one run.  Two more launches per
+// block: before the tiles, a pulse kernel writes each instance's per-level
+// row table of the pulse (at 0 degrees it depends on x and t only; the tile
+// code reads it through the CW path's row table, one table per level) and the
+// phasors e^{i w t} of the block's sample times; after the tiles, a DFT kernel
+// reads the NTFF path samples the tiles left in their line buffers and adds
+// v e^{i w t} of every level into per-instance sums S[2][path][nfreq] (FP64),
+// from which the time-domain NTFF's far field at each frequency follows
+// (fdtd_dft.cu).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -52,6 +64,13 @@ struct BatchInst {
   StencilView<R> v[2];
   TBlockView<R> tb[2];
   int n_steps;
+  // broadband mode (src null: CW)
+  typename Cplx<R>::T *src;  // [K][nxa] pulse rows of the current block (v[p].ex, level stride nxa)
+  double2 *S;                // [2][ncell][nfreq] sum_t v e^{i w t} of the E / H path samples
+  const SurfCell *cells;
+  int ncell;
+  double t0, w, inv_c;       // field.c:224-256: t0 = 500 - centre peak, carrier w_s, cos(0)/C
+  double coef;               // NTFF sample scale 1/(4 pi C R), mpiTM_UPML.c:852-854
 };
 
 constexpr int kBWarps = 4;
@@ -66,7 +85,97 @@ __global__ void batch_source_kernel(BatchInst<R> *inst, const double *omega, int
   const double rc = 1.0 - exp(-pow(0.01 * t, 2.0));  // field.c:312-315
   double sn, cs;
   sincos(omega[i] * t, &sn, &cs);
-  inst[i].tb[clk->q & 1].sc[l] = make_double2(rc * cs, -rc * sn);
+  // a pulse instance carries its whole source in the row table (the pulse has no ramp)
+  inst[i].tb[clk->q & 1].sc[l] = inst[i].src ? make_double2(1.0, 0.0) : make_double2(rc * cs, -rc * sn);
+}
+
+// Broadband: the Gaussian pulse of field.c:224-256 at 0 degrees (cos_per_c =
+// 1/C, sin_per_c = 0, no gap) as per-level row tables: value at array row i
+// (global x = i + ox) and level l (time t + l) = g(r) e^{i r w}, g = exp(-(r/50)^2),
+// r = x/C - (t + l - t0); grid (chunks, instances).  Block (0, 0) also writes
+// the block's DFT phasors P[l][k] = e^{i w_k (t + l - 1)} (the E sample time
+// of level l; the far field adds the H samples' half step).
+template <typename R>
+__global__ void batch_pulse_kernel(BatchInst<R> *inst, int K, const BatchClock *clk, const double *freq, int nfreq,
+                                   double2 *P)
+{
+  using T = typename Cplx<R>::T;
+  const BatchInst<R> &I = inst[blockIdx.y];
+  const double t = clk->t;
+  if (blockIdx.x == 0 && blockIdx.y == 0)
+    for (int q = threadIdx.x; q < K * nfreq; q += blockDim.x) {
+      const int l = q / nfreq, k = q - l * nfreq;
+      double sn, cs;
+      sincos(freq[k] * (t + l - 1.0), &sn, &cs);
+      P[q] = make_double2(cs, sn);
+    }
+  if (!I.src) return;
+  const int nxa = I.v[0].nxa, ox = I.v[0].ox;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < K * nxa; q += gridDim.x * blockDim.x) {
+    const int l = q / nxa, i = q - l * nxa;
+    const double r = (double)(i + ox) * I.inv_c - ((t + l) - I.t0);
+    const double g = exp(-(r / 50.0) * (r / 50.0));
+    double sn, cs;
+    sincos(r * I.w, &sn, &cs);
+    T v;
+    v.x = (R)(g * cs);
+    v.y = (R)(g * sn);
+    I.src[q] = v;
+  }
+}
+
+// Broadband: one warp per (instance, path cell), one lane per frequency.  The
+// E and H samples of every level come from the tiles' line buffers exactly as
+// line_gather_kernel forms them (sign, H average, 1/(4 pi C R)); each lane adds
+// sum_l v_l P[l][k] to the cell's sums.  Runs after both tile kernels of the
+// block and before the clock advances (the parity is the block's).
+template <typename R, int K>
+__global__ void __launch_bounds__(128) batch_dft_kernel(const BatchInst<R> *inst, const BatchClock *clk,
+                                                         const double2 *P, int nfreq)
+{
+  using T = typename Cplx<R>::T;
+  const BatchInst<R> &I = inst[blockIdx.y];
+  if (!I.src) return;
+  const int c = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (c >= I.ncell) return;  // whole warp
+  const int left = I.n_steps - (int)clk->t;
+  if (left <= 0) return;
+  const int nlev = left < K ? left : K;
+  const int p = clk->q & 1;
+  const StencilView<R> &v = I.v[p];
+  const TBlockView<R> &tb = I.tb[p];
+  const SurfCell sc = I.cells[c];
+  const int i = (int)(sc.k / v.P), j = (int)(sc.k % v.P);
+  const int fh = sc.h_slot == 3 ? 1 : 2;  // TM: Hx (bottom/top), Hy (right/left)
+  const int i1 = sc.hoff == -1 ? i : i - 1, j1 = sc.hoff == -1 ? j - 1 : j;
+  double2 ev[K], hv[K];
+#pragma unroll
+  for (int l = 0; l < K; l++) {
+    ev[l] = hv[l] = make_double2(0.0, 0.0);  // levels past nlev add nothing
+    if (l >= nlev) continue;
+    T e = czero<T>(), h0 = czero<T>(), h1 = czero<T>();  // path cells always lie on a sampled line
+    tile::line_get(v, tb, l, 0, i, j, e);
+    tile::line_get(v, tb, l, fh, i, j, h0);
+    tile::line_get(v, tb, l, fh, i1, j1, h1);
+    const double sg = sc.sign;
+    ev[l] = make_double2(sg * (double)e.x * I.coef, sg * (double)e.y * I.coef);
+    hv[l] = make_double2((sg * 0.5) * ((double)h0.x + (double)h1.x) * I.coef,
+                         (sg * 0.5) * ((double)h0.y + (double)h1.y) * I.coef);
+  }
+  for (int k = lane; k < nfreq; k += 32) {
+    double2 *se = I.S + (size_t)c * nfreq + k, *sh = I.S + ((size_t)I.ncell + c) * nfreq + k;
+    double2 ae = *se, ah = *sh;
+#pragma unroll
+    for (int l = 0; l < K; l++) {
+      const double2 ph = P[l * nfreq + k];
+      ae.x = fma(ev[l].x, ph.x, fma(-ev[l].y, ph.y, ae.x));
+      ae.y = fma(ev[l].x, ph.y, fma(ev[l].y, ph.x, ae.y));
+      ah.x = fma(hv[l].x, ph.x, fma(-hv[l].y, ph.y, ah.x));
+      ah.y = fma(hv[l].x, ph.y, fma(hv[l].y, ph.x, ah.y));
+    }
+    *se = ae;
+    *sh = ah;
+  }
 }
 
 __global__ void batch_clock_kernel(BatchClock *clk, int K)
@@ -141,6 +250,14 @@ struct fdtd_batch {
   cudaGraphExec_t graph = nullptr;
   int graph_blocks = 0;
   long long launches = 0;
+  // broadband mode (fdtd_batch_broadband)
+  std::vector<int> bb_lam;      // wavelengths (nm); empty: CW
+  void *d_bb_freq = nullptr;    // [nfreq] radians per step
+  void *d_bb_phase = nullptr;   // [kMaxTBlock][nfreq] phasors of the current block
+  std::vector<void *> bb_src;   // per instance: [kMaxTBlock][nxa] pulse rows (field precision)
+  std::vector<void *> bb_S;     // per instance: [2][ncell][nfreq] DFT sums
+  void *d_bb_X = nullptr;       // [360][nfreq] far-field scratch
+  int max_nxa = 0, max_ncell = 0;
 };
 
 static void batch_free(fdtd_batch *b)
@@ -153,6 +270,11 @@ static void batch_free(fdtd_batch *b)
   cudaFree(b->d_tgen);
   cudaFree(b->d_clock);
   cudaFree(b->d_omega);
+  cudaFree(b->d_bb_freq);
+  cudaFree(b->d_bb_phase);
+  cudaFree(b->d_bb_X);
+  for (void *p : b->bb_src) cudaFree(p);
+  for (void *p : b->bb_S) cudaFree(p);
   if (b->graph) cudaGraphExecDestroy(b->graph);
   if (b->ev_fork) cudaEventDestroy(b->ev_fork);
   if (b->ev_join) cudaEventDestroy(b->ev_join);
@@ -274,8 +396,34 @@ static int batch_descriptors(fdtd_batch *b)
       I.tb[0].out[a] = I.v[1].f[a];
       I.tb[1].out[a] = I.v[0].f[a];
     }
-    for (int p = 0; p < 2; p++) I.tb[p].L = b->rows[i];  // no NTFF lines (col/row null)
+    for (int p = 0; p < 2; p++) I.tb[p].L = b->rows[i];  // CW: no NTFF lines (col/row null)
     I.n_steps = s->cfg.step_num;
+    if (!b->bb_lam.empty()) {  // broadband: pulse rows as the source table, path samples into the line buffers
+      using T = typename Cplx<R>::T;
+      const fdtd_geometry &g = s->geo;
+      const int cj[4] = {g.ntff_bottom - 1, g.ntff_bottom, g.ntff_top - 1, g.ntff_top};
+      const int ri[4] = {g.ntff_left - 1, g.ntff_left, g.ntff_right - 1, g.ntff_right};
+      I.src = (T *)b->bb_src[i];
+      I.S = (double2 *)b->bb_S[i];
+      I.cells = (const SurfCell *)s->d_cells;
+      I.ncell = s->ncell;
+      const double C0 = s->c0;
+      const double cos_per_c = cos(0.0) / C0;  // field.c:230 at 0 degrees
+      I.inv_c = cos_per_c;
+      I.t0 = -((g.n_px / 2.0) * cos_per_c) + 500;  // field.c:231-232
+      I.w = g.omega_s;
+      I.coef = 1.0 / (4 * M_PI * C0 * 1.0e6);
+      for (int p = 0; p < 2; p++) {
+        I.v[p].ex = I.src;
+        I.v[p].src_lstride = s->nxa;
+        I.tb[p].col = (T *)s->d_tbcol;
+        I.tb[p].row = (T *)s->d_tbrow;
+        for (int q = 0; q < 4; q++) {
+          I.tb[p].cj[q] = cj[q];
+          I.tb[p].ri[q] = ri[q];
+        }
+      }
+    }
   }
   BCK(cudaMemcpyAsync(b->d_inst, inst.data(), sizeof(BatchInst<R>) * n, cudaMemcpyHostToDevice, b->stream));
   BCK(cudaStreamSynchronize(b->stream));  // inst is a host temporary
@@ -308,6 +456,17 @@ static int batch_plan(fdtd_batch *b)
     for (const int4 &t : plan.general) tgen.push_back(make_int4(i, t.x, t.y, t.z));
     b->rows[i] = L;
     omega[i] = s->geo.omega_s;
+    if (!b->bb_lam.empty()) {  // broadband buffers: pulse rows, DFT sums, NTFF line buffers
+      const int nfreq = (int)b->bb_lam.size();
+      if (!b->bb_src[i]) BCK(cudaMalloc(&b->bb_src[i], (size_t)kMaxTBlock * s->nxa * s->esize));
+      if (!b->bb_S[i]) BCK(cudaMalloc(&b->bb_S[i], sizeof(double2) * 2 * (size_t)s->ncell * nfreq));
+      if (!s->d_tbcol) {
+        BCK(cudaMalloc(&s->d_tbcol, (size_t)kMaxTBlock * 12 * s->nxa * s->esize));
+        BCK(cudaMalloc(&s->d_tbrow, (size_t)kMaxTBlock * 12 * s->pitch * s->esize));
+      }
+      b->max_nxa = std::max(b->max_nxa, s->nxa);
+      b->max_ncell = std::max(b->max_ncell, s->ncell);
+    }
   }
   // largest tiles first (rows walked = height + 2K), so the warps that take the
   // last tiles of a launch finish together
@@ -348,6 +507,10 @@ static void batch_block(fdtd_batch *b)
   auto *inst = (BatchInst<R> *)b->d_inst;
   auto *clk = (BatchClock *)b->d_clock;
   batch_source_kernel<R><<<(n * K + 127) / 128, 128, 0, st>>>(inst, (const double *)b->d_omega, n, K, clk);
+  const int nfreq = (int)b->bb_lam.size();
+  if (nfreq > 0)
+    batch_pulse_kernel<R><<<dim3((unsigned)((K * b->max_nxa + 255) / 256), (unsigned)n), 256, 0, st>>>(
+        inst, K, clk, (const double *)b->d_bb_freq, nfreq, (double2 *)b->d_bb_phase);
   // the two tile kernels run side by side (fork onto the second stream, join)
   cudaEventRecord(b->ev_fork, st);
   cudaStreamWaitEvent(b->stream2, b->ev_fork, 0);
@@ -359,6 +522,9 @@ static void batch_block(fdtd_batch *b)
     batch_tile_kernel<R, K, false, TM, CPL><<<b->grid_int, 32 * kBWarps, 0, st>>>(inst, (const int4 *)b->d_tint,
                                                                              b->n_int, clk);
   cudaStreamWaitEvent(st, b->ev_join, 0);
+  if (nfreq > 0)
+    batch_dft_kernel<R, K><<<dim3((unsigned)((b->max_ncell + 3) / 4), (unsigned)n), 128, 0, st>>>(
+        inst, clk, (const double2 *)b->d_bb_phase, nfreq);
   batch_clock_kernel<<<1, 1, 0, st>>>((BatchClock *)b->d_clock, K);
 }
 
@@ -428,6 +594,9 @@ extern "C" int fdtd_batch_run(fdtd_batch *b)
   if (int rc = b->f32 ? batch_descriptors<float>(b) : batch_descriptors<double>(b)) return rc;
   BatchClock c0{0.0, 0, {0, 0}};
   BCK(cudaMemcpyAsync(b->d_clock, &c0, sizeof c0, cudaMemcpyHostToDevice, b->stream));
+  for (size_t i = 0; i < b->bb_S.size(); i++)  // broadband: the DFT sums start at zero every run
+    BCK(cudaMemsetAsync(b->bb_S[i], 0, sizeof(double2) * 2 * (size_t)b->sims[i]->ncell * b->bb_lam.size(),
+                        b->stream));
   if (!b->graph) {
     cudaGraph_t g = nullptr;
     BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
@@ -451,7 +620,7 @@ extern "C" int fdtd_batch_run(fdtd_batch *b)
   }
   const int nblocks = (max_n + b->K - 1) / b->K;
   const int reps = (nblocks + b->graph_blocks - 1) / b->graph_blocks;
-  const int per_block = 2 + (b->n_int > 0) + (b->n_gen > 0);
+  const int per_block = 2 + (b->n_int > 0) + (b->n_gen > 0) + (b->bb_lam.empty() ? 0 : 2);
   for (int r = 0; r < reps; r++) BCK(cudaGraphLaunch(b->graph, b->stream));
   b->launches += (long long)reps * b->graph_blocks * per_block;
   BCK(cudaStreamSynchronize(b->stream));
@@ -470,5 +639,76 @@ extern "C" int fdtd_batch_reset(fdtd_batch *b)
   if (!b) return set_error(FDTD_E_ARG, "null batch");
   for (fdtd_sim *s : b->sims)
     if (int rc = fdtd_reset(s)) return rc;
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_batch_broadband(fdtd_batch *b, int nlam, const int *lambda_nm)
+{
+  if (!b || !lambda_nm || nlam < 1 || nlam > 64) return set_error(FDTD_E_ARG, "1..64 wavelengths");
+  if (!b->tm) return set_error(FDTD_E_UNSUPPORTED, "the broadband batch runs MPI_TM_UPML");
+  const fdtd_sim *s0 = b->sims[0];
+  for (const fdtd_sim *s : b->sims) {
+    if (s->cfg.angle_deg != 0) return set_error(FDTD_E_UNSUPPORTED, "the broadband pulse runs at 0 degrees");
+    if (!s->d_cells || s->ncell <= 0)
+      return set_error(FDTD_E_STATE, "broadband instances need the NTFF path (no FDTD_CFG_NO_TIME_NTFF)");
+    if (s->cfg.h_u_nm != s0->cfg.h_u_nm || s->c0 != s0->c0)
+      return set_error(FDTD_E_ARG, "broadband instances share one cell size and Courant number");
+  }
+  std::vector<double> freq(nlam);
+  for (int k = 0; k < nlam; k++) {
+    if (lambda_nm[k] <= 0) return set_error(FDTD_E_ARG, "wavelength %d nm", lambda_nm[k]);
+    const double lambda_s = (double)lambda_nm[k] / s0->cfg.h_u_nm;  // field.c:105-109: w = C k, k = 2 pi / lambda_s
+    freq[k] = s0->c0 * (2 * M_PI / lambda_s);
+  }
+  BCK(cudaStreamSynchronize(b->stream));
+  cudaFree(b->d_bb_freq);
+  cudaFree(b->d_bb_phase);
+  cudaFree(b->d_bb_X);
+  for (void *p : b->bb_src) cudaFree(p);
+  for (void *p : b->bb_S) cudaFree(p);
+  b->d_bb_freq = b->d_bb_phase = b->d_bb_X = nullptr;
+  b->bb_src.assign(b->sims.size(), nullptr);
+  b->bb_S.assign(b->sims.size(), nullptr);
+  b->bb_lam.assign(lambda_nm, lambda_nm + nlam);
+  BCK(cudaMalloc(&b->d_bb_freq, sizeof(double) * nlam));
+  BCK(cudaMemcpy(b->d_bb_freq, freq.data(), sizeof(double) * nlam, cudaMemcpyHostToDevice));
+  BCK(cudaMalloc(&b->d_bb_phase, sizeof(double2) * kMaxTBlock * (size_t)nlam));
+  BCK(cudaMalloc(&b->d_bb_X, sizeof(double2) * 360 * (size_t)nlam));
+  b->planned_k = 0;  // buffers and graph are made again by the next run
+  return FDTD_OK;
+}
+
+extern "C" int fdtd_batch_broadband_spectrum(fdtd_batch *b, int index, double *out)
+{
+  if (!b || !out || index < 0 || index >= (int)b->sims.size()) return set_error(FDTD_E_ARG, "bad instance index");
+  if (b->bb_lam.empty() || !b->bb_S[index]) return set_error(FDTD_E_STATE, "no broadband run (fdtd_batch_broadband)");
+  fdtd_sim *s = b->sims[index];
+  if (s->time != s->cfg.step_num) return set_error(FDTD_E_STATE, "the instance has not run to its step_num");
+  const int nfreq = (int)b->bb_lam.size();
+  if (int rc = fdtd_far_field_of_sums(s, (const double *)b->d_bb_freq, nfreq, (const double2 *)b->bb_S[index],
+                                      (double2 *)b->d_bb_X))
+    return rc;
+  std::vector<double2> X(360 * (size_t)nfreq);
+  BCK(cudaMemcpyAsync(X.data(), b->d_bb_X, sizeof(double2) * X.size(), cudaMemcpyDeviceToHost, s->stream));
+  BCK(cudaStreamSynchronize(s->stream));
+  std::vector<double> freq(nfreq);
+  BCK(cudaMemcpy(freq.data(), b->d_bb_freq, sizeof(double) * nfreq, cudaMemcpyDeviceToHost));
+  // the incident pulse at x = 0 (field.c:224-256), transformed with the samples' e^{i w t}:
+  // dividing by it leaves the response to a unit incident wave, the CW run's steady state
+  const double t0 = -((s->geo.n_px / 2.0) * (cos(0.0) / s->c0)) + 500, w = s->geo.omega_s;
+  for (int k = 0; k < nfreq; k++) {
+    double ar = 0, ai = 0;
+    for (int t = 0; t < s->cfg.step_num; t++) {
+      const double r = -(t - t0), g = exp(-(r / 50.0) * (r / 50.0));
+      const double ph = r * w + freq[k] * (t - 1.0);
+      ar += g * cos(ph);
+      ai += g * sin(ph);
+    }
+    const double a2 = ar * ar + ai * ai;
+    for (int ang = 0; ang < 360; ang++) {
+      const double2 x = X[(size_t)ang * nfreq + k];
+      out[(size_t)k * 360 + ang] = (x.x * x.x + x.y * x.y) / a2;
+    }
+  }
   return FDTD_OK;
 }

@@ -56,15 +56,15 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b)
 
 // X[a][k] = coef sum_{c, f} g e^{i w M} kappa S ; one block per angle, threads over k
 __global__ void dft_farfield_kernel(NtffView n, const double2 *S, const double *omega, int nfreq, int tm,
-                                    const double2 *dir, double2 coef, double2 *X)
+                                    double z0, const double2 *dir, double2 coef, double2 *X)
 {
   const int ang = blockIdx.x;
   const double2 d = dir[ang];
   const double px = -d.y, py = d.x, sz = -1.0;
   // weight of accumulators 0, 1, 2 in the angle's far-field component (spectrum_kernel's combination)
   double g[3];
-  if (tm) { g[0] = -px; g[1] = -py; g[2] = -kZ0 * sz; }
-  else { g[0] = -kZ0 * px; g[1] = -kZ0 * py; g[2] = sz; }
+  if (tm) { g[0] = -px; g[1] = -py; g[2] = -z0 * sz; }
+  else { g[0] = -z0 * px; g[1] = -z0 * py; g[2] = sz; }
   for (int k = threadIdx.x; k < nfreq; k += blockDim.x) {
     const double w = omega[k];
     double sw, cw;
@@ -101,10 +101,10 @@ void launch_dft_accumulate(const NtffView &n, const DftView &d, int nb, double t
       n, d.phasor, d.S, d.nfreq, nb);
 }
 
-void launch_dft_farfield(const NtffView &n, const DftView &d, int tm, const double2 *dir, double2 coef, double2 *X,
-                         cudaStream_t st)
+void launch_dft_farfield(const NtffView &n, const DftView &d, int tm, double z0, const double2 *dir, double2 coef,
+                         double2 *X, cudaStream_t st)
 {
-  dft_farfield_kernel<<<360, 128, 0, st>>>(n, d.S, d.omega, d.nfreq, tm, dir, coef, X);
+  dft_farfield_kernel<<<360, 128, 0, st>>>(n, d.S, d.omega, d.nfreq, tm, z0, dir, coef, X);
 }
 
 }  // namespace fdtd

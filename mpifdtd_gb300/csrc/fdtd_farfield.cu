@@ -35,13 +35,13 @@ __global__ void __launch_bounds__(1024) spectrum_kernel(SpectrumView s)
       if (s.tm) {  // ETH = coef (-Z0 WTH - UPH), WTH = Wz sz, UPH = Ux px + Uy py
         const double2 ux = u0[n], uy = u1[n], wz = u2[n];
         const double uphr = ux.x * px + uy.x * py, uphi = ux.y * px + uy.y * py;
-        w.x = -kZ0 * (wz.x * sz) - uphr;
-        w.y = -kZ0 * (wz.y * sz) - uphi;
+        w.x = -s.z0 * (wz.x * sz) - uphr;
+        w.y = -s.z0 * (wz.y * sz) - uphi;
       } else {     // EPH = coef (-Z0 WPH + UTH), WPH = Wx px + Wy py, UTH = Uz sz
         const double2 wx = u0[n], wy = u1[n], uz = u2[n];
         const double wphr = wx.x * px + wy.x * py, wphi = wx.y * px + wy.y * py;
-        w.x = -kZ0 * wphr + uz.x * sz;
-        w.y = -kZ0 * wphi + uz.y * sz;
+        w.x = -s.z0 * wphr + uz.x * sz;
+        w.y = -s.z0 * wphi + uz.y * sz;
       }
       e.x = s.coef.x * w.x - s.coef.y * w.y;
       e.y = s.coef.x * w.y + s.coef.y * w.x;
@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(1024) spectrum_kernel(SpectrumView s)
   }
   for (int l = threadIdx.x; l <= kLambdaEn - kLambdaSt; l += blockDim.x) {
     const int lam = kLambdaSt + l;
-    double p = kC * s.h_u_nm * kNfft / lam;  // ntffTM.c:227
+    double p = s.c0 * s.h_u_nm * kNfft / lam;  // ntffTM.c:227
     const int idx = (int)floor(p);
     p = p - idx;
     const double2 a = buf[idx], b = buf[idx + 1];
@@ -154,8 +154,8 @@ __global__ void __launch_bounds__(256) frequency_kernel(FrequencyView f)
     // phi component of the bottom/top (x) and right/left (y) sums: -x sin + y cos
     const double pr = -red[2][0] * ry + red[4][0] * rx, pi = -red[3][0] * ry + red[5][0] * rx;
     double br, bi;
-    if (!te) { br = kZ0 * red[0][0] + pr; bi = kZ0 * red[1][0] + pi; }   // Z0 N_z + L_phi
-    else     { br = kZ0 * pr - red[0][0]; bi = kZ0 * pi - red[1][0]; }    // Z0 N_phi - L_z
+    if (!te) { br = f.z0 * red[0][0] + pr; bi = f.z0 * red[1][0] + pi; }   // Z0 N_z + L_phi
+    else     { br = f.z0 * pr - red[0][0]; bi = f.z0 * pi - red[1][0]; }    // Z0 N_phi - L_z
     f.out[ang] = make_double2((f.coef.x * br - f.coef.y * bi) * f.scale, (f.coef.x * bi + f.coef.y * br) * f.scale);
   }
 }

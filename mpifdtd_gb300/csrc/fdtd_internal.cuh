@@ -51,6 +51,10 @@ struct StencilView {
   const Coef4<R> *tx_i, *tx_h;  // indexed by row i (sigma_x at x, x+1/2)
   const Coef4<R> *ty_i, *ty_h;  // indexed by column j (sigma_y at y, y+1/2)
   const typename Cplx<R>::T *ex, *ey;  // CW source phase tables e^{i x kcos}, e^{i y ksin} in R
+  // Elements between the ex tables of consecutive levels of a blocked launch:
+  // 0 (one table for every level, the CW source) or nxa (a batched Gaussian
+  // pulse at 0 degrees, whose row table changes with the level's time).
+  int src_lstride;
   int P, nxa, ni, nj, ox;
   int in_x0, in_x1, in_y0, in_y1;  // interior (all sigma = 0): x in [in_x0,in_x1)
   int rows;                        // rows per thread of the stencil kernels (1, 2, 4, 8)
@@ -163,6 +167,7 @@ namespace fdtd {
 struct SpectrumView {
   const double2 *acc[3];   // NTFF accumulators incl. guard
   int array_size, max_time, tm, h_u_nm;
+  double c0, z0;           // Courant number and impedance (field.h:70, :75 by default)
   const double2 *dir;      // [360] (cos phi, sin phi)
   const double2 *twiddle;  // [4096] e^{+2 pi i k / 8192}
   double2 coef;            // 1/(4 pi C) sqrt(2 pi C / (i w))  (ntffTM.c:165)
@@ -176,6 +181,7 @@ struct FrequencyView {
   int f32;                 // fields are float2 (FP32 mode) instead of double2
   int P, ox, lt, rt, bm, tp;
   double cx, cy, k_s, scale;  // scale: sqrt(h_u_nm) (TM), h_u_nm (TE)
+  double z0;               // impedance (field.h:75 by default)
   const double2 *dir;      // [360] (cos, sin)
   double2 coef;            // csqrt(i k/(8 pi R0)) e^{i k R0}  (ntffTM.c:82, ntffTE.c:256)
   double2 *out;            // [360]
@@ -190,8 +196,15 @@ struct DftView {
   double2 *S;           // [2][ncell][nfreq] sum_t v_c(t) e^{i w t} (E samples, H samples)
 };
 void launch_dft_accumulate(const NtffView &n, const DftView &d, int nb, double t0, cudaStream_t st);
-void launch_dft_farfield(const NtffView &n, const DftView &d, int tm, const double2 *dir, double2 coef, double2 *X,
-                         cudaStream_t st);
+void launch_dft_farfield(const NtffView &n, const DftView &d, int tm, double z0, const double2 *dir, double2 coef,
+                         double2 *X, cudaStream_t st);
+// The settings of a configuration that the reference hard-codes (fdtd_config:
+// courant_e4, pml_order, ntff_inset; 0 = the reference's value).
+inline double config_courant(const fdtd_config &c) { return c.courant_e4 > 0 ? c.courant_e4 / 1.0e4 : kC; }
+// field.h:75 writes sqrt(mu0/eps0) = 1/C as the literal 1.41422712488 for C = 0.7071
+inline double config_z0(const fdtd_config &c) { return c.courant_e4 > 0 ? 1.0 / config_courant(c) : kZ0; }
+inline int config_pml_order(const fdtd_config &c) { return c.pml_order > 0 ? c.pml_order : 2; }
+inline int config_ntff_inset(const fdtd_config &c) { return c.ntff_inset > 0 ? c.ntff_inset : 5; }
 void launch_frequency(const FrequencyView &f, cudaStream_t st);
 // fdtd_split.cu: split-field PML and NS-FDTD solvers (one step = two launches)
 struct SplitView {

@@ -16,6 +16,7 @@ struct fdtd_sim {
   bool coef_dirty = true;       // the permittivity changed since the coefficients were made
   fdtd_config cfg{};
   fdtd_geometry geo{};
+  double c0 = fdtd::kC, z0 = fdtd::kZ0;  // Courant number, impedance (config_courant, config_z0)
   // array frame (see fdtd_internal.cuh)
   int ox = 0, ni = 0, nj = 0, nxa = 0, ncols = 0, pitch = 0;
   size_t esize = 0;
@@ -84,3 +85,10 @@ int fdtd_plan_tiles(const fdtd_sim *s, int K, int L, int cpl, TilePlan *plan);
 // The stencil view of a simulation's current field set (fdtd_api.cu).
 template <typename R>
 fdtd::StencilView<R> fdtd_view_of(fdtd_sim *s);
+
+// Far field X[360][nfreq] (device) of the running-DFT sums S[2][ncell][nfreq]
+// (device, E then H path samples, phasors of the E sample times) at the
+// frequencies omega[nfreq] (device, radians per step), with the simulation's
+// own path, shifts and spectrum coefficient (fdtd_api.cu; the broadband batch
+// keeps its sums outside the simulation).
+int fdtd_far_field_of_sums(fdtd_sim *s, const double *d_omega, int nfreq, const double2 *d_S, double2 *d_X);

@@ -53,28 +53,6 @@ __global__ void __launch_bounds__(32 * kWarps, 3) tblock_general_kernel(StencilV
   else te_tile<R, K, true, CPL>(v, tb, t4.x, t4.y, t4.z, K);
 }
 
-// NTFF surface samples of level lev from the line buffers (zero on the halo ring)
-template <typename R>
-__device__ __forceinline__ bool line_get(const StencilView<R> &v, const TBlockView<R> &tb, int lev, int f, int i,
-                                         int j, typename Cplx<R>::T &out)
-{
-  if (i < 1 || i > v.ni || j < 1 || j > v.nj) {
-    out = czero<typename Cplx<R>::T>();
-    return true;
-  }
-  for (int q = 0; q < 4; q++)
-    if (j == tb.cj[q]) {
-      out = tb.col[((size_t)(lev * 4 + q) * 3 + f) * v.nxa + i];
-      return true;
-    }
-  for (int q = 0; q < 4; q++)
-    if (i == tb.ri[q]) {
-      out = tb.row[((size_t)(lev * 4 + q) * 3 + f) * v.P + j];
-      return true;
-    }
-  return false;
-}
-
 // Same values as ntff_gather_kernel, for the K steps of one blocked launch.
 template <typename R>
 __global__ void line_gather_kernel(StencilView<R> v, TBlockView<R> tb, NtffView n, double coef, int slot0, int tm)
@@ -89,8 +67,8 @@ __global__ void line_gather_kernel(StencilView<R> v, TBlockView<R> tb, NtffView 
   const int fh = tm ? (sc.h_slot == 3 ? 1 : 2) : 2;     // TM: Hx / Hy ; TE: Hz
   const int i1 = sc.hoff == -1 ? i : i - 1, j1 = sc.hoff == -1 ? j - 1 : j;
   T e, h0, h1;
-  if (!line_get(v, tb, lev, fe, i, j, e) || !line_get(v, tb, lev, fh, i, j, h0) ||
-      !line_get(v, tb, lev, fh, i1, j1, h1)) {
+  if (!tile::line_get(v, tb, lev, fe, i, j, e) || !tile::line_get(v, tb, lev, fh, i, j, h0) ||
+      !tile::line_get(v, tb, lev, fh, i1, j1, h1)) {
     atomicOr(n.status, kStatusNtffRange);
     return;
   }

@@ -32,7 +32,7 @@ struct NoAllocPath {
   int i0, i1, j0, j1;        // path ranges clipped as mpiTM_UPML.c:886-887, :926-927
   int bm, tp, lt, rt, cx, cy;
   int nb, nr, ncell;         // cells on the bottom (= top) and right (= left) sides
-  double rf, coef;
+  double rf, coef, c0;       // RFperC, 1/(4 pi C R), Courant number
   long long array_size, lo, hi;  // valid accumulator indices [lo, hi) around element 0
 };
 
@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(256) noalloc_deposit_kernel(NoAllocPath p, con
   // -(r1x r2x + r1y r2y) / C + RFperC, rounded step by step as the reference
   const double2 d = g_noalloc_dir[ang];
   const double dot = __dadd_rn(__dmul_rn(d.x, r2x), __dmul_rn(d.y, r2y));
-  const double sh = __dadd_rn(-__ddiv_rn(dot, kC), p.rf);
+  const double sh = __dadd_rn(-__ddiv_rn(dot, p.c0), p.rf);
   double2 *acc[3] = {u0, u1, u2};
   const int uid = p.tm ? (horiz ? 0 : 1) : 2;
   const int wid = p.tm ? 2 : (horiz ? 0 : 1);
@@ -200,7 +200,8 @@ extern "C" int fdtd_ntff_step_noalloc(const fdtd_ntff_step_args *a, void *stream
     return set_error(FDTD_E_ARG, "NTFF path of %d cells exceeds the static scratch (%d cells)", p.ncell,
                      FDTD_NOALLOC_MAX_PATH);
   p.rf = g.rf_per_c;
-  p.coef = 1.0 / (4 * M_PI * kC * 1.0e6);  // mpiTM_UPML.c:852-854
+  p.c0 = config_courant(a->cfg);
+  p.coef = 1.0 / (4 * M_PI * p.c0 * 1.0e6);  // mpiTM_UPML.c:852-854
   p.array_size = g.array_size;
   p.lo = -FDTD_NTFF_GUARD;
   p.hi = 360LL * g.array_size + FDTD_NTFF_GUARD;

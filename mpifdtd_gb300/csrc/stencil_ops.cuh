@@ -37,6 +37,23 @@ __device__ __forceinline__ void cw_add(const StencilView<R> &v, double s_re, dou
   e.y = e.y + qi;
 }
 
+// The same increment in a blocked launch, at level lvl: the row table of that
+// level (v.src_lstride = 0 for the CW source: one table for every level).
+template <typename R>
+__device__ __forceinline__ void cw_add_level(const StencilView<R> &v, double s_re, double s_im, int lvl, int i,
+                                             int j, R ie, typename Cplx<R>::T &e)
+{
+  const typename Cplx<R>::T ex = v.ex[(size_t)lvl * v.src_lstride + i], ey = v.ey[j];
+  const R sr = (R)s_re, si = (R)s_im;
+  const R pr = ex.x * ey.x - ex.y * ey.y;
+  const R pi = ex.x * ey.y + ex.y * ey.x;
+  const R amp = ie - (R)1;
+  const R qr = (pr * sr - pi * si) * amp;
+  const R qi = (pr * si + pi * sr) * amp;
+  e.x = e.x + qr;
+  e.y = e.y + qi;
+}
+
 template <typename R>
 __device__ __forceinline__ void cw_source(const StencilView<R> &v, const SourceStep &s, int i, int j, R ie,
                                           typename Cplx<R>::T &e)

@@ -295,7 +295,7 @@ __device__ __forceinline__ void tm_tile(const StencilView<R> &v, const TBlockVie
           T ez = dz;
           if (!is_one(en[q].ie)) {
             ez = cscale(dz, en[q].ie);
-            cw_add<R>(v, tb.sc[l - 1].x, tb.sc[l - 1].y, e, j + q, en[q].ie, ez);
+            cw_add_level<R>(v, tb.sc[l - 1].x, tb.sc[l - 1].y, l - 1, e, j + q, en[q].ie, ez);
           }
           en[q].e = ez;
         }
@@ -513,7 +513,7 @@ __device__ __forceinline__ void te_tile(const StencilView<R> &v, const TBlockVie
           if (!is_one(en[q].iex)) ex = cscale(dx, en[q].iex);
           if (!is_one(en[q].iey)) {
             ey = cscale(dy, en[q].iey);
-            cw_add<R>(v, tb.sc[l - 1].x, tb.sc[l - 1].y, e, j + q, en[q].iey, ey);
+            cw_add_level<R>(v, tb.sc[l - 1].x, tb.sc[l - 1].y, l - 1, e, j + q, en[q].iey, ey);
           }
           en[q].ex = ex;
           en[q].ey = ey;
@@ -599,6 +599,28 @@ __device__ __forceinline__ void te_tile(const StencilView<R> &v, const TBlockVie
       }
     }
   }
+}
+
+// NTFF surface samples of level lev from the line buffers (zero on the halo ring)
+template <typename R>
+__device__ __forceinline__ bool line_get(const StencilView<R> &v, const TBlockView<R> &tb, int lev, int f, int i,
+                                         int j, typename Cplx<R>::T &out)
+{
+  if (i < 1 || i > v.ni || j < 1 || j > v.nj) {
+    out = czero<typename Cplx<R>::T>();
+    return true;
+  }
+  for (int q = 0; q < 4; q++)
+    if (j == tb.cj[q]) {
+      out = tb.col[((size_t)(lev * 4 + q) * 3 + f) * v.nxa + i];
+      return true;
+    }
+  for (int q = 0; q < 4; q++)
+    if (i == tb.ri[q]) {
+      out = tb.row[((size_t)(lev * 4 + q) * 3 + f) * v.P + j];
+      return true;
+    }
+  return false;
 }
 
 }  // namespace tile

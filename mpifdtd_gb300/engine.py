@@ -36,7 +36,11 @@ class FdtdError(RuntimeError):
 
 @dataclass
 class FieldInfo:
-    """field.h:20-28 FieldInfo (physical sizes in nm)."""
+    """field.h:20-28 FieldInfo (physical sizes in nm), plus three settings the
+    reference hard-codes (0 keeps the reference's value): the Courant number
+    (C_0_S = 0.7071, field.h:70; given to the engine in units of 1e-4), the
+    sigma grading exponent (2, field.c:259-283) and the NTFF path's distance
+    from the PML in cells (5, field.c:136-139)."""
     width_nm: int
     height_nm: int
     h_u_nm: int
@@ -44,6 +48,9 @@ class FieldInfo:
     lambda_nm: int
     angle_deg: int
     step_num: int
+    courant: float = 0.0
+    pml_order: int = 0
+    ntff_inset: int = 0
 
     def astuple(self):
         return (self.width_nm, self.height_nm, self.h_u_nm, self.pml, self.lambda_nm,
@@ -52,7 +59,8 @@ class FieldInfo:
 
 class _Config(C.Structure):
     _fields_ = [(n, C.c_int) for n in ("width_nm", "height_nm", "h_u_nm", "pml", "lambda_nm",
-                                       "angle_deg", "step_num", "precision", "flags")] + [("reserved", C.c_int * 7)]
+                                       "angle_deg", "step_num", "precision", "flags", "courant_e4",
+                                       "pml_order", "ntff_inset")] + [("reserved", C.c_int * 4)]
 
 
 class Geometry(C.Structure):
@@ -124,6 +132,8 @@ def load():
         "fdtd_batch_run": (I, [P]),
         "fdtd_batch_reset": (I, [P]),
         "fdtd_batch_launch_count": (C.c_longlong, [P]),
+        "fdtd_batch_broadband": (I, [P, I, C.POINTER(I)]),
+        "fdtd_batch_broadband_spectrum": (I, [P, I, dp]),
         "fdtd_last_error": (C.c_char_p, []),
         "fdtd_version": (C.c_char_p, []),
     }
@@ -152,6 +162,10 @@ def _config(fi: FieldInfo, precision: int, flags: int = 0) -> _Config:
     (c.width_nm, c.height_nm, c.h_u_nm, c.pml, c.lambda_nm, c.angle_deg, c.step_num) = fi.astuple()
     c.precision = precision
     c.flags = flags
+    e4 = round(fi.courant * 1e4)
+    if abs(fi.courant * 1e4 - e4) > 1e-6:
+        raise ValueError(f"Courant number {fi.courant} is not a multiple of 1e-4")
+    c.courant_e4, c.pml_order, c.ntff_inset = e4, fi.pml_order, fi.ntff_inset
     return c
 
 
@@ -441,6 +455,20 @@ class Batch:
     def run(self):
         """Every instance from time 0 to its own step_num."""
         _check(self.lib.fdtd_batch_run(self.h))
+
+    def broadband(self, lambdas_nm):
+        """Gaussian-pulse source and a running DFT of the NTFF path at these
+        wavelengths (fdtd_batch_broadband); call before run()."""
+        lam = np.ascontiguousarray(lambdas_nm, dtype=np.int32)
+        self._bb_n = int(lam.size)
+        _check(self.lib.fdtd_batch_broadband(self.h, self._bb_n, lam.ctypes.data_as(C.POINTER(C.c_int))))
+
+    def broadband_spectrum(self, index: int) -> np.ndarray:
+        """Far-field intensity [n_lambda, 360] of instance `index` per unit
+        incident wave (fdtd_batch_broadband_spectrum); angle a is direction a."""
+        out = np.empty((self._bb_n, 360))
+        _check(self.lib.fdtd_batch_broadband_spectrum(self.h, int(index), _dptr(out)))
+        return out
 
     def reset(self):
         _check(self.lib.fdtd_batch_reset(self.h))

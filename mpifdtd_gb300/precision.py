@@ -7,9 +7,12 @@ come with its error against FP64 on the same input; this module measures it:
 * field relative L2 of each field component after `steps` steps,
 * relative L2 of the NTFF accumulators (the time-domain far field),
 * far-field error in dB: 10 log10 of the ratio of the FP32 and FP64 far-field
-  intensity per angle, from the frequency-domain NTFF (TM) or, where the run
-  fits the reference's 8192-point spectrum, from the spectrum at the source
-  wavelength; reported as the maximum over angles with non-negligible power.
+  intensity per angle, from the frequency-domain NTFF of the final fields
+  (ntffTM_Frequency / ntffTE_Frequency; MPI solvers) or the time-domain
+  far-field energy per angle, and where the run fits the reference's
+  8192-point spectrum from the spectrum at the source wavelength; reported as
+  the maximum over angles with non-negligible power, with the relative L2 of
+  the complex frequency-domain far field beside it.
 """
 from __future__ import annotations
 
@@ -52,8 +55,10 @@ def compare_precisions(solver, fi, model, steps, eps=None):
     for w, n in enumerate(names):
         rep["field_rel_l2"][n] = _rel(a.field(w), b.field(w))
     rep["ntff_rel_l2"] = max(_rel(a.ntff(w), b.ntff(w)) for w in range(3))
-    if a.tm:   # frequency-domain far field at the source wavelength (ntffTM_Frequency)
-        rep["farfield_db_max"] = _db_max(np.abs(a.frequency()) ** 2, np.abs(b.frequency()) ** 2)
+    if a.mpi:  # frequency-domain far field at the source wavelength (ntffTM_Frequency / ntffTE_Frequency)
+        f32, f64 = a.frequency(), b.frequency()
+        rep["farfield_db_max"] = _db_max(np.abs(f32) ** 2, np.abs(f64) ** 2)
+        rep["farfield_rel_l2"] = _rel(f32, f64)
     else:      # time-domain far-field energy per angle
         e32 = sum(np.sum(np.abs(a.ntff(w).reshape(360, -1)) ** 2, axis=1) for w in range(3))
         e64 = sum(np.sum(np.abs(b.ntff(w).reshape(360, -1)) ** 2, axis=1) for w in range(3))

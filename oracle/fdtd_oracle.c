@@ -81,6 +81,8 @@ struct of_sim {
   double *eps[3];
   cplx *nt_base[3], *nt[3];
   int skip_ntff;                         /* of_bench_opts: leave the time-domain NTFF out (timing only) */
+  double c0, mu0, z0;                    /* Courant number, 1/C^2, impedance (field.h:70-75 by default) */
+  int pml_m, inset;                      /* sigma grading exponent, NTFF inset (field.c:259-283, :136-139) */
 };
 
 /* ---------------------------------------------------------------- models */
@@ -286,18 +288,19 @@ static void model_init(of_sim *s)
 
 /* ---------------------------------------------------------------- field */
 
-/* field.c:259-283 */
+/* field.c:259-283: pow(t, M), M = 2 in the reference (t * t, the same value) */
+static double grade(const of_sim *s, double t) { return s->pml_m == 2 ? t * t : pow(t, (double)s->pml_m); }
 static double sigma_x(const of_sim *s, double x)
 {
-  if (x < s->n_pml) { double t = 1.0 * (s->n_pml - x) / s->n_pml; return t * t; }
+  if (x < s->n_pml) return grade(s, 1.0 * (s->n_pml - x) / s->n_pml);
   if (x < s->n_x + s->n_pml) return 0;
-  double t = 1.0 * (x - (s->n_px - s->n_pml - 1)) / s->n_pml; return t * t;
+  return grade(s, 1.0 * (x - (s->n_px - s->n_pml - 1)) / s->n_pml);
 }
 static double sigma_y(const of_sim *s, double y)
 {
-  if (y < s->n_pml) { double t = 1.0 * (s->n_pml - y) / s->n_pml; return t * t; }
+  if (y < s->n_pml) return grade(s, 1.0 * (s->n_pml - y) / s->n_pml);
   if (y < s->n_y + s->n_pml) return 0.0;
-  double t = 1.0 * (y - (s->n_py - s->n_pml - 1)) / s->n_pml; return t * t;
+  return grade(s, 1.0 * (y - (s->n_py - s->n_pml - 1)) / s->n_pml);
 }
 
 static void field_setup(of_sim *s)
@@ -310,16 +313,16 @@ static void field_setup(of_sim *s)
   s->n_y = s->n_py - 2 * s->n_pml;
   s->lambda_s = (double)f->lambda_nm / f->h_u_nm;
   s->k_s = 2 * M_PI / s->lambda_s;
-  s->w_s = OF_C * s->k_s;
+  s->w_s = s->c0 * s->k_s;
   s->time = 0;
   s->ray_coef = 0;
   s->max_time = f->step_num;
   s->cx = s->n_px / 2;
   s->cy = s->n_py / 2;
-  s->top = s->n_py - s->n_pml - 5;
-  s->bottom = s->n_pml + 5;
-  s->left = s->n_pml + 5;
-  s->right = s->n_px - s->n_pml - 5;
+  s->top = s->n_py - s->n_pml - s->inset;
+  s->bottom = s->n_pml + s->inset;
+  s->left = s->n_pml + s->inset;
+  s->right = s->n_px - s->n_pml - s->inset;
   double len = (s->top - s->bottom) / 2;
   s->rf = len * 2;
   s->array_size = (int)(s->max_time + 2 * s->rf);
@@ -338,12 +341,12 @@ static void *zalloc(size_t n)
 
 static void coefficients(of_sim *s)
 {
-  const double R = 1.0e-8, M = 2.0;
+  const double R = 1.0e-8, M = (double)s->pml_m;
   double sig_max;
   if (s->tm) /* mpiTM_UPML.c:672, fdtdTM_upml.c:232 (extra 1/cos(pi/3)) */
-    sig_max = -(M + 1.0) * OF_EPS0 * OF_C / 2.0 / s->n_pml / cos(M_PI / 3) * log(R);
+    sig_max = -(M + 1.0) * OF_EPS0 * s->c0 / 2.0 / s->n_pml / cos(M_PI / 3) * log(R);
   else       /* mpiTE_UPML.c:497, fdtdTE_upml.c:369 */
-    sig_max = -(M + 1.0) * OF_EPS0 * OF_C / 2.0 / s->n_pml * log(R);
+    sig_max = -(M + 1.0) * OF_EPS0 * s->c0 / 2.0 / s->n_pml * log(R);
   const double e2 = 2 * OF_EPS0, sz = 0;
   /* MPI: cells 1..n-2 of the padded array (global x=i-1); serial: every cell */
   int i0 = s->mpi ? 1 : 0, i1 = s->mpi ? s->nx - 1 : s->nx;
@@ -424,8 +427,18 @@ of_sim *of_create(int solver, const of_field_info *fi, const of_model *m)
   s->family = (solver == OF_TM_2D || solver == OF_TE_2D) ? 1 : (solver == OF_NS_TM_2D || solver == OF_NS_TE_2D) ? 2 : 0;
   s->fi = *fi;
   if (m) s->model = *m;
+  if ((s->family && (fi->courant != 0 || fi->pml_order || fi->ntff_inset)) || fi->courant < 0 ||
+      fi->courant > 0.7071 || fi->pml_order < 0 || fi->ntff_inset < 0) { free(s); return NULL; }
+  s->c0 = fi->courant > 0 ? fi->courant : OF_C;
+  s->mu0 = 1.0 / s->c0 / s->c0;                            /* field.h:74 */
+  s->z0 = fi->courant > 0 ? 1.0 / fi->courant : OF_Z0;     /* field.h:75 (the literal for 0.7071) */
+  s->pml_m = fi->pml_order > 0 ? fi->pml_order : 2;
+  s->inset = fi->ntff_inset > 0 ? fi->ntff_inset : 5;
   field_setup(s);
-  if (s->n_pml <= 0 || s->n_px < 2 * (s->n_pml + 6) || s->n_py < 2 * (s->n_pml + 6)) { free(s); return NULL; }
+  if (s->n_pml <= 0 || s->n_px < 2 * (s->n_pml + s->inset + 1) || s->n_py < 2 * (s->n_pml + s->inset + 1)) {
+    free(s);
+    return NULL;
+  }
   model_init(s);
   s->nx = s->mpi ? s->n_px + 2 : s->n_px;
   s->ny = s->mpi ? s->n_py + 2 : s->n_py;
@@ -495,8 +508,8 @@ static void tm_mb_h(of_sim *s)     /* mpiTM_UPML.c:491-530 / fdtdTM_upml.c:181-2
   for (int i = 1; i < s->nx - 1; i++)
     for (int j = 1; j < ny - 1; j++) {
       int k = i * ny + j;
-      Hx[k] = Bx[k] / OF_MU0;
-      Hy[k] = By[k] / OF_MU0;
+      Hx[k] = Bx[k] / s->mu0;
+      Hy[k] = By[k] / s->mu0;
     }
 }
 
@@ -539,7 +552,7 @@ static void te_mb_h(of_sim *s)     /* mpiTE_UPML.c:377-399 / fdtdTE_upml.c:293-3
       Bz[k] = c[12][k] * Bz[k] + c[13][k] * Mz[k] - c[14][k] * now;
     }
   for (int i = 1; i < s->nx - 1; i++)
-    for (int j = 1; j < ny - 1; j++) { int k = i * ny + j; Hz[k] = Bz[k] / OF_MU0; }
+    for (int j = 1; j < ny - 1; j++) { int k = i * ny + j; Hz[k] = Bz[k] / s->mu0; }
 }
 
 /* ---------------------------------------------------------------- sources */
@@ -568,7 +581,7 @@ static void pulse_source(of_sim *s, cplx *p, const double *eps, double gapX, dou
 {
   double t = s->time, w = s->w_s;
   double rad = s->fi.angle_deg * M_PI / 180.0;
-  double cos_per_c = cos(rad) / OF_C, sin_per_c = sin(rad) / OF_C;
+  double cos_per_c = cos(rad) / s->c0, sin_per_c = sin(rad) / s->c0;
   const double beam_width = 50;
   const double center_peak = (s->n_px / 2.0 + gapX) * cos_per_c + (s->n_py / 2 + gapY) * sin_per_c;
   const double t0 = -center_peak + 500;
@@ -607,7 +620,7 @@ static inline void deposit(cplx *U, int stp, double time, double shift, cplx v, 
  * serial one in global coordinates. */
 static void ntff_mpi(of_sim *s)
 {
-  const double C = OF_C, R = 1.0e6;
+  const double C = s->c0, R = 1.0e6;
   const double coef = 1.0 / (4 * M_PI * C * R);
   const int cx = s->n_px / 2, cy = s->n_py / 2, ny = s->ny;
   const double timeE = s->time - 1, timeH = s->time - 0.5;
@@ -688,7 +701,7 @@ static void ntff_serial(of_sim *s)
   const int rb = s->right * ny + s->bottom, rtp = s->right * ny + s->top;
   for (int ang = 0; ang < 360; ang++) {
     double rad = ang * (M_PI / 180.0);
-    double r1x = cos(rad) / OF_C, r1y = sin(rad) / OF_C;
+    double r1x = cos(rad) / s->c0, r1y = sin(rad) / s->c0;
     const int stp = ang * s->array_size;
     if (s->tm) {
       cplx *Ez = s->f[0], *Hx = s->f[3], *Hy = s->f[6];
@@ -1051,7 +1064,7 @@ int of_time_output(of_sim *s, double *out)
   if (s->family) return -1;  /* no NTFF */
   const int maxTime = (int)s->max_time;
   if (maxTime > OF_NFFT) return -1;
-  const double complex coef = 1.0 / (4 * M_PI * OF_C) * csqrt(2 * M_PI * OF_C / (I * s->w_s));
+  const double complex coef = 1.0 / (4 * M_PI * s->c0) * csqrt(2 * M_PI * s->c0 / (I * s->w_s));
   cplx *buf = (cplx *)malloc(sizeof(cplx) * OF_NFFT);
   for (int ang = 0; ang < 360; ang++) {
     double phi = ang * (M_PI / 180.0), theta = 0;
@@ -1063,17 +1076,17 @@ int of_time_output(of_sim *s, double *out)
       if (s->tm) {
         cplx Ux = s->nt[0][k + i], Uy = s->nt[1][k + i], Wz = s->nt[2][k + i];
         cplx WTH = Wz * sz, UPH = Ux * px + Uy * py;
-        buf[i] = coef * (-OF_Z0 * WTH - UPH);                 /* E_theta */
+        buf[i] = coef * (-s->z0 * WTH - UPH);                 /* E_theta */
       } else {
         cplx Wx = s->nt[0][k + i], Wy = s->nt[1][k + i], Uz = s->nt[2][k + i];
         cplx WPH = Wx * px + Wy * py, UTH = Uz * sz;
-        buf[i] = coef * (-OF_Z0 * WPH + UTH);                 /* E_phi */
+        buf[i] = coef * (-s->z0 * WPH + UTH);                 /* E_phi */
         (void)sx; (void)sy;
       }
     }
     fft_pos(buf, OF_NFFT);
     for (int lam = OF_LAMBDA_ST; lam <= OF_LAMBDA_EN; lam++) {
-      double p = OF_C * s->fi.h_u_nm * OF_NFFT / lam;
+      double p = s->c0 * s->fi.h_u_nm * OF_NFFT / lam;
       int idx = (int)floor(p);
       p = p - idx;
       double n0 = creal(buf[idx]) * creal(buf[idx]) + cimag(buf[idx]) * cimag(buf[idx]);
@@ -1123,7 +1136,7 @@ static void frequency_te(const of_sim *s, const cplx *Ex, const cplx *Ey, const 
       Ny += 0.5 * (Hz[k] + Hz[k - NY]) * e; Lz += Ey[k] * e;
     }
     cplx Nphi = -Nx * sin(rad) + Ny * cos(rad);
-    cplx r = coef * (OF_Z0 * Nphi - Lz) * s->fi.h_u_nm;
+    cplx r = coef * (s->z0 * Nphi - Lz) * s->fi.h_u_nm;
     out[2 * ang] = creal(r); out[2 * ang + 1] = cimag(r);
   }
 }
@@ -1177,7 +1190,7 @@ int of_frequency(of_sim *s, double *out)
       Nz -= 0.5 * (Hy[k] + Hy[k - NY]) * e; Ly -= Ez[k] * e;
     }
     cplx Lphi = -Lx * sin(rad) + Ly * cos(rad);
-    cplx r = coef * (OF_Z0 * Nz + Lphi) * sqrt((double)s->fi.h_u_nm);
+    cplx r = coef * (s->z0 * Nz + Lphi) * sqrt((double)s->fi.h_u_nm);
     out[2 * ang] = creal(r); out[2 * ang + 1] = cimag(r);
   }
   for (int q = 0; q < 3; q++) free(g[q]);

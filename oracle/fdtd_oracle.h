@@ -28,6 +28,14 @@ enum { OF_MODEL_NONE = 0, OF_MODEL_CIRCLE = 1, OF_MODEL_MORPHO = 2, OF_MODEL_DIS
 
 typedef struct of_field_info {      /* field.h:20-28 FieldInfo */
   int width_nm, height_nm, h_u_nm, pml, lambda_nm, angle_deg, step_num;
+  /* Settings the reference hard-codes, 0 = the reference's value (UPML
+   * solvers only; the split-field / NS solvers refuse others):
+   * courant: C_0_S = 0.7071 (field.h:70), which also sets MU_0_S = 1/C^2 and
+   * Z_0_S = 1/C (field.h:74-75); pml_order: the sigma grading exponent M = 2
+   * (field.c:259-283); ntff_inset: NTFF path 5 cells inside the PML
+   * (field.c:136-139). */
+  double courant;
+  int pml_order, ntff_inset;
 } of_field_info;
 
 /* circle: p = {radius_nm, eps (<=0: N=1.6 default)}

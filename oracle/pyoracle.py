@@ -53,7 +53,10 @@ NFFT = 8192
 
 @dataclass
 class FieldInfo:
-    """field.h:20-28 FieldInfo (all physical sizes in nm)."""
+    """field.h:20-28 FieldInfo (all physical sizes in nm), plus the settings the
+    reference hard-codes (0 = its value): Courant number (0.7071, field.h:70),
+    sigma grading exponent (2, field.c:259-283), NTFF inset in cells (5,
+    field.c:136-139).  RefSim takes the reference's values only."""
     width_nm: int
     height_nm: int
     h_u_nm: int
@@ -61,6 +64,9 @@ class FieldInfo:
     lambda_nm: int
     angle_deg: int
     step_num: int
+    courant: float = 0.0
+    pml_order: int = 0
+    ntff_inset: int = 0
 
     def astuple(self):
         return (self.width_nm, self.height_nm, self.h_u_nm, self.pml,
@@ -108,7 +114,8 @@ class Model:
 
 class _OfFieldInfo(C.Structure):
     _fields_ = [(n, C.c_int) for n in ("width_nm", "height_nm", "h_u_nm", "pml",
-                                       "lambda_nm", "angle_deg", "step_num")]
+                                       "lambda_nm", "angle_deg", "step_num")] + \
+               [("courant", C.c_double), ("pml_order", C.c_int), ("ntff_inset", C.c_int)]
 
 
 class _OfModel(C.Structure):
@@ -181,7 +188,7 @@ def oracle_lib():
 
 
 def _pack(fi: FieldInfo, m: Model):
-    cfi = _OfFieldInfo(*fi.astuple())
+    cfi = _OfFieldInfo(*fi.astuple(), float(fi.courant), int(fi.pml_order), int(fi.ntff_inset))
     cm = _OfModel()
     cm.kind = m.kind
     for i, v in enumerate(m.p[:40]):
@@ -315,6 +322,8 @@ class RefSim:
             TM_2D: "splittm", TE_2D: "splitte", NS_TM_2D: "nstm", NS_TE_2D: "nste"}
 
     def __init__(self, solver, fi: FieldInfo, model: Model | None = None):
+        if fi.courant or fi.pml_order or fi.ntff_inset:
+            raise ValueError("the reference hard-codes the Courant number, sigma grading and NTFF inset")
         self.lib = ref_lib()
         self.solver = SOLVERS[solver] if isinstance(solver, str) else solver
         self.fi = fi

@@ -156,3 +156,44 @@ def test_reference_program_links_against_dropin(libs, tmp_path):
     syms = subprocess.run(["nm", str(exe)], capture_output=True, text=True).stdout
     assert " U mpi_fdtdTM_upml_getUpdate" in syms and " U fdtdTE_upml_getInit" in syms
     assert " U fdtdTM_getUpdate" in syms and " U nsFdtdTE_getInit" in syms
+
+
+class _EngineConfig(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("width_nm", "height_nm", "h_u_nm", "pml", "lambda_nm", "angle_deg",
+                                       "step_num", "precision", "flags", "courant_e4", "pml_order",
+                                       "ntff_inset")] + [("reserved", C.c_int * 4)]
+
+
+@pytest.mark.parametrize("courant,order,inset", [(0, 0, 0), (0.5, 3, 20), (0.6, 4, 8)])
+def test_engine_geometry_with_settings_matches_oracle(libs, oracle_built, courant, order, inset):
+    """fdtd_geometry_of (no GPU needed) and the oracle agree on the NTFF box,
+    RFperC, arraySize and omega for the reference's settings and for a Courant
+    number, grading order and NTFF inset the reference hard-codes."""
+    from mpifdtd_gb300.engine import Geometry
+    from oracle.pyoracle import FieldInfo as OFI, OracleSim
+    e = libs["engine"]
+    e.fdtd_geometry_of.argtypes = [C.POINTER(_EngineConfig), C.POINTER(Geometry)]
+    fi = (600, 640, 5, 8, 150, 0, 300)
+    cfg = _EngineConfig(*fi, 0, 0, round(courant * 1e4), order, inset)
+    g = Geometry()
+    assert e.fdtd_geometry_of(C.byref(cfg), C.byref(g)) == 0
+    o = OracleSim("MPI_TM_UPML", OFI(*fi, courant=courant, pml_order=order, ntff_inset=inset))
+    assert (g.ntff_top, g.ntff_bottom, g.ntff_left, g.ntff_right) == (o.top, o.bottom, o.left, o.right)
+    assert g.ntff_left == 8 + (inset or 5)
+    assert g.rf_per_c == o.rf and g.array_size == o.array_size
+    assert g.omega_s == (courant or 0.7071) * (2 * np.pi / (150 / 5))   # field.c:107-109
+
+
+def test_engine_rejects_settings_out_of_range_and_for_split_solvers(libs):
+    """Courant above 1/sqrt 2, a negative grading order and any setting on the
+    split-field / NS solvers are refused before any device work."""
+    e = libs["engine"]
+    e.fdtd_create.argtypes = [C.c_int, C.POINTER(_EngineConfig), C.POINTER(C.c_void_p)]
+    e.fdtd_last_error.restype = C.c_char_p
+    h = C.c_void_p()
+    base = (600, 640, 5, 8, 150, 0, 300, 0, 0)
+    assert e.fdtd_create(4, C.byref(_EngineConfig(*base, 7072, 0, 0)), C.byref(h)) == 1        # FDTD_E_ARG
+    assert e.fdtd_create(4, C.byref(_EngineConfig(*base, 0, -1, 0)), C.byref(h)) == 1
+    for solver in (0, 1, 6, 7):
+        assert e.fdtd_create(solver, C.byref(_EngineConfig(*base, 5000, 0, 0)), C.byref(h)) == 5   # UNSUPPORTED
+        assert b"reference's Courant number" in e.fdtd_last_error()

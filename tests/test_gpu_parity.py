@@ -289,3 +289,56 @@ def test_gpu_flush_deposits_a_run_shorter_than_the_ntff_block():
     b.run(20)
     for w in range(3):
         assert rel(a.ntff(w), b.ntff(w)) <= 1e-12
+
+
+SETTINGS = {"c05_cubic_inset20": dict(courant=0.5, pml_order=3, ntff_inset=20),
+            "c06_quartic_inset8": dict(courant=0.6, pml_order=4, ntff_inset=8)}
+
+
+@pytest.mark.parametrize("setting", sorted(SETTINGS))
+@pytest.mark.parametrize("solver", ["MPI_TM_UPML", "MPI_TE_UPML", "TM_UPML", "TE_UPML"])
+def test_gpu_settings_the_reference_fixes_match_oracle(solver, setting):
+    """Courant number, sigma grading order and NTFF inset away from the
+    reference's hard-coded values (field.h:70, field.c:259-283,
+    field.c:136-139): fields, NTFF accumulators and the far field (frequency
+    NTFF of the MPI solvers, spectrum of the serial ones) against the oracle
+    restatement at the same settings, 1e-12."""
+    m = _engine()
+    from oracle.pyoracle import FieldInfo as OFI, Model, OracleSim
+    fi = (500, 520, 5, 8, 120, 20, 150)
+    o = OracleSim(solver, OFI(*fi, **SETTINGS[setting]), Model.circle(90, 2.25))
+    mpi = solver.startswith("MPI")
+    sim = m.Simulation(solver, m.FieldInfo(*fi, **SETTINGS[setting]))
+    sim.set_eps(*[crop(o.eps(w), mpi) for w in range(3)])
+    assert (sim.geo.ntff_left, sim.array_size) == (o.left, o.array_size)
+    o.step(150)
+    sim.run(150)
+    for w in range(3):
+        e = rel(sim.field(w), crop(o.field(w), mpi))
+        assert e <= TOL, (solver, setting, "field", w, e)
+        e = rel(sim.ntff(w), o.ntff(w))
+        assert e <= TOL, (solver, setting, "ntff", w, e)
+    if mpi:
+        e = rel(sim.frequency(), o.frequency())
+    else:
+        e = rel(sim.spectrum(), o.time_output())
+    assert e <= TOL, (solver, setting, "far field", e)
+
+
+@pytest.mark.parametrize("solver", ["MPI_TM_UPML", "MPI_TE_UPML"])
+def test_gpu_settings_blocked_kernels_match_oracle(solver):
+    """The temporally blocked kernels (K = 4) at a Courant number of 0.5,
+    cubic grading and a 20-cell NTFF inset."""
+    m = _engine()
+    from oracle.pyoracle import FieldInfo as OFI, Model, OracleSim
+    fi = (500, 520, 5, 8, 120, 0, 150)
+    st = SETTINGS["c05_cubic_inset20"]
+    o = OracleSim(solver, OFI(*fi, **st), Model.circle(90, 2.25))
+    sim = m.Simulation(solver, m.FieldInfo(*fi, **st))
+    sim.set_eps(*[crop(o.eps(w), True) for w in range(3)])
+    sim.set_option(m.OPT_TBLOCK, 4)
+    o.step(120)
+    sim.run(120)
+    for w in range(3):
+        assert rel(sim.field(w), crop(o.field(w), True)) <= TOL
+        assert rel(sim.ntff(w), o.ntff(w)) <= TOL

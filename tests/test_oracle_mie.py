@@ -63,3 +63,22 @@ def test_oracle_elliptic_ring_matches_mie_near_field(solver, pol):
     ref = mie.near_field_ring(r, lam, eps, pol, 1.2 * lam)
     err = float(np.linalg.norm(ring - ref) / np.linalg.norm(ref))
     assert err < (0.02 if pol == "TM" else 0.04), err
+
+
+@pytest.mark.parametrize("solver,pol", [("MPI_TM_UPML", "TM"), ("MPI_TE_UPML", "TE")])
+def test_oracle_far_field_matches_mie_with_settings_the_reference_fixes(solver, pol):
+    """The restatement with a Courant number of 0.5, cubic sigma grading and
+    the NTFF path 20 cells inside the PML -- settings the reference hard-codes
+    (field.h:70, field.c:259-283, field.c:136-139) and so cannot produce golden
+    vectors for -- still lands on the Mie series: same cylinder as above, run
+    1.41x longer since a step now advances the wave 0.5 cells instead of 0.7071."""
+    r, lam, eps = 100, 300, 2.25
+    fi = po.FieldInfo(800, 800, 5, 10, lam, 0, 1300, courant=0.5, pml_order=3, ntff_inset=20)
+    sim = po.OracleSim(solver, fi, po.Model.circle(r, eps))
+    assert (sim.left, sim.bottom) == (30, 30) and sim.right == 160 - 30
+    sim.step(1300)
+    inten = np.abs(sim.frequency()) ** 2
+    ref = np.abs(mie.far_field(r, lam, eps, pol, angles_deg=np.arange(360) + 180)) ** 2
+    err, _ = mie.pattern_error(inten, ref)
+    assert err < 0.02, err
+    assert abs(int(np.argmax(inten)) - 180) <= 2

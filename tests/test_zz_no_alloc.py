@@ -20,7 +20,8 @@ pytestmark = pytest.mark.gpu
 
 class _Config(C.Structure):
     _fields_ = [(n, C.c_int) for n in ("width_nm", "height_nm", "h_u_nm", "pml", "lambda_nm",
-                                       "angle_deg", "step_num", "precision")] + [("reserved", C.c_int * 8)]
+                                       "angle_deg", "step_num", "precision", "flags", "courant_e4",
+                                       "pml_order", "ntff_inset")] + [("reserved", C.c_int * 4)]
 
 
 class _StepArgs(C.Structure):
