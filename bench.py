@@ -514,6 +514,7 @@ def run_e2e(m, sim, args, torch):
     n_px, n_py = sim.n_px, sim.n_py
     n = n_px * n_py
     eps_h = torch.empty(n, dtype=torch.float64, pin_memory=True)
+    eps_h.zero_()   # first touch on the CPU: a pinned buffer only the GPU has written read back at 14 GB/s, not 160
     sim.eps_into(0, eps_h.data_ptr())                     # the workload's EPS_EZ on the host
     ez_h = torch.empty(2 * n, dtype=torch.float64, pin_memory=True)
     nt_len = 360 * sim.array_size

@@ -37,6 +37,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <new>
 #include <vector>
@@ -258,6 +259,9 @@ struct fdtd_batch {
   std::vector<void *> bb_S;     // per instance: [2][ncell][nfreq] DFT sums
   void *d_bb_X = nullptr;       // [360][nfreq] far-field scratch
   int max_nxa = 0, max_ncell = 0;
+  std::vector<double> bb_freq;  // host copy of d_bb_freq
+  // |A(w)|^2 of the incident pulse per (t0, carrier, step_num): the instances of a sweep share it
+  std::vector<std::pair<std::array<double, 3>, std::vector<double>>> bb_a2;
 };
 
 static void batch_free(fdtd_batch *b)
@@ -670,6 +674,8 @@ extern "C" int fdtd_batch_broadband(fdtd_batch *b, int nlam, const int *lambda_n
   b->bb_src.assign(b->sims.size(), nullptr);
   b->bb_S.assign(b->sims.size(), nullptr);
   b->bb_lam.assign(lambda_nm, lambda_nm + nlam);
+  b->bb_freq = freq;
+  b->bb_a2.clear();
   BCK(cudaMalloc(&b->d_bb_freq, sizeof(double) * nlam));
   BCK(cudaMemcpy(b->d_bb_freq, freq.data(), sizeof(double) * nlam, cudaMemcpyHostToDevice));
   BCK(cudaMalloc(&b->d_bb_phase, sizeof(double2) * kMaxTBlock * (size_t)nlam));
@@ -691,20 +697,30 @@ extern "C" int fdtd_batch_broadband_spectrum(fdtd_batch *b, int index, double *o
   std::vector<double2> X(360 * (size_t)nfreq);
   BCK(cudaMemcpyAsync(X.data(), b->d_bb_X, sizeof(double2) * X.size(), cudaMemcpyDeviceToHost, s->stream));
   BCK(cudaStreamSynchronize(s->stream));
-  std::vector<double> freq(nfreq);
-  BCK(cudaMemcpy(freq.data(), b->d_bb_freq, sizeof(double) * nfreq, cudaMemcpyDeviceToHost));
   // the incident pulse at x = 0 (field.c:224-256), transformed with the samples' e^{i w t}:
   // dividing by it leaves the response to a unit incident wave, the CW run's steady state
   const double t0 = -((s->geo.n_px / 2.0) * (cos(0.0) / s->c0)) + 500, w = s->geo.omega_s;
-  for (int k = 0; k < nfreq; k++) {
-    double ar = 0, ai = 0;
-    for (int t = 0; t < s->cfg.step_num; t++) {
-      const double r = -(t - t0), g = exp(-(r / 50.0) * (r / 50.0));
-      const double ph = r * w + freq[k] * (t - 1.0);
-      ar += g * cos(ph);
-      ai += g * sin(ph);
+  const std::array<double, 3> key{t0, w, (double)s->cfg.step_num};
+  const std::vector<double> *a2v = nullptr;
+  for (const auto &e : b->bb_a2)
+    if (e.first == key) a2v = &e.second;
+  if (!a2v) {
+    std::vector<double> a2(nfreq);
+    for (int k = 0; k < nfreq; k++) {
+      double ar = 0, ai = 0;
+      for (int t = 0; t < s->cfg.step_num; t++) {
+        const double r = -(t - t0), g = exp(-(r / 50.0) * (r / 50.0));
+        const double ph = r * w + b->bb_freq[k] * (t - 1.0);
+        ar += g * cos(ph);
+        ai += g * sin(ph);
+      }
+      a2[k] = ar * ar + ai * ai;
     }
-    const double a2 = ar * ar + ai * ai;
+    b->bb_a2.emplace_back(key, std::move(a2));
+    a2v = &b->bb_a2.back().second;
+  }
+  for (int k = 0; k < nfreq; k++) {
+    const double a2 = (*a2v)[k];
     for (int ang = 0; ang < 360; ang++) {
       const double2 x = X[(size_t)ang * nfreq + k];
       out[(size_t)k * 360 + ang] = (x.x * x.x + x.y * x.y) / a2;

@@ -26,11 +26,13 @@ def main(argv=None):
                     help="average the prediction over the structure, its mirror image and views-2 translations")
     ap.add_argument("--seed", type=int, default=20261207)
     ap.add_argument("--tol", type=float, default=0.02)
+    ap.add_argument("--mode", choices=["broadband", "cw"], default="broadband",
+                    help="FDTD data: one pulse run per map (broadband) or one CW run per wavelength (cw)")
     a = ap.parse_args(argv)
     from .data import Generator
     from .model import FNO
     from . import screen as S
-    gen = Generator(group=64)
+    gen = Generator(group=256 if a.mode == "broadband" else 64, mode=a.mode)
     maps, inten, sec = S.generate(a.train + a.val, a.seed, gen)
     net = FNO(seed=1)
     t_train = S.train(net, maps[:a.train], inten[:a.train], steps=a.steps, batch=a.batch, lr=a.lr,
@@ -39,10 +41,10 @@ def main(argv=None):
     ev1 = ev if a.views <= 1 else S.evaluate(net, maps[a.train:], inten[a.train:])
     rate = S.inference_rate(net)
     k = max(1, int(np.ceil(0.01 * a.val)))
-    audit = Generator(group=k)
+    audit = Generator(group=k, mode=a.mode)
     _, st = S.screen(net, maps[a.train:], gen, audit_frac=0.01, tol=a.tol, batch=a.val, audit_gen=audit,
                      views=a.views)
-    out = {"maps": a.train + a.val, "fdtd_structures_per_s": (a.train + a.val) / sec,
+    out = {"maps": a.train + a.val, "mode": a.mode, "fdtd_structures_per_s": (a.train + a.val) / sec,
            "train": {"maps": a.train, "with_mirror_images": 2 * a.train, "steps": a.steps, "lr": a.lr,
                      "random_translations": not a.no_shift, "seconds": t_train},
            "heldout_rel_l2": ev, "views": a.views, "heldout_rel_l2_one_view": ev1, "network_structures_per_s": rate,

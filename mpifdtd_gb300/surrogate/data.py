@@ -3,11 +3,21 @@
 A structure is a binary permittivity map {1.0, 2.43} on 256 x 256 cells of
 5 nm: 2 to 12 lamellae stacked along y with random thicknesses, gaps and
 widths, their centres offset along x in a zigzag (alternating side, random
-amplitude).  Each map is simulated with MPI_TM_UPML (CW source at 0 deg,
-10-cell UPML around the 256^2 map, 12 optical periods) at the 31 wavelengths
-400, 410, ..., 700 nm by the batched FP32 engine (FP64 far-field sums), and
-the target is the far-field intensity |E(phi)|^2 of ntffTM_Frequency at the
-360 angles: a 31 x 360 float32 array per map.
+amplitude).  The target is its far-field intensity at the 31 wavelengths
+400, 410, ..., 700 nm and 360 angles (31 x 360 float32), MPI_TM_UPML at
+0 degrees with a 10-cell UPML around the 256^2 map, FP32 fields and FP64
+far-field sums, from one of two generators of the batched engine:
+
+* broadband (default): one run per map, driven by the reference's Gaussian
+  pulse (field.c:224-256, carrier 550 nm), the NTFF path samples of every step
+  transformed at the 31 wavelengths (fdtd_batch_broadband); the intensity is
+  per unit incident wave, angle a is the direction a;
+* cw: 31 runs per map, one per wavelength, 12 optical periods of the CW wave,
+  far field from ntffTM_Frequency of the final fields (angle a is the
+  direction a + 180).
+
+The two agree up to one scale per wavelength and the CW runs' distance from
+steady state; the broadband runs cost about 25x fewer cell-updates.
 """
 from __future__ import annotations
 
@@ -68,22 +78,39 @@ def eps_of(m: np.ndarray) -> np.ndarray:
     return e
 
 
-class Generator:
-    """Simulates maps in groups of `group` structures x 31 wavelengths, one
-    batched engine reused for every group."""
+BROADBAND_STEPS = 2500      # the pulse and the structures' ringing have left the 276^2 grid
+BROADBAND_CARRIER = 550
 
-    def __init__(self, group: int = 64, lambdas=LAMBDAS, tblock: int = 4):
+
+class Generator:
+    """Simulates maps in groups of `group` structures, one batched engine
+    reused for every group: broadband (one pulse run per map) or cw (31 runs
+    per map)."""
+
+    def __init__(self, group: int = 64, lambdas=LAMBDAS, tblock: int = 4, mode: str = "broadband",
+                 steps: int = BROADBAND_STEPS):
         from ..engine import OPT_TBLOCK
         self.lambdas = list(lambdas)
         self.group = group
-        fis = [field_info(lam) for _ in range(group) for lam in self.lambdas]
-        self.batch = Batch("MPI_TM_UPML", fis, "f32")
+        self.mode = mode
+        if mode == "broadband":
+            side = (GRID + 2 * PML) * H_U
+            fis = [FieldInfo(side, side, H_U, PML, BROADBAND_CARRIER, 0, steps) for _ in range(group)]
+            self.batch = Batch("MPI_TM_UPML", fis, "f32", no_time_ntff=False)
+            self.batch.broadband(self.lambdas)
+        elif mode == "cw":
+            fis = [field_info(lam) for _ in range(group) for lam in self.lambdas]
+            self.batch = Batch("MPI_TM_UPML", fis, "f32")
+        else:
+            raise ValueError(f"unknown generator mode {mode!r}")
         self.batch.set_option(OPT_TBLOCK, tblock)
         self.cell_steps = sum((f.width_nm // H_U) ** 2 * f.step_num for f in fis)
         self.seconds = 0.0
 
     def far_field(self, maps: np.ndarray) -> np.ndarray:
-        """|E|^2 at 360 angles: (len(maps), n_lambda, 360) float32."""
+        """Far-field intensity at 360 angles: (len(maps), n_lambda, 360) float32."""
+        if self.mode == "broadband":
+            return self._broadband(maps)
         nl = len(self.lambdas)
         out = np.zeros((len(maps), nl, 360), np.float32)
         for g0 in range(0, len(maps), self.group):
@@ -102,6 +129,22 @@ class Generator:
                 for k in range(nl):
                     f = self.batch.instances[q * nl + k].frequency()
                     out[g0 + q, k] = (np.abs(f) ** 2).astype(np.float32)
+        return out
+
+    def _broadband(self, maps: np.ndarray) -> np.ndarray:
+        out = np.zeros((len(maps), len(self.lambdas), 360), np.float32)
+        for g0 in range(0, len(maps), self.group):
+            part = maps[g0:g0 + self.group]
+            self.batch.reset()
+            for q, s in enumerate(self.batch.instances):
+                s.set_eps(eps_of(part[q] if q < len(part) else part[-1]))
+            for s in self.batch.instances:
+                s.synchronize()
+            t = time.perf_counter()
+            self.batch.run()
+            self.seconds += time.perf_counter() - t
+            for q in range(len(part)):
+                out[g0 + q] = self.batch.broadband_spectrum(q).astype(np.float32)
         return out
 
     def close(self):

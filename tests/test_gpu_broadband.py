@@ -36,14 +36,16 @@ def _broadband(precision, radii=(100.0, 150.0), eps=2.25):
 def test_broadband_far_field_matches_mie_at_seven_wavelengths(precision):
     """Cylinders r = 100, 150 nm, eps 2.25: the intensity pattern at every
     wavelength from 400 to 700 nm is within 3 % (relative L2 after one scale)
-    of the series, and scattering peaks forward (0 degrees)."""
+    of the series, and the scattering is forward (the forward lobe of these
+    small cylinders is flat to 0.1 % over a few degrees, so the test takes
+    the intensity at 0 degrees against the maximum, not the arg max)."""
     out = _broadband(precision)
     for r, inten in zip((100.0, 150.0), out):
         for k, lam in enumerate(LAMS):
             ref = np.abs(mie.far_field(r, lam, 2.25, "TM", angles_deg=np.arange(360))) ** 2
             err, _ = mie.pattern_error(inten[k], ref)
             assert err < 0.03, (r, lam, err)
-            assert min(int(np.argmax(inten[k])), 360 - int(np.argmax(inten[k]))) <= 2
+            assert inten[k][0] >= 0.99 * inten[k].max() and inten[k][0] > 2 * inten[k][180], (r, lam)
 
 
 def test_broadband_fp32_fields_agree_with_fp64():
