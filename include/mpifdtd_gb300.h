@@ -301,6 +301,8 @@ long long fdtd_batch_launch_count(const fdtd_batch *batch);
  * pulse and the structure's ringing leave the grid. */
 int fdtd_batch_broadband(fdtd_batch *batch, int nlam, const int *lambda_nm);
 int fdtd_batch_broadband_spectrum(fdtd_batch *batch, int index, double *out);
+/* The same for every instance: out[n][nlam][360]. */
+int fdtd_batch_broadband_spectra(fdtd_batch *batch, double *out);
 
 /* Number of kernel launches the engine issued since creation. */
 long long fdtd_launch_count(const fdtd_sim *sim);

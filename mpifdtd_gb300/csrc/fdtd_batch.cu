@@ -257,7 +257,7 @@ struct fdtd_batch {
   void *d_bb_phase = nullptr;   // [kMaxTBlock][nfreq] phasors of the current block
   std::vector<void *> bb_src;   // per instance: [kMaxTBlock][nxa] pulse rows (field precision)
   std::vector<void *> bb_S;     // per instance: [2][ncell][nfreq] DFT sums
-  void *d_bb_X = nullptr;       // [360][nfreq] far-field scratch
+  void *d_bb_X = nullptr;       // [n][360][nfreq] far fields of every instance
   int max_nxa = 0, max_ncell = 0;
   std::vector<double> bb_freq;  // host copy of d_bb_freq
   // |A(w)|^2 of the incident pulse per (t0, carrier, step_num): the instances of a sweep share it
@@ -679,52 +679,77 @@ extern "C" int fdtd_batch_broadband(fdtd_batch *b, int nlam, const int *lambda_n
   BCK(cudaMalloc(&b->d_bb_freq, sizeof(double) * nlam));
   BCK(cudaMemcpy(b->d_bb_freq, freq.data(), sizeof(double) * nlam, cudaMemcpyHostToDevice));
   BCK(cudaMalloc(&b->d_bb_phase, sizeof(double2) * kMaxTBlock * (size_t)nlam));
-  BCK(cudaMalloc(&b->d_bb_X, sizeof(double2) * 360 * (size_t)nlam));
+  BCK(cudaMalloc(&b->d_bb_X, sizeof(double2) * 360 * (size_t)nlam * b->sims.size()));
   b->planned_k = 0;  // buffers and graph are made again by the next run
+  return FDTD_OK;
+}
+
+// |A(w_k)|^2 of instance s: the incident pulse at x = 0 (field.c:224-256)
+// transformed with the samples' e^{i w t} over the run; dividing by it leaves
+// the response to a unit incident wave, the CW run's steady state.  Cached by
+// (t0, carrier, step_num): the instances of a sweep share it.
+static const std::vector<double> &pulse_spectrum2(fdtd_batch *b, const fdtd_sim *s)
+{
+  const int nfreq = (int)b->bb_lam.size();
+  const double t0 = -((s->geo.n_px / 2.0) * (cos(0.0) / s->c0)) + 500, w = s->geo.omega_s;
+  const std::array<double, 3> key{t0, w, (double)s->cfg.step_num};
+  for (const auto &e : b->bb_a2)
+    if (e.first == key) return e.second;
+  std::vector<double> a2(nfreq);
+  for (int k = 0; k < nfreq; k++) {
+    double ar = 0, ai = 0;
+    for (int t = 0; t < s->cfg.step_num; t++) {
+      const double r = -(t - t0), g = exp(-(r / 50.0) * (r / 50.0));
+      const double ph = r * w + b->bb_freq[k] * (t - 1.0);
+      ar += g * cos(ph);
+      ai += g * sin(ph);
+    }
+    a2[k] = ar * ar + ai * ai;
+  }
+  b->bb_a2.emplace_back(key, std::move(a2));
+  return b->bb_a2.back().second;
+}
+
+// Far fields of instances [i0, i1) into out[(i - i0)][nlam][360]: one
+// far-field launch per instance on its own stream, one copy back.
+static int broadband_spectra(fdtd_batch *b, int i0, int i1, double *out)
+{
+  if (b->bb_lam.empty()) return set_error(FDTD_E_STATE, "no broadband run (fdtd_batch_broadband)");
+  const int nfreq = (int)b->bb_lam.size();
+  const size_t per = 360 * (size_t)nfreq;
+  for (int i = i0; i < i1; i++) {
+    fdtd_sim *s = b->sims[i];
+    if (!b->bb_S[i]) return set_error(FDTD_E_STATE, "no broadband run (fdtd_batch_broadband)");
+    if (s->time != s->cfg.step_num) return set_error(FDTD_E_STATE, "instance %d has not run to its step_num", i);
+    if (int rc = fdtd_far_field_of_sums(s, (const double *)b->d_bb_freq, nfreq, (const double2 *)b->bb_S[i],
+                                        (double2 *)b->d_bb_X + (size_t)i * per))
+      return rc;
+  }
+  for (int i = i0; i < i1; i++) BCK(cudaStreamSynchronize(b->sims[i]->stream));
+  std::vector<double2> X(per * (size_t)(i1 - i0));
+  BCK(cudaMemcpy(X.data(), (double2 *)b->d_bb_X + (size_t)i0 * per, sizeof(double2) * X.size(),
+                 cudaMemcpyDeviceToHost));
+  for (int i = i0; i < i1; i++) {
+    const std::vector<double> &a2 = pulse_spectrum2(b, b->sims[i]);
+    const double2 *x = X.data() + (size_t)(i - i0) * per;
+    double *o = out + (size_t)(i - i0) * per;
+    for (int k = 0; k < nfreq; k++)
+      for (int ang = 0; ang < 360; ang++) {
+        const double2 v = x[(size_t)ang * nfreq + k];
+        o[(size_t)k * 360 + ang] = (v.x * v.x + v.y * v.y) / a2[k];
+      }
+  }
   return FDTD_OK;
 }
 
 extern "C" int fdtd_batch_broadband_spectrum(fdtd_batch *b, int index, double *out)
 {
   if (!b || !out || index < 0 || index >= (int)b->sims.size()) return set_error(FDTD_E_ARG, "bad instance index");
-  if (b->bb_lam.empty() || !b->bb_S[index]) return set_error(FDTD_E_STATE, "no broadband run (fdtd_batch_broadband)");
-  fdtd_sim *s = b->sims[index];
-  if (s->time != s->cfg.step_num) return set_error(FDTD_E_STATE, "the instance has not run to its step_num");
-  const int nfreq = (int)b->bb_lam.size();
-  if (int rc = fdtd_far_field_of_sums(s, (const double *)b->d_bb_freq, nfreq, (const double2 *)b->bb_S[index],
-                                      (double2 *)b->d_bb_X))
-    return rc;
-  std::vector<double2> X(360 * (size_t)nfreq);
-  BCK(cudaMemcpyAsync(X.data(), b->d_bb_X, sizeof(double2) * X.size(), cudaMemcpyDeviceToHost, s->stream));
-  BCK(cudaStreamSynchronize(s->stream));
-  // the incident pulse at x = 0 (field.c:224-256), transformed with the samples' e^{i w t}:
-  // dividing by it leaves the response to a unit incident wave, the CW run's steady state
-  const double t0 = -((s->geo.n_px / 2.0) * (cos(0.0) / s->c0)) + 500, w = s->geo.omega_s;
-  const std::array<double, 3> key{t0, w, (double)s->cfg.step_num};
-  const std::vector<double> *a2v = nullptr;
-  for (const auto &e : b->bb_a2)
-    if (e.first == key) a2v = &e.second;
-  if (!a2v) {
-    std::vector<double> a2(nfreq);
-    for (int k = 0; k < nfreq; k++) {
-      double ar = 0, ai = 0;
-      for (int t = 0; t < s->cfg.step_num; t++) {
-        const double r = -(t - t0), g = exp(-(r / 50.0) * (r / 50.0));
-        const double ph = r * w + b->bb_freq[k] * (t - 1.0);
-        ar += g * cos(ph);
-        ai += g * sin(ph);
-      }
-      a2[k] = ar * ar + ai * ai;
-    }
-    b->bb_a2.emplace_back(key, std::move(a2));
-    a2v = &b->bb_a2.back().second;
-  }
-  for (int k = 0; k < nfreq; k++) {
-    const double a2 = (*a2v)[k];
-    for (int ang = 0; ang < 360; ang++) {
-      const double2 x = X[(size_t)ang * nfreq + k];
-      out[(size_t)k * 360 + ang] = (x.x * x.x + x.y * x.y) / a2;
-    }
-  }
-  return FDTD_OK;
+  return broadband_spectra(b, index, index + 1, out);
+}
+
+extern "C" int fdtd_batch_broadband_spectra(fdtd_batch *b, double *out)
+{
+  if (!b || !out) return set_error(FDTD_E_ARG, "null argument");
+  return broadband_spectra(b, 0, (int)b->sims.size(), out);
 }

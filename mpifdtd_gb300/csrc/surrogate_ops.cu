@@ -176,17 +176,20 @@ __global__ void head_unpool_kernel(const float *dflat, float *dh, int B, int C)
 }
 
 // squared error against targets of width nt inside rows of width n (the rest
-// is padding with zero gradient); loss[b] per row; dout = 2 (out - y) / (B nt) in bf16
-__global__ void mse_kernel(const float *out, const float *y, bf16 *dout, float *loss, int B, int n, int nt)
+// is padding with zero gradient), each row weighted by w[b] (null: 1);
+// loss[b] = w[b] mean_j d^2 per row; dout = 2 w[b] (out - y) / (B nt) in bf16
+__global__ void mse_kernel(const float *out, const float *y, const float *w, bf16 *dout, float *loss, int B, int n,
+                           int nt)
 {
   const int b = blockIdx.x;
+  const float wb = w ? w[b] : 1.0f;
   float acc = 0;
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     float g = 0;
     if (j < nt) {
       const float d = out[(size_t)b * n + j] - y[(size_t)b * nt + j];
       acc += d * d;
-      g = 2.0f * d / ((float)B * nt);
+      g = 2.0f * wb * d / ((float)B * nt);
     }
     if (dout) dout[(size_t)b * n + j] = __float2bfloat16(g);
   }
@@ -197,7 +200,7 @@ __global__ void mse_kernel(const float *out, const float *y, bf16 *dout, float *
     if ((int)threadIdx.x < w) r[threadIdx.x] += r[threadIdx.x + w];
     __syncthreads();
   }
-  if (threadIdx.x == 0) loss[b] = r[0] / nt;
+  if (threadIdx.x == 0) loss[b] = wb * r[0] / nt;
 }
 
 // dpre = du * gelu'(pre)  -> bf16
@@ -326,9 +329,10 @@ int sg_head_unpool(const float *dflat, float *dh, int B, int C, void *stream)
   head_unpool_kernel<<<nb((size_t)B * C * 1024, 256), 256, 0, ST>>>(dflat, dh, B, C);
   RET;
 }
-int sg_mse(const float *out, const float *y, void *dout, float *loss, int B, int n, int nt, void *stream)
+int sg_mse(const float *out, const float *y, const float *w, void *dout, float *loss, int B, int n, int nt,
+           void *stream)
 {
-  mse_kernel<<<B, 256, 0, ST>>>(out, y, (bf16 *)dout, loss, B, n, nt);
+  mse_kernel<<<B, 256, 0, ST>>>(out, y, w, (bf16 *)dout, loss, B, n, nt);
   RET;
 }
 int sg_gelu_bwd(const float *du, const float *pre, void *dpre, long long n, void *stream)

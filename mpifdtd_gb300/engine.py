@@ -134,6 +134,7 @@ def load():
         "fdtd_batch_launch_count": (C.c_longlong, [P]),
         "fdtd_batch_broadband": (I, [P, I, C.POINTER(I)]),
         "fdtd_batch_broadband_spectrum": (I, [P, I, dp]),
+        "fdtd_batch_broadband_spectra": (I, [P, dp]),
         "fdtd_last_error": (C.c_char_p, []),
         "fdtd_version": (C.c_char_p, []),
     }
@@ -468,6 +469,12 @@ class Batch:
         incident wave (fdtd_batch_broadband_spectrum); angle a is direction a."""
         out = np.empty((self._bb_n, 360))
         _check(self.lib.fdtd_batch_broadband_spectrum(self.h, int(index), _dptr(out)))
+        return out
+
+    def broadband_spectra(self) -> np.ndarray:
+        """Far-field intensity [n, n_lambda, 360] of every instance (fdtd_batch_broadband_spectra)."""
+        out = np.empty((len(self.instances), self._bb_n, 360))
+        _check(self.lib.fdtd_batch_broadband_spectra(self.h, _dptr(out)))
         return out
 
     def reset(self):

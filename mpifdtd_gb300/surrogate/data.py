@@ -143,8 +143,7 @@ class Generator:
             t = time.perf_counter()
             self.batch.run()
             self.seconds += time.perf_counter() - t
-            for q in range(len(part)):
-                out[g0 + q] = self.batch.broadband_spectrum(q).astype(np.float32)
+            out[g0:g0 + len(part)] = self.batch.broadband_spectra()[:len(part)].astype(np.float32)
         return out
 
     def close(self):

@@ -152,9 +152,10 @@ class FNO:
         return out
 
     # ------------------------------------------------------------ backward
-    def loss_and_grads(self, x, y):
-        """Mean squared error against standardised targets y [B, NT]; returns
-        (per-row loss [B], grads dict of FP32 tensors shaped like the params)."""
+    def loss_and_grads(self, x, y, w=None):
+        """Mean squared error against normalised targets y [B, NT], row b
+        weighted by w[b] (None: 1); returns (per-row loss [B], grads dict of
+        FP32 tensors shaped like the params)."""
         t = self.torch
         bf = t.bfloat16
         B = x.shape[0]
@@ -162,7 +163,7 @@ class FNO:
         a = self.acts
         dout = self._e((B, NOUT), bf)
         loss = self._e((B,))
-        K.op("sg_mse", out, y, dout, loss, B, NOUT, NT)
+        K.op("sg_mse", out, y, w, dout, loss, B, NOUT, NT)
         g = {}
         g["W2"] = self._e((NOUT, H1))
         K.gemm(K.transpose(dout), K.transpose(a["u"]), g["W2"])
@@ -223,9 +224,13 @@ class FNO:
             K.op("sg_adam", w, g[k], m, v, self.bf.get(k), w.numel(), lr, b1, b2, eps, c1, c2, wd)
 
     # ------------------------------------------------------------ targets
-    # target "lin" (default): intensity / (mean intensity of its wavelength over
-    # the training set), so the loss weighs the strong lobes as the relative L2
-    # error of the far field does; "log": per-element standardised log10 intensity.
+    # target "lin": intensity / (mean intensity of its wavelength over the
+    # training set), so the loss weighs the strong lobes as the relative L2
+    # error of the far field does; "rel": intensity / its mean over the
+    # training set (one scale), trained with per-structure weights
+    # 1 / |I_b|^2 (screen.train), so the loss is the mean squared relative L2
+    # error per structure, the metric itself; "log": per-element standardised
+    # log10 intensity.
     def set_normalisation(self, intensity, target="lin"):
         t = self.torch
         self.target = target
@@ -234,6 +239,9 @@ class FNO:
             lg = t.log10(I.reshape(-1, NT) + FLOOR)
             self.mu = lg.mean(0).float()
             self.sd = (lg.std(0) + 1e-3).float()
+        elif target == "rel":
+            self.mu = t.zeros(NT, device="cuda")
+            self.sd = t.full((NT,), float(I.mean()), device="cuda")
         else:
             scale = I.mean(dim=(0, 2))  # per wavelength
             self.mu = t.zeros(NT, device="cuda")

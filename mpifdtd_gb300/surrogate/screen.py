@@ -74,12 +74,14 @@ def shifted(dev_maps, idx, ranges, rng):
     return dev_maps[b[:, None, None], xi[:, :, None], yi[:, None, :]].contiguous()
 
 
-def train(net: FNO, maps, inten, steps=400, batch=128, lr=1e-3, seed=0, log=None, target="lin", augment=True,
+def train(net: FNO, maps, inten, steps=400, batch=128, lr=1e-3, seed=0, log=None, target="rel", augment=True,
           wd=0.0, shift=True):
     """Adam (cosine-decayed learning rate) on minibatches of normalised far
     fields, the training set doubled by its mirror images; with `shift` every
     minibatch structure is also translated at random within the map (same
-    far-field intensity).  Returns seconds."""
+    far-field intensity).  target "rel" (default) weights each structure's
+    squared error by 1 / |its intensity|^2 (mean weight 1): the loss is the
+    evaluation's per-structure relative L2 error, squared.  Returns seconds."""
     import torch
     if augment:
         mm, mi = mirror(maps, inten)
@@ -90,6 +92,10 @@ def train(net: FNO, maps, inten, steps=400, batch=128, lr=1e-3, seed=0, log=None
     target = torch.tensor(inten, device="cuda")
     net.set_normalisation(target, target=target_mode)
     y_all = net.encode(target)
+    w_all = None
+    if target_mode == "rel":
+        sq = (y_all.double() ** 2).mean(1)
+        w_all = (sq.mean() / sq.clamp_min(1e-30)).float().contiguous()
     x_all = None if shift else net.pool(dev_maps)
     ranges = shift_ranges(maps) if shift else None
     n = len(maps)
@@ -102,7 +108,7 @@ def train(net: FNO, maps, inten, steps=400, batch=128, lr=1e-3, seed=0, log=None
         frac = it / max(1, steps - 1)
         step_lr = lr * 0.5 * (1 + math.cos(math.pi * frac))  # cosine decay
         x = net.pool(shifted(dev_maps, pick, ranges, rng)) if shift else x_all[idx].contiguous()
-        loss, g = net.loss_and_grads(x, y_all[idx].contiguous())
+        loss, g = net.loss_and_grads(x, y_all[idx].contiguous(), None if w_all is None else w_all[idx].contiguous())
         net.adam_step(g, lr=step_lr, wd=wd)
         if log is not None and (it % 100 == 0 or it == steps - 1):
             log(it, float(loss.mean()))

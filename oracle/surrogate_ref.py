@@ -53,8 +53,9 @@ def head_unpool(d, B):
     return np.repeat(np.repeat(d.reshape(B, C, 8, 8), 4, axis=2), 4, axis=3).reshape(B, C, NS) / 16
 
 
-def loss_and_grads(p, x, y, D, E):
-    """p: float32 params (model.init_params layout), x [B, 1024], y [B, NT].
+def loss_and_grads(p, x, y, D, E, w=None):
+    """p: float32 params (model.init_params layout), x [B, 1024], y [B, NT],
+    w [B] row weights of the squared error (None: 1).
     Returns (per-row loss [B], grads dict)."""
     p = {k: np.asarray(v, np.float64) for k, v in p.items()}
     B = x.shape[0]
@@ -79,9 +80,10 @@ def loss_and_grads(p, x, y, D, E):
     u = bf16(gelu(pre1))
     out = u @ W2b.T + p["b2"]
     d = out[:, :NT] - y
-    loss = (d * d).mean(axis=1)
+    wv = np.ones(B) if w is None else np.asarray(w, np.float64)
+    loss = wv * (d * d).mean(axis=1)
     dout = np.zeros((B, NOUT))
-    dout[:, :NT] = 2 * d / (B * NT)
+    dout[:, :NT] = 2 * wv[:, None] * d / (B * NT)
     dout = bf16(dout)
     g = {"W2": dout.T @ u, "b2": dout.sum(0)}
     du = dout @ W2b

@@ -26,7 +26,9 @@ def _broadband(precision, radii=(100.0, 150.0), eps=2.25):
         s.fill_model(m.MODEL_CIRCLE, [r, eps])
     b.broadband(LAMS)
     b.run()
-    out = [b.broadband_spectrum(i) for i in range(len(radii))]
+    out = list(b.broadband_spectra())
+    for i in range(len(radii)):   # the batched read-out equals the per-instance one
+        np.testing.assert_array_equal(out[i], b.broadband_spectrum(i))
     assert all(s.status == 0 for s in b.instances)
     b.close()
     return out

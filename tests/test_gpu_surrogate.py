@@ -21,14 +21,15 @@ def test_surrogate_gradients_match_cpu_oracle():
     params = Mdl.init_params(7)
     net = Mdl.FNO(params)
     x = net.pool(torch.tensor(maps, device="cuda"))
-    loss, g = net.loss_and_grads(x, torch.tensor(y, device="cuda"))
+    w = rng.uniform(0.5, 2.0, B).astype(np.float32)   # per-structure loss weights
+    loss, g = net.loss_and_grads(x, torch.tensor(y, device="cuda"), torch.tensor(w, device="cuda"))
     torch.cuda.synchronize()
     from mpifdtd_gb300.surrogate import kernels as K
     assert int(K.err_word().item()) == 0
     x_cpu = R.pool_map(maps)
     np.testing.assert_allclose(x.cpu().numpy(), x_cpu, rtol=0, atol=1e-7)
     D, E = Mdl.basis()
-    loss_ref, g_ref = R.loss_and_grads(params, x_cpu, y.astype(np.float64), D, E)
+    loss_ref, g_ref = R.loss_and_grads(params, x_cpu, y.astype(np.float64), D, E, w.astype(np.float64))
     assert _rel(loss.cpu().numpy(), loss_ref) < 1e-3
     for k, ref in g_ref.items():
         e = _rel(g[k].cpu().numpy().astype(np.float64), ref)
