@@ -339,6 +339,7 @@ static void free_sim(fdtd_sim *s)
   cudaFree(s->d_dft_P);
   cudaFree(s->d_dft_S);
   cudaFree(s->d_dft_X);
+  cudaFree(s->d_dft_T);
   for (int a = 0; a < 3; a++) cudaFree(s->d_ntff[a]);
   cudaFree(s->d_status);
   cudaFree(s->d_chunk);
@@ -1671,6 +1672,35 @@ extern "C" int fdtd_dft_enable(fdtd_sim *s, int nlam, const int *lambda_nm)
   return FDTD_OK;
 }
 
+// The far field's table of e^{i w m} over the retarded bins m = floor(shift +
+// 1/2) (E) and floor(shift + 1) (H) of the path, in the simulation's buffer.
+static int dft_bins(fdtd_sim *s, int nfreq, DftBins *bins)
+{
+  if (s->bin_nm < 0) {
+    double lo = 0, hi = 0;
+    if (!s->h_shift.empty()) {
+      const auto mm = std::minmax_element(s->h_shift.begin(), s->h_shift.end());
+      lo = *mm.first;
+      hi = *mm.second;
+    }
+    s->bin_mlo = (int)floor(lo) - 1;
+    s->bin_nm = (int)floor(hi) + 2 - s->bin_mlo + 1;
+  }
+  const size_t bytes = sizeof(double2) * (size_t)s->bin_nm * nfreq;
+  if (bytes > s->d_dft_T_bytes) {
+    CK(cudaStreamSynchronize(s->stream));  // the previous table may still be read
+    cudaFree(s->d_dft_T);
+    s->d_dft_T = nullptr;
+    s->d_dft_T_bytes = 0;
+    CK(cudaMalloc(&s->d_dft_T, bytes));
+    s->d_dft_T_bytes = bytes;
+  }
+  bins->T = (double2 *)s->d_dft_T;
+  bins->mlo = s->bin_mlo;
+  bins->nm = s->bin_nm;
+  return FDTD_OK;
+}
+
 int fdtd_far_field_of_sums(fdtd_sim *s, const double *d_omega, int nfreq, const double2 *d_S, double2 *d_X)
 {
   if (!s->d_cells) return fail(FDTD_E_STATE, "no NTFF path (FDTD_CFG_NO_TIME_NTFF)");
@@ -1680,8 +1710,10 @@ int fdtd_far_field_of_sums(fdtd_sim *s, const double *d_omega, int nfreq, const 
   d.omega = d_omega;
   d.nfreq = nfreq;
   d.S = const_cast<double2 *>(d_S);
+  DftBins bins{};
+  if (int rc = dft_bins(s, nfreq, &bins)) return rc;
   launch_dft_farfield(ntff_view(s), d, s->tm ? 1 : 0, s->z0, (const double2 *)s->d_dirs,
-                      make_double2(c.real(), c.imag()), d_X, s->stream);
+                      make_double2(c.real(), c.imag()), bins, d_X, s->stream);
   s->launches += 1;
   CK(cudaGetLastError());
   return FDTD_OK;
@@ -1696,8 +1728,10 @@ extern "C" int fdtd_dft_far_field(fdtd_sim *s, double *out_complex)
   if (int rc = ensure_farfield(s)) return rc;
   const std::complex<double> c = spectrum_coef(s);
   const DftView d = dft_view(s);
+  DftBins bins{};
+  if (int rc = dft_bins(s, d.nfreq, &bins)) return rc;
   launch_dft_farfield(ntff_view(s), d, s->tm ? 1 : 0, s->z0, (const double2 *)s->d_dirs, make_double2(c.real(), c.imag()),
-                      (double2 *)s->d_dft_X, s->stream);
+                      bins, (double2 *)s->d_dft_X, s->stream);
   s->launches += 1;
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(out_complex, s->d_dft_X, sizeof(double2) * 360 * (size_t)d.nfreq, cudaMemcpyDeviceToHost,

@@ -29,11 +29,16 @@
 // block: before the tiles, a pulse kernel writes each instance's per-level
 // row table of the pulse (at 0 degrees it depends on x and t only; the tile
 // code reads it through the CW path's row table, one table per level) and the
-// phasors e^{i w t} of the block's sample times; after the tiles, a DFT kernel
+// phasors e^{i w t} of the block's sample time; after the tiles, a DFT kernel
 // reads the NTFF path samples the tiles left in their line buffers and adds
-// v e^{i w t} of every level into per-instance sums S[2][path][nfreq] (FP64),
-// from which the time-domain NTFF's far field at each frequency follows
-// (fdtd_dft.cu).
+// v e^{i w t} of the block's last level into per-instance sums
+// S[2][path][nfreq] (FP64), from which the time-domain NTFF's far field at
+// each frequency follows (fdtd_dft.cu).  One sample per K steps suffices: the
+// pulse's spectrum (a Gaussian of width 1/50 rad per step about its carrier,
+// 0.03-0.06 rad per step for 400-700 nm on 5 nm cells) is negligible long
+// before the Nyquist frequency pi/K of the decimated series, so its Fourier
+// sums at the wavelengths of interest are those of every step divided by K;
+// the incident pulse's sum (the normalisation) is taken over the same times.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -94,8 +99,9 @@ __global__ void batch_source_kernel(BatchInst<R> *inst, const double *omega, int
 // 1/C, sin_per_c = 0, no gap) as per-level row tables: value at array row i
 // (global x = i + ox) and level l (time t + l) = g(r) e^{i r w}, g = exp(-(r/50)^2),
 // r = x/C - (t + l - t0); grid (chunks, instances).  Block (0, 0) also writes
-// the block's DFT phasors P[l][k] = e^{i w_k (t + l - 1)} (the E sample time
-// of level l; the far field adds the H samples' half step).
+// the block's DFT phasors P[k] = e^{i w_k (t + K - 2)}: the E sample time of
+// the last level, the one the DFT takes (the far field adds the H samples'
+// half step).
 template <typename R>
 __global__ void batch_pulse_kernel(BatchInst<R> *inst, int K, const BatchClock *clk, const double *freq, int nfreq,
                                    double2 *P)
@@ -104,11 +110,10 @@ __global__ void batch_pulse_kernel(BatchInst<R> *inst, int K, const BatchClock *
   const BatchInst<R> &I = inst[blockIdx.y];
   const double t = clk->t;
   if (blockIdx.x == 0 && blockIdx.y == 0)
-    for (int q = threadIdx.x; q < K * nfreq; q += blockDim.x) {
-      const int l = q / nfreq, k = q - l * nfreq;
+    for (int k = threadIdx.x; k < nfreq; k += blockDim.x) {
       double sn, cs;
-      sincos(freq[k] * (t + l - 1.0), &sn, &cs);
-      P[q] = make_double2(cs, sn);
+      sincos(freq[k] * (t + K - 2.0), &sn, &cs);
+      P[k] = make_double2(cs, sn);
     }
   if (!I.src) return;
   const int nxa = I.v[0].nxa, ox = I.v[0].ox;
@@ -126,10 +131,11 @@ __global__ void batch_pulse_kernel(BatchInst<R> *inst, int K, const BatchClock *
 }
 
 // Broadband: one warp per (instance, path cell), one lane per frequency.  The
-// E and H samples of every level come from the tiles' line buffers exactly as
-// line_gather_kernel forms them (sign, H average, 1/(4 pi C R)); each lane adds
-// sum_l v_l P[l][k] to the cell's sums.  Runs after both tile kernels of the
-// block and before the clock advances (the parity is the block's).
+// E and H samples of the block's last level come from the tiles' line buffers
+// exactly as line_gather_kernel forms them (sign, H average, 1/(4 pi C R));
+// each lane adds v P[k] to the cell's sums.  Runs after both tile kernels of
+// the block and before the clock advances (the parity is the block's).  An
+// instance whose step_num ends inside the block takes no sample from it.
 template <typename R, int K>
 __global__ void __launch_bounds__(128) batch_dft_kernel(const BatchInst<R> *inst, const BatchClock *clk,
                                                          const double2 *P, int nfreq)
@@ -139,9 +145,7 @@ __global__ void __launch_bounds__(128) batch_dft_kernel(const BatchInst<R> *inst
   if (!I.src) return;
   const int c = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (c >= I.ncell) return;  // whole warp
-  const int left = I.n_steps - (int)clk->t;
-  if (left <= 0) return;
-  const int nlev = left < K ? left : K;
+  if (I.n_steps - (int)clk->t < K) return;
   const int p = clk->q & 1;
   const StencilView<R> &v = I.v[p];
   const TBlockView<R> &tb = I.tb[p];
@@ -149,31 +153,22 @@ __global__ void __launch_bounds__(128) batch_dft_kernel(const BatchInst<R> *inst
   const int i = (int)(sc.k / v.P), j = (int)(sc.k % v.P);
   const int fh = sc.h_slot == 3 ? 1 : 2;  // TM: Hx (bottom/top), Hy (right/left)
   const int i1 = sc.hoff == -1 ? i : i - 1, j1 = sc.hoff == -1 ? j - 1 : j;
-  double2 ev[K], hv[K];
-#pragma unroll
-  for (int l = 0; l < K; l++) {
-    ev[l] = hv[l] = make_double2(0.0, 0.0);  // levels past nlev add nothing
-    if (l >= nlev) continue;
-    T e = czero<T>(), h0 = czero<T>(), h1 = czero<T>();  // path cells always lie on a sampled line
-    tile::line_get(v, tb, l, 0, i, j, e);
-    tile::line_get(v, tb, l, fh, i, j, h0);
-    tile::line_get(v, tb, l, fh, i1, j1, h1);
-    const double sg = sc.sign;
-    ev[l] = make_double2(sg * (double)e.x * I.coef, sg * (double)e.y * I.coef);
-    hv[l] = make_double2((sg * 0.5) * ((double)h0.x + (double)h1.x) * I.coef,
-                         (sg * 0.5) * ((double)h0.y + (double)h1.y) * I.coef);
-  }
+  T e = czero<T>(), h0 = czero<T>(), h1 = czero<T>();  // path cells always lie on a sampled line
+  tile::line_get(v, tb, K - 1, 0, i, j, e);
+  tile::line_get(v, tb, K - 1, fh, i, j, h0);
+  tile::line_get(v, tb, K - 1, fh, i1, j1, h1);
+  const double sg = sc.sign;
+  const double2 ev = make_double2(sg * (double)e.x * I.coef, sg * (double)e.y * I.coef);
+  const double2 hv = make_double2((sg * 0.5) * ((double)h0.x + (double)h1.x) * I.coef,
+                                  (sg * 0.5) * ((double)h0.y + (double)h1.y) * I.coef);
   for (int k = lane; k < nfreq; k += 32) {
     double2 *se = I.S + (size_t)c * nfreq + k, *sh = I.S + ((size_t)I.ncell + c) * nfreq + k;
     double2 ae = *se, ah = *sh;
-#pragma unroll
-    for (int l = 0; l < K; l++) {
-      const double2 ph = P[l * nfreq + k];
-      ae.x = fma(ev[l].x, ph.x, fma(-ev[l].y, ph.y, ae.x));
-      ae.y = fma(ev[l].x, ph.y, fma(ev[l].y, ph.x, ae.y));
-      ah.x = fma(hv[l].x, ph.x, fma(-hv[l].y, ph.y, ah.x));
-      ah.y = fma(hv[l].x, ph.y, fma(hv[l].y, ph.x, ah.y));
-    }
+    const double2 ph = P[k];
+    ae.x = fma(ev.x, ph.x, fma(-ev.y, ph.y, ae.x));
+    ae.y = fma(ev.x, ph.y, fma(ev.y, ph.x, ae.y));
+    ah.x = fma(hv.x, ph.x, fma(-hv.y, ph.y, ah.x));
+    ah.y = fma(hv.x, ph.y, fma(hv.y, ph.x, ah.y));
     *se = ae;
     *sh = ah;
   }
@@ -254,14 +249,14 @@ struct fdtd_batch {
   // broadband mode (fdtd_batch_broadband)
   std::vector<int> bb_lam;      // wavelengths (nm); empty: CW
   void *d_bb_freq = nullptr;    // [nfreq] radians per step
-  void *d_bb_phase = nullptr;   // [kMaxTBlock][nfreq] phasors of the current block
+  void *d_bb_phase = nullptr;   // [nfreq] phasors of the current block's sample time
   std::vector<void *> bb_src;   // per instance: [kMaxTBlock][nxa] pulse rows (field precision)
   std::vector<void *> bb_S;     // per instance: [2][ncell][nfreq] DFT sums
   void *d_bb_X = nullptr;       // [n][360][nfreq] far fields of every instance
   int max_nxa = 0, max_ncell = 0;
   std::vector<double> bb_freq;  // host copy of d_bb_freq
   // |A(w)|^2 of the incident pulse per (t0, carrier, step_num): the instances of a sweep share it
-  std::vector<std::pair<std::array<double, 3>, std::vector<double>>> bb_a2;
+  std::vector<std::pair<std::array<double, 4>, std::vector<double>>> bb_a2;
 };
 
 static void batch_free(fdtd_batch *b)
@@ -678,27 +673,28 @@ extern "C" int fdtd_batch_broadband(fdtd_batch *b, int nlam, const int *lambda_n
   b->bb_a2.clear();
   BCK(cudaMalloc(&b->d_bb_freq, sizeof(double) * nlam));
   BCK(cudaMemcpy(b->d_bb_freq, freq.data(), sizeof(double) * nlam, cudaMemcpyHostToDevice));
-  BCK(cudaMalloc(&b->d_bb_phase, sizeof(double2) * kMaxTBlock * (size_t)nlam));
+  BCK(cudaMalloc(&b->d_bb_phase, sizeof(double2) * (size_t)nlam));
   BCK(cudaMalloc(&b->d_bb_X, sizeof(double2) * 360 * (size_t)nlam * b->sims.size()));
   b->planned_k = 0;  // buffers and graph are made again by the next run
   return FDTD_OK;
 }
 
 // |A(w_k)|^2 of instance s: the incident pulse at x = 0 (field.c:224-256)
-// transformed with the samples' e^{i w t} over the run; dividing by it leaves
-// the response to a unit incident wave, the CW run's steady state.  Cached by
-// (t0, carrier, step_num): the instances of a sweep share it.
+// transformed with the samples' e^{i w t} at the times the DFT sampled (the
+// last level of every full K-step block: clock t = K-1, 2K-1, ...); dividing
+// by it leaves the response to a unit incident wave, the CW run's steady
+// state.  Cached by (t0, carrier, step_num, K): the instances of a sweep share it.
 static const std::vector<double> &pulse_spectrum2(fdtd_batch *b, const fdtd_sim *s)
 {
-  const int nfreq = (int)b->bb_lam.size();
+  const int nfreq = (int)b->bb_lam.size(), K = b->planned_k;
   const double t0 = -((s->geo.n_px / 2.0) * (cos(0.0) / s->c0)) + 500, w = s->geo.omega_s;
-  const std::array<double, 3> key{t0, w, (double)s->cfg.step_num};
+  const std::array<double, 4> key{t0, w, (double)s->cfg.step_num, (double)K};
   for (const auto &e : b->bb_a2)
     if (e.first == key) return e.second;
   std::vector<double> a2(nfreq);
   for (int k = 0; k < nfreq; k++) {
     double ar = 0, ai = 0;
-    for (int t = 0; t < s->cfg.step_num; t++) {
+    for (int t = K - 1; t < s->cfg.step_num; t += K) {
       const double r = -(t - t0), g = exp(-(r / 50.0) * (r / 50.0));
       const double ph = r * w + b->bb_freq[k] * (t - 1.0);
       ar += g * cos(ph);

@@ -54,40 +54,75 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b)
   return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-// X[a][k] = coef sum_{c, f} g e^{i w M} kappa S ; one block per angle, threads over k
-__global__ void dft_farfield_kernel(NtffView n, const double2 *S, const double *omega, int nfreq, int tm,
-                                    double z0, const double2 *dir, double2 coef, double2 *X)
+// T[m][k] = e^{i w_k (m + mlo)} for the integer bins m + mlo the far field
+// needs (the same sincos of w M the far field would take per element)
+__global__ void dft_bin_phasor_kernel(const double *omega, int nfreq, int mlo, int nm, double2 *T)
 {
-  const int ang = blockIdx.x;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nm * nfreq) return;
+  const int m = i / nfreq, k = i - m * nfreq;
+  double sm, cm;
+  sincos(omega[k] * (double)(m + mlo), &sm, &cm);
+  T[i] = make_double2(cm, sm);
+}
+
+// X[a][k] = coef sum_{c, f} g e^{i w M} kappa S ; one block per angle, 128
+// threads = 4 groups of path cells x 32 frequencies (lane k), the groups'
+// sums added in shared memory.  e^{i w M} comes from the bin table T (the
+// sincos fallback covers a bin outside it, which the table's range excludes).
+__global__ void __launch_bounds__(128) dft_farfield_kernel(NtffView n, const double2 *S, const double *omega,
+                                                           int nfreq, int tm, double z0, const double2 *dir,
+                                                           double2 coef, const double2 *T, int mlo, int nm,
+                                                           double2 *X)
+{
+  __shared__ double2 part[4][32];
+  const int ang = blockIdx.x, lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
   const double2 d = dir[ang];
   const double px = -d.y, py = d.x, sz = -1.0;
   // weight of accumulators 0, 1, 2 in the angle's far-field component (spectrum_kernel's combination)
   double g[3];
   if (tm) { g[0] = -px; g[1] = -py; g[2] = -z0 * sz; }
   else { g[0] = -z0 * px; g[1] = -z0 * py; g[2] = sz; }
-  for (int k = threadIdx.x; k < nfreq; k += blockDim.x) {
-    const double w = omega[k];
-    double sw, cw;
-    sincos(w, &sw, &cw);
+  for (int k0 = 0; k0 < nfreq; k0 += 32) {
+    const int k = k0 + lane;
     double2 sum = make_double2(0.0, 0.0);
-    for (int c = 0; c < n.ncell; c++) {
-      const double sh = n.shift[(size_t)ang * n.ncell + c];
-      const unsigned char uw = (unsigned char)n.cells[c].uid_wid;
-      for (int f = 0; f < 2; f++) {
-        const double u = (f == 0 ? sh : sh + 0.5) + 0.5;
-        const double M = floor(u);
-        const double a = u - M, b = 1.0 - a;
-        // kappa = b e^{-iw} + (a - b) - a e^{iw}
-        const double2 kap = make_double2(b * cw + (a - b) - a * cw, -b * sw - a * sw);
-        double sm, cm;
-        sincos(w * M, &sm, &cm);
-        const double2 t = cmul(cmul(make_double2(cm, sm), kap), S[((size_t)f * n.ncell + c) * nfreq + k]);
-        const double gw = g[f == 0 ? (uw & 15) : (uw >> 4)];
-        sum.x += gw * t.x;
-        sum.y += gw * t.y;
+    if (k < nfreq) {
+      const double w = omega[k];
+      double sw, cw;
+      sincos(w, &sw, &cw);
+      for (int c = grp; c < n.ncell; c += 4) {
+        const double sh = n.shift[(size_t)ang * n.ncell + c];
+        const unsigned char uw = (unsigned char)n.cells[c].uid_wid;
+        for (int f = 0; f < 2; f++) {
+          const double u = (f == 0 ? sh : sh + 0.5) + 0.5;
+          const double M = floor(u);
+          const double a = u - M, b = 1.0 - a;
+          // kappa = b e^{-iw} + (a - b) - a e^{iw}
+          const double2 kap = make_double2(b * cw + (a - b) - a * cw, -b * sw - a * sw);
+          const long long m = (long long)M - mlo;
+          double2 em;
+          if (m >= 0 && m < nm) {
+            em = T[(size_t)m * nfreq + k];
+          } else {
+            double sm, cm;
+            sincos(w * M, &sm, &cm);
+            em = make_double2(cm, sm);
+          }
+          const double2 t = cmul(cmul(em, kap), S[((size_t)f * n.ncell + c) * nfreq + k]);
+          const double gw = g[f == 0 ? (uw & 15) : (uw >> 4)];
+          sum.x += gw * t.x;
+          sum.y += gw * t.y;
+        }
       }
     }
-    X[(size_t)ang * nfreq + k] = cmul(coef, sum);
+    part[grp][lane] = sum;
+    __syncthreads();
+    if (grp == 0 && k < nfreq) {
+      const double2 a0 = part[0][lane], a1 = part[1][lane], a2 = part[2][lane], a3 = part[3][lane];
+      const double2 tot = make_double2(((a0.x + a1.x) + a2.x) + a3.x, ((a0.y + a1.y) + a2.y) + a3.y);
+      X[(size_t)ang * nfreq + k] = cmul(coef, tot);
+    }
+    __syncthreads();
   }
 }
 
@@ -102,9 +137,13 @@ void launch_dft_accumulate(const NtffView &n, const DftView &d, int nb, double t
 }
 
 void launch_dft_farfield(const NtffView &n, const DftView &d, int tm, double z0, const double2 *dir, double2 coef,
-                         double2 *X, cudaStream_t st)
+                         const DftBins &bins, double2 *X, cudaStream_t st)
 {
-  dft_farfield_kernel<<<360, 128, 0, st>>>(n, d.S, d.omega, d.nfreq, tm, z0, dir, coef, X);
+  if (bins.nm > 0)
+    dft_bin_phasor_kernel<<<(bins.nm * d.nfreq + 255) / 256, 256, 0, st>>>(d.omega, d.nfreq, bins.mlo, bins.nm,
+                                                                           bins.T);
+  dft_farfield_kernel<<<360, 128, 0, st>>>(n, d.S, d.omega, d.nfreq, tm, z0, dir, coef, bins.T, bins.mlo, bins.nm,
+                                          X);
 }
 
 }  // namespace fdtd

@@ -196,8 +196,14 @@ struct DftView {
   double2 *S;           // [2][ncell][nfreq] sum_t v_c(t) e^{i w t} (E samples, H samples)
 };
 void launch_dft_accumulate(const NtffView &n, const DftView &d, int nb, double t0, cudaStream_t st);
+// Table of e^{i w_k m} for the integer retarded bins m in [mlo, mlo + nm) of
+// a path (the caller's device buffer, nm x nfreq; nm = 0: no table).
+struct DftBins {
+  double2 *T;
+  int mlo, nm;
+};
 void launch_dft_farfield(const NtffView &n, const DftView &d, int tm, double z0, const double2 *dir, double2 coef,
-                         double2 *X, cudaStream_t st);
+                         const DftBins &bins, double2 *X, cudaStream_t st);
 // The settings of a configuration that the reference hard-codes (fdtd_config:
 // courant_e4, pml_order, ntff_inset; 0 = the reference's value).
 inline double config_courant(const fdtd_config &c) { return c.courant_e4 > 0 ? c.courant_e4 / 1.0e4 : kC; }

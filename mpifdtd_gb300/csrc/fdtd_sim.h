@@ -64,6 +64,9 @@ struct fdtd_sim {
   std::vector<int> dft_lam;
   std::vector<double> dft_frac;  // interpolation weight of the upper bin per wavelength
   void *d_dft_omega = nullptr, *d_dft_P = nullptr, *d_dft_S = nullptr, *d_dft_X = nullptr;
+  void *d_dft_T = nullptr;        // far-field bin table e^{i w m} (fdtd_dft.cu DftBins), d_dft_T_bytes long
+  size_t d_dft_T_bytes = 0;
+  int bin_mlo = 0, bin_nm = -1;   // retarded bins of the path's shifts (-1: not yet derived)
   // far-field outputs (allocated on first use)
   void *d_spec = nullptr, *d_dirs = nullptr, *d_twiddle = nullptr, *d_freq = nullptr;
   // per-kernel event timing (fdtd_profile_*): 5 events per step

@@ -32,21 +32,49 @@ __device__ __forceinline__ float gelu_grad(float x)
   return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * k0 * (1.0f + 3.0f * k1 * x * x);
 }
 
-// map [B][256][256] u8 -> x [B][32*32] f32: mean of each 8 x 8 block
+// map [B][256][256] u8 -> x [kNin][B][32*32] f32: per 8 x 8 block the
+// dielectric's fill fraction and its first and second moments about the
+// block centre, u = (p - 3.5) / 4 along x and y (where in the block the
+// material sits, which the fill fraction alone loses):
+//   x0 = mean e, x1 = mean e u_x, x2 = mean e u_y, x3 = mean e u_x^2, x4 = mean e u_y^2
+constexpr int kNin = 5;
 __global__ void pool_map_kernel(const uint8_t *map, float *x, int B)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= B * 1024) return;
   const int b = i / 1024, p = i % 1024, px = p / 32, py = p % 32;
   const uint8_t *m = map + (size_t)b * 65536 + (size_t)(px * 8) * 256 + py * 8;
-  int s = 0;
+  int s = 0, sx = 0, sy = 0, sxx = 0, syy = 0;  // in units of (2u)*4 = 2r - 7: integers
   for (int r = 0; r < 8; r++)
-    for (int c = 0; c < 8; c++) s += m[r * 256 + c] ? 1 : 0;
+    for (int c = 0; c < 8; c++)
+      if (m[r * 256 + c]) {
+        const int ux = 2 * r - 7, uy = 2 * c - 7;
+        s += 1;
+        sx += ux;
+        sy += uy;
+        sxx += ux * ux;
+        syy += uy * uy;
+      }
+  const size_t n = (size_t)B * 1024;
   x[i] = s * (1.0f / 64.0f);
+  x[n + i] = sx * (1.0f / (64.0f * 8.0f));
+  x[2 * n + i] = sy * (1.0f / (64.0f * 8.0f));
+  x[3 * n + i] = sxx * (1.0f / (64.0f * 64.0f));
+  x[4 * n + i] = syy * (1.0f / (64.0f * 64.0f));
 }
 
-// h0[b][c][s] = x[b][s] wl[c] + bl[c] in both layouts: i < n writes the
-// channels-first copy, n <= i < 2n the channels-last one (each coalesced)
+// h0[b][c][s] = sum_i x[i][b][s] wl[i][c] + bl[c] in both layouts: idx < n
+// writes the channels-first copy, n <= idx < 2n the channels-last one
+// (each coalesced)
+__device__ __forceinline__ float lift_value(const float *x, const float *wl, const float *bl, int B, int C, int b,
+                                            int c, int s)
+{
+  const size_t n = (size_t)B * 1024, o = (size_t)b * 1024 + s;
+  float v = bl[c];
+#pragma unroll
+  for (int q = 0; q < kNin; q++) v += x[q * n + o] * wl[q * C + c];
+  return v;
+}
 __global__ void lift_kernel(const float *x, const float *wl, const float *bl, bf16 *h_cf, bf16 *h_cl, int B, int C)
 {
   const size_t n = (size_t)B * C * 1024;
@@ -54,17 +82,18 @@ __global__ void lift_kernel(const float *x, const float *wl, const float *bl, bf
   if (i >= 2 * n) return;
   if (i < n) {
     const int s = i % 1024, c = (i / 1024) % C, b = (int)(i / (1024 * (size_t)C));
-    h_cf[i] = __float2bfloat16(x[(size_t)b * 1024 + s] * wl[c] + bl[c]);
+    h_cf[i] = __float2bfloat16(lift_value(x, wl, bl, B, C, b, c, s));
   } else {
     const size_t k = i - n;
     const int c = k % C, s = (k / C) % 1024, b = (int)(k / ((size_t)C * 1024));
-    h_cl[k] = __float2bfloat16(x[(size_t)b * 1024 + s] * wl[c] + bl[c]);
+    h_cl[k] = __float2bfloat16(lift_value(x, wl, bl, B, C, b, c, s));
   }
 }
 
 // column sums of a tall FP32 [R][64] matrix, plain and weighted by w[r]:
-// out[c] += sum_r a[r][c], out_w[c] += sum_r a[r][c] w[r] (both zeroed by the
-// caller); 4 row lanes x 64 columns per block, one atomic per column and block
+// out[c] += sum_r a[r][c] (out may be null), out_w[c] += sum_r a[r][c] w[r]
+// (both zeroed by the caller); 4 row lanes x 64 columns per block, one atomic
+// per column and block
 __global__ void colsum_tall_kernel(const float *a, const float *w, float *out, float *out_w, long long R)
 {
   const int c = threadIdx.x & 63, rl = threadIdx.x >> 6;
@@ -79,7 +108,7 @@ __global__ void colsum_tall_kernel(const float *a, const float *w, float *out, f
   rw[rl][c] = sw;
   __syncthreads();
   if (rl == 0) {
-    atomicAdd(&out[c], rs[0][c] + rs[1][c] + rs[2][c] + rs[3][c]);
+    if (out) atomicAdd(&out[c], rs[0][c] + rs[1][c] + rs[2][c] + rs[3][c]);
     if (w) atomicAdd(&out_w[c], rw[0][c] + rw[1][c] + rw[2][c] + rw[3][c]);
   }
 }
@@ -175,29 +204,37 @@ __global__ void head_unpool_kernel(const float *dflat, float *dh, int B, int C)
   dh[i] = dflat[((size_t)b * C + c) * 64 + px * 8 + py] * (1.0f / 16.0f);
 }
 
-// squared error against targets of width nt inside rows of width n (the rest
-// is padding with zero gradient), each row weighted by w[b] (null: 1);
-// loss[b] = w[b] mean_j d^2 per row; dout = 2 w[b] (out - y) / (B nt) in bf16
-__global__ void mse_kernel(const float *out, const float *y, const float *w, bf16 *dout, float *loss, int B, int n,
-                           int nt)
+// Amplitude head: row b of out holds the far-field amplitude, real parts in
+// columns [0, nt) and imaginary parts in [nt, 2 nt) (the rest is padding with
+// zero gradient); the predicted intensity is I_j = re_j^2 + im_j^2.  Squared
+// error of I against targets y [B][nt], row b weighted by w[b] (null: 1):
+// loss[b] = w[b] mean_j (I_j - y_j)^2; dout = dL/d(re, im) = 2 g (re, im)
+// with g = 2 w[b] (I - y) / (B nt), in bf16.
+__global__ void amp_mse_kernel(const float *out, const float *y, const float *w, bf16 *dout, float *loss, int B,
+                               int n, int nt)
 {
   const int b = blockIdx.x;
   const float wb = w ? w[b] : 1.0f;
+  const float *o = out + (size_t)b * n;
+  bf16 *dz = dout ? dout + (size_t)b * n : nullptr;
   float acc = 0;
-  for (int j = threadIdx.x; j < n; j += blockDim.x) {
-    float g = 0;
-    if (j < nt) {
-      const float d = out[(size_t)b * n + j] - y[(size_t)b * nt + j];
-      acc += d * d;
-      g = 2.0f * wb * d / ((float)B * nt);
+  for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+    const float re = o[j], im = o[nt + j];
+    const float d = (re * re + im * im) - y[(size_t)b * nt + j];
+    acc += d * d;
+    if (dz) {
+      const float g = 2.0f * wb * d / ((float)B * nt);
+      dz[j] = __float2bfloat16(2.0f * g * re);
+      dz[nt + j] = __float2bfloat16(2.0f * g * im);
     }
-    if (dout) dout[(size_t)b * n + j] = __float2bfloat16(g);
   }
+  if (dz)
+    for (int j = 2 * nt + threadIdx.x; j < n; j += blockDim.x) dz[j] = __float2bfloat16(0.0f);
   __shared__ float r[256];
   r[threadIdx.x] = acc;
   __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if ((int)threadIdx.x < w) r[threadIdx.x] += r[threadIdx.x + w];
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) r[threadIdx.x] += r[threadIdx.x + s];
     __syncthreads();
   }
   if (threadIdx.x == 0) loss[b] = wb * r[0] / nt;
@@ -290,16 +327,19 @@ int sg_lift(const float *x, const float *wl, const float *bl, void *h_cf, void *
   lift_kernel<<<nb(2 * (size_t)B * C * 1024, 256), 256, 0, ST>>>(x, wl, bl, (bf16 *)h_cf, (bf16 *)h_cl, B, C);
   RET;
 }
-// dwl[c] = sum_{b,s} dh[b][s][c] x[b][s], dbl[c] = sum dh[b][s][c]  (dh channels-last)
+// dwl[i][c] = sum_{b,s} dh[b][s][c] x[i][b][s], dbl[c] = sum dh[b][s][c]  (dh channels-last)
 int sg_lift_bwd(const float *x, const float *dh, float *dwl, float *dbl, int B, int C, void *stream)
 {
   if (C != 64) return 1;
-  if (cudaMemsetAsync(dwl, 0, 64 * sizeof(float), ST) != cudaSuccess ||
+  if (cudaMemsetAsync(dwl, 0, kNin * 64 * sizeof(float), ST) != cudaSuccess ||
       cudaMemsetAsync(dbl, 0, 64 * sizeof(float), ST) != cudaSuccess)
     return 2;
-  colsum_tall_kernel<<<304, 256, 0, ST>>>(dh, x, dbl, dwl, (long long)B * 1024);
+  const long long R = (long long)B * 1024;
+  for (int q = 0; q < kNin; q++)
+    colsum_tall_kernel<<<304, 256, 0, ST>>>(dh, x + q * R, q == 0 ? dbl : nullptr, dwl + q * 64, R);
   RET;
 }
+int sg_input_channels(void) { return kNin; }
 int sg_mode_permute(const void *in, void *out, int B, int C, int Q, int dir, void *stream)
 {
   mode_permute_kernel<<<nb((size_t)B * C * 2 * Q, 256), 256, 0, ST>>>((const bf16 *)in, (bf16 *)out, B, C, Q, dir);
@@ -329,10 +369,11 @@ int sg_head_unpool(const float *dflat, float *dh, int B, int C, void *stream)
   head_unpool_kernel<<<nb((size_t)B * C * 1024, 256), 256, 0, ST>>>(dflat, dh, B, C);
   RET;
 }
-int sg_mse(const float *out, const float *y, const float *w, void *dout, float *loss, int B, int n, int nt,
-           void *stream)
+int sg_amp_mse(const float *out, const float *y, const float *w, void *dout, float *loss, int B, int n, int nt,
+               void *stream)
 {
-  mse_kernel<<<B, 256, 0, ST>>>(out, y, w, (bf16 *)dout, loss, B, n, nt);
+  if (n < 2 * nt) return 1;
+  amp_mse_kernel<<<B, 256, 0, ST>>>(out, y, w, (bf16 *)dout, loss, B, n, nt);
   RET;
 }
 int sg_gelu_bwd(const float *du, const float *pre, void *dpre, long long n, void *stream)

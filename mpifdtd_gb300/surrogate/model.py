@@ -4,8 +4,10 @@ own kernels (tcgen05 BF16 GEMM with FP32 accumulation, element-wise kernels,
 Adam).  torch supplies device memory and the stream only.
 
 Architecture (B structures, C = 64 channels, 32 x 32 grid, Q = 256 modes):
-  x      = 8 x 8 mean pool of the 256 x 256 map                [B, 1024]
-  h0     = x wl + bl                                            [B, C, 1024]
+  x      = per 8 x 8 block of the 256 x 256 map: the fill fraction and the
+           first and second moments of where the material sits in the
+           block (x, y)                                         [NIN, B, 1024]
+  h0     = sum_i x_i wl_i + bl                                  [B, C, 1024]
   layer l = 0..3 (spectral mixing):
     F    = h D^T      truncated 2-D DFT (modes kx -8..7, ky 0..15, cos/sin
                       rows of D, fixed)                         [B*C, 512]
@@ -18,10 +20,14 @@ Architecture (B structures, C = 64 channels, 32 x 32 grid, Q = 256 modes):
            for the DFT GEMM and channels-last [B*1024, C] for the mixing GEMM
   flat   = 4 x 4 mean pool of h                                 [B, C*64]
   u      = GELU(flat W1^T + b1)                                 [B, 512]
-  out    = u W2^T + b2                                          [B, 11264]
-The first 31*360 outputs are the standardised log10 intensity (per output
-element mean / std of the training targets); the rest is padding that makes
-the output width a multiple of the GEMM tile.
+  out    = u W2^T + b2                                          [B, 22336]
+  I      = out[:, :NT]^2 + out[:, NT:2 NT]^2                    [B, 31*360]
+The head predicts the far-field amplitude (real and imaginary parts of each of
+the 31 x 360 values, in a phase convention of its own) and the intensity is
+its squared modulus: the intensity's interference nulls and lobes are smooth
+sign changes of the amplitude, which a linear read-out follows more easily.
+I is the normalised intensity (intensity / the training set's mean); the last
+16 outputs are padding that makes the width a multiple of the GEMM tile.
 """
 from __future__ import annotations
 
@@ -32,13 +38,13 @@ import numpy as np
 from . import kernels as K
 
 C = 64
+NIN = 5
 NS = 1024
 Q = 256
 NL = 4
 H1 = 512
 NT = 31 * 360
-NOUT = 11264
-FLOOR = 1e-30
+NOUT = 22336
 
 
 def basis():
@@ -63,7 +69,7 @@ def basis():
 def init_params(seed=1234):
     """FP32 parameters (numpy), the layout the GPU model and the CPU oracle share."""
     rng = np.random.default_rng(seed)
-    p = {"wl": rng.normal(0, 1, C), "bl": np.zeros(C)}
+    p = {"wl": rng.normal(0, 1 / math.sqrt(NIN), (NIN, C)), "bl": np.zeros(C)}
     for l in range(NL):
         p[f"M{l}"] = rng.normal(0, 0.5 / math.sqrt(2 * C), (Q, 2 * C, 2 * C))
         p[f"wp{l}"] = rng.normal(0, 1 / math.sqrt(C), (C, C))
@@ -101,17 +107,17 @@ class FNO:
         return self.torch.empty(shape, device="cuda", dtype=dtype or self.torch.float32)
 
     def pool(self, maps_u8):
-        """uint8 maps [B, 256, 256] (device) -> x [B, 1024]."""
+        """uint8 maps [B, 256, 256] (device) -> x [NIN, B, 1024]."""
         B = maps_u8.shape[0]
-        x = self._e((B, NS))
+        x = self._e((NIN, B, NS))
         K.op("sg_pool_map", maps_u8, x, B)
         return x
 
     # ------------------------------------------------------------ forward
     def forward(self, x, save=False):
-        """x [B, 1024] FP32 (B % 128 == 0) -> out [B, NOUT] FP32."""
+        """x [NIN, B, 1024] FP32 (B % 128 == 0) -> out [B, NOUT] FP32."""
         t = self.torch
-        B = x.shape[0]
+        B = x.shape[1]
         assert B % 128 == 0
         bf = t.bfloat16
         h = self._e((B, C, NS), bf)                 # channels-first
@@ -158,12 +164,12 @@ class FNO:
         FP32 tensors shaped like the params)."""
         t = self.torch
         bf = t.bfloat16
-        B = x.shape[0]
+        B = x.shape[1]
         out = self.forward(x, save=True)
         a = self.acts
         dout = self._e((B, NOUT), bf)
         loss = self._e((B,))
-        K.op("sg_mse", out, y, w, dout, loss, B, NOUT, NT)
+        K.op("sg_amp_mse", out, y, w, dout, loss, B, NOUT, NT)
         g = {}
         g["W2"] = self._e((NOUT, H1))
         K.gemm(K.transpose(dout), K.transpose(a["u"]), g["W2"])
@@ -206,7 +212,7 @@ class FNO:
             K.gemm(dz_cl.view(B * NS, C), K.transpose(self.bf[f"wp{l}"]), dh_prev.view(B * NS, C),
                    accumulate=True)                                    # + point-wise part
             dh = dh_prev
-        g["wl"] = self._e((C,))
+        g["wl"] = self._e((NIN, C))
         g["bl"] = self._e((C,))
         K.op("sg_lift_bwd", a["x"], dh, g["wl"], g["bl"], B, C)
         self.acts = None
@@ -229,17 +235,12 @@ class FNO:
     # error of the far field does; "rel": intensity / its mean over the
     # training set (one scale), trained with per-structure weights
     # 1 / |I_b|^2 (screen.train), so the loss is the mean squared relative L2
-    # error per structure, the metric itself; "log": per-element standardised
-    # log10 intensity.
+    # error per structure, the metric itself.
     def set_normalisation(self, intensity, target="lin"):
         t = self.torch
         self.target = target
         I = intensity.reshape(-1, 31, 360).double()
-        if target == "log":
-            lg = t.log10(I.reshape(-1, NT) + FLOOR)
-            self.mu = lg.mean(0).float()
-            self.sd = (lg.std(0) + 1e-3).float()
-        elif target == "rel":
+        if target == "rel":
             self.mu = t.zeros(NT, device="cuda")
             self.sd = t.full((NT,), float(I.mean()), device="cuda")
         else:
@@ -248,16 +249,12 @@ class FNO:
             self.sd = scale[:, None].expand(31, 360).reshape(NT).float().contiguous()
 
     def encode(self, intensity):
-        t = self.torch
         I = intensity.reshape(-1, NT)
-        if getattr(self, "target", "lin") == "log":
-            return ((t.log10(I + FLOOR) - self.mu) / self.sd).float().contiguous()
         return (I / self.sd).float().contiguous()
 
     def decode(self, out):
-        if getattr(self, "target", "lin") == "log":
-            return 10.0 ** (out[:, :NT] * self.sd + self.mu) - FLOOR
-        return out[:, :NT] * self.sd
+        """Intensity from the head's amplitude outputs."""
+        return (out[:, :NT] ** 2 + out[:, NT:2 * NT] ** 2) * self.sd
 
     def predict(self, maps_u8, batch=4096):
         """Far-field intensity [N, 31, 360] of uint8 maps on the device."""

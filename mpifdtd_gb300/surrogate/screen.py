@@ -107,7 +107,7 @@ def train(net: FNO, maps, inten, steps=400, batch=128, lr=1e-3, seed=0, log=None
         idx = torch.tensor(pick, device="cuda")
         frac = it / max(1, steps - 1)
         step_lr = lr * 0.5 * (1 + math.cos(math.pi * frac))  # cosine decay
-        x = net.pool(shifted(dev_maps, pick, ranges, rng)) if shift else x_all[idx].contiguous()
+        x = net.pool(shifted(dev_maps, pick, ranges, rng)) if shift else x_all[:, idx].contiguous()
         loss, g = net.loss_and_grads(x, y_all[idx].contiguous(), None if w_all is None else w_all[idx].contiguous())
         net.adam_step(g, lr=step_lr, wd=wd)
         if log is not None and (it % 100 == 0 or it == steps - 1):

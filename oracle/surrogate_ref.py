@@ -10,7 +10,7 @@ from __future__ import annotations
 
 import numpy as np
 
-C, NS, Q, NL, H1, NT, NOUT = 64, 1024, 256, 4, 512, 31 * 360, 11264
+C, NS, Q, NL, H1, NT, NOUT = 64, 1024, 256, 4, 512, 31 * 360, 22336
 
 
 def bf16(a):
@@ -33,8 +33,14 @@ def gelu_grad(x):
 
 
 def pool_map(maps):
+    """[NIN, B, 1024]: per 8 x 8 block the fill fraction and the moments
+    mean(e u_x), mean(e u_y), mean(e u_x^2), mean(e u_y^2), u = (p - 3.5) / 4."""
     b = maps.shape[0]
-    return (maps > 0).reshape(b, 32, 8, 32, 8).mean(axis=(2, 4)).reshape(b, NS).astype(np.float64)
+    e = (maps > 0).reshape(b, 32, 8, 32, 8).astype(np.float64)
+    u = (np.arange(8) - 3.5) / 4
+    ux, uy = u[None, None, :, None, None], u[None, None, None, None, :]
+    chans = [e, e * ux, e * uy, e * ux * ux, e * uy * uy]
+    return np.stack([c.mean(axis=(2, 4)).reshape(b, NS) for c in chans])
 
 
 def to_modes(F, B):   # [B*C, 2Q] -> [Q, B, 2C] with [q][b][r*C + c] = F[b*C + c][2q + r]
@@ -54,16 +60,16 @@ def head_unpool(d, B):
 
 
 def loss_and_grads(p, x, y, D, E, w=None):
-    """p: float32 params (model.init_params layout), x [B, 1024], y [B, NT],
+    """p: float32 params (model.init_params layout), x [NIN, B, 1024] (pool_map), y [B, NT],
     w [B] row weights of the squared error (None: 1).
     Returns (per-row loss [B], grads dict)."""
     p = {k: np.asarray(v, np.float64) for k, v in p.items()}
-    B = x.shape[0]
+    B = x.shape[1]
     Db, Eb = bf16(D), bf16(E)
     Mb = [bf16(p[f"M{l}"]) for l in range(NL)]
     W1b, W2b = bf16(p["W1"]), bf16(p["W2"])
     Wpb = [bf16(p[f"wp{l}"]) for l in range(NL)]   # the point-wise mixing runs in the BF16 GEMM
-    h = bf16(x[:, None, :] * p["wl"][None, :, None] + p["bl"][None, :, None])
+    h = bf16(np.einsum("ibs,ic->bcs", x, p["wl"]) + p["bl"][None, :, None])
     hs, Fms, zs = [], [], []
     for l in range(NL):
         F = bf16(h.reshape(B * C, NS) @ Db.T)
@@ -79,11 +85,14 @@ def loss_and_grads(p, x, y, D, E, w=None):
     pre1 = flat @ W1b.T + p["b1"]
     u = bf16(gelu(pre1))
     out = u @ W2b.T + p["b2"]
-    d = out[:, :NT] - y
+    re, im = out[:, :NT], out[:, NT:2 * NT]        # amplitude head: I = re^2 + im^2
+    d = (re * re + im * im) - y
     wv = np.ones(B) if w is None else np.asarray(w, np.float64)
     loss = wv * (d * d).mean(axis=1)
     dout = np.zeros((B, NOUT))
-    dout[:, :NT] = 2 * wv[:, None] * d / (B * NT)
+    gI = 2 * wv[:, None] * d / (B * NT)
+    dout[:, :NT] = 2 * gI * re
+    dout[:, NT:2 * NT] = 2 * gI * im
     dout = bf16(dout)
     g = {"W2": dout.T @ u, "b2": dout.sum(0)}
     du = dout @ W2b
@@ -103,6 +112,6 @@ def loss_and_grads(p, x, y, D, E, w=None):
         dFm = bf16(np.einsum("qbn,qnk->qbk", dY, Mb[l]))
         dspec = from_modes(dFm, B) @ Db
         dh = np.einsum("ck,bcs->bks", Wpb[l], dzb) + dspec.reshape(B, C, NS)
-    g["wl"] = (dh * x[:, None, :]).sum(axis=(0, 2))
+    g["wl"] = np.einsum("bcs,ibs->ic", dh, x)
     g["bl"] = dh.sum(axis=(0, 2))
     return loss, g

@@ -46,7 +46,7 @@ def test_surrogate_training_reduces_loss_on_fixed_batch():
     x = net.pool(maps)
     # targets: a smooth function of the map the network can represent
     y = torch.tensor(rng.normal(0, 0.1, (B, Mdl.NT)), device="cuda", dtype=torch.float32)
-    y += x.mean(1, keepdim=True) * 5.0
+    y += x[0].mean(1, keepdim=True) * 5.0
     first = None
     for it in range(60):
         loss, g = net.loss_and_grads(x, y)
