@@ -431,7 +431,7 @@ def run_variants(m, args, torch, cells, ms_f64):
     return out
 
 
-def run_surrogate(n_train=16384, n_val=256, steps=30000, lr=2e-3, views=4, audit_frac=0.01):
+def run_surrogate(n_train=16384, n_val=256, steps=30000, lr=6e-4, views=4, audit_frac=0.01):
     """The learned far-field surrogate against the batched FDTD engine.
 
     Data: seeded random lamella maps (256^2, eps {1, 2.43}), each simulated

@@ -180,28 +180,31 @@ __global__ void __launch_bounds__(256) act_bwd_kernel(const float *dh, const flo
   }
 }
 
-// head pooling: h [B][C][32][32] -> flat [B][C*64] (mean of 4 x 4 blocks); backward broadcasts /16
-__global__ void head_pool_kernel(const bf16 *h, bf16 *flat, int B, int C)
+// head pooling: h [B][C][32][32] -> flat [B][C*g*g] (mean of hp x hp blocks, g = 32 / hp);
+// backward broadcasts / hp^2
+__global__ void head_pool_kernel(const bf16 *h, bf16 *flat, int B, int C, int hp)
 {
+  const int g = 32 / hp, gg = g * g;
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (size_t)B * C * 64) return;
-  const int p = i % 64, c = (i / 64) % C, b = (int)(i / (64 * (size_t)C));
-  const int px = p / 8, py = p % 8;
-  const bf16 *src = h + ((size_t)b * C + c) * 1024 + (px * 4) * 32 + py * 4;
+  if (i >= (size_t)B * C * gg) return;
+  const int p = i % gg, c = (i / gg) % C, b = (int)(i / (gg * (size_t)C));
+  const int px = p / g, py = p % g;
+  const bf16 *src = h + ((size_t)b * C + c) * 1024 + (px * hp) * 32 + py * hp;
   float s = 0;
-  for (int r = 0; r < 4; r++)
-    for (int q = 0; q < 4; q++) s += __bfloat162float(src[r * 32 + q]);
-  flat[i] = __float2bfloat16(s * (1.0f / 16.0f));
+  for (int r = 0; r < hp; r++)
+    for (int q = 0; q < hp; q++) s += __bfloat162float(src[r * 32 + q]);
+  flat[i] = __float2bfloat16(s / (float)(hp * hp));
 }
 
 // the backward of head_pool into channels-last dh [B][S][C]
-__global__ void head_unpool_kernel(const float *dflat, float *dh, int B, int C)
+__global__ void head_unpool_kernel(const float *dflat, float *dh, int B, int C, int hp)
 {
+  const int g = 32 / hp;
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (size_t)B * C * 1024) return;
   const int c = i % C, s = (i / C) % 1024, b = (int)(i / ((size_t)C * 1024));
-  const int px = (s / 32) / 4, py = (s % 32) / 4;
-  dh[i] = dflat[((size_t)b * C + c) * 64 + px * 8 + py] * (1.0f / 16.0f);
+  const int px = (s / 32) / hp, py = (s % 32) / hp;
+  dh[i] = dflat[((size_t)b * C + c) * g * g + px * g + py] / (float)(hp * hp);
 }
 
 // Amplitude head: row b of out holds the far-field amplitude, real parts in
@@ -359,14 +362,17 @@ int sg_act_bwd(const float *dh, const float *z, void *dz_cl, void *dz_cf, float 
   act_bwd_kernel<<<dim3(32, B), 256, 0, ST>>>(dh, z, (bf16 *)dz_cl, (bf16 *)dz_cf, dbp, act);
   RET;
 }
-int sg_head_pool(const void *h, void *flat, int B, int C, void *stream)
+int sg_head_pool(const void *h, void *flat, int B, int C, int hp, void *stream)
 {
-  head_pool_kernel<<<nb((size_t)B * C * 64, 256), 256, 0, ST>>>((const bf16 *)h, (bf16 *)flat, B, C);
+  if (hp != 1 && hp != 2 && hp != 4) return 1;
+  head_pool_kernel<<<nb((size_t)B * C * (1024 / (hp * hp)), 256), 256, 0, ST>>>((const bf16 *)h, (bf16 *)flat, B, C,
+                                                                                 hp);
   RET;
 }
-int sg_head_unpool(const float *dflat, float *dh, int B, int C, void *stream)
+int sg_head_unpool(const float *dflat, float *dh, int B, int C, int hp, void *stream)
 {
-  head_unpool_kernel<<<nb((size_t)B * C * 1024, 256), 256, 0, ST>>>(dflat, dh, B, C);
+  if (hp != 1 && hp != 2 && hp != 4) return 1;
+  head_unpool_kernel<<<nb((size_t)B * C * 1024, 256), 256, 0, ST>>>(dflat, dh, B, C, hp);
   RET;
 }
 int sg_amp_mse(const float *out, const float *y, const float *w, void *dout, float *loss, int B, int n, int nt,

@@ -20,7 +20,7 @@ def main(argv=None):
     ap.add_argument("--val", type=int, default=256)
     ap.add_argument("--steps", type=int, default=20000)
     ap.add_argument("--batch", type=int, default=128)
-    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--lr", type=float, default=6e-4)
     ap.add_argument("--no-shift", action="store_true", help="no random translations of the training maps")
     ap.add_argument("--views", type=int, default=1,
                     help="average the prediction over the structure, its mirror image and views-2 translations")

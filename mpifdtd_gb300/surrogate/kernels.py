@@ -47,8 +47,8 @@ _OPS: dict = {
     "sg_act_fwd": [P, P, P, I, I, I, P],
     "sg_act_bwd": [P, P, P, P, P, I, I, I, P],
     "sg_colsum_f32": [P, P, I, I, P],
-    "sg_head_pool": [P, P, I, I, P],
-    "sg_head_unpool": [P, P, I, I, P],
+    "sg_head_pool": [P, P, I, I, I, P],
+    "sg_head_unpool": [P, P, I, I, I, P],
     "sg_amp_mse": [P, P, P, P, P, I, I, I, P],
     "sg_gelu_bwd": [P, P, P, L_, P],
     "sg_colsum": [P, P, I, I, P],

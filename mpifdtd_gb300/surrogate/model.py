@@ -8,7 +8,7 @@ Architecture (B structures, C = 64 channels, 32 x 32 grid, Q = 256 modes):
            first and second moments of where the material sits in the
            block (x, y)                                         [NIN, B, 1024]
   h0     = sum_i x_i wl_i + bl                                  [B, C, 1024]
-  layer l = 0..3 (spectral mixing):
+  layer l = 0..NL-1 (spectral mixing):
     F    = h D^T      truncated 2-D DFT (modes kx -8..7, ky 0..15, cos/sin
                       rows of D, fixed)                         [B*C, 512]
     Fm   = permute(F)                                           [Q, B, 2C]
@@ -18,7 +18,7 @@ Architecture (B structures, C = 64 channels, 32 x 32 grid, Q = 256 modes):
     z   += h_cl wp_l^T + bp_l   point-wise channel mixing, same GEMM kernel
     h    = GELU(z) (no GELU after the last layer), kept channels-first [B, C, 1024]
            for the DFT GEMM and channels-last [B*1024, C] for the mixing GEMM
-  flat   = 4 x 4 mean pool of h                                 [B, C*64]
+  flat   = HP x HP mean pool of h                               [B, C*(32/HP)^2]
   u      = GELU(flat W1^T + b1)                                 [B, 512]
   out    = u W2^T + b2                                          [B, 22336]
   I      = out[:, :NT]^2 + out[:, NT:2 NT]^2                    [B, 31*360]
@@ -41,8 +41,9 @@ C = 64
 NIN = 5
 NS = 1024
 Q = 256
-NL = 4
+NL = 6          # spectral layers (4: 1.77 % held-out median, 6: 1.61 %, 8: 1.92 % on 16384 maps)
 H1 = 512
+HP = 4          # the head pools the last layer in HP x HP blocks: (32 / HP)^2 points per channel
 NT = 31 * 360
 NOUT = 22336
 
@@ -74,7 +75,8 @@ def init_params(seed=1234):
         p[f"M{l}"] = rng.normal(0, 0.5 / math.sqrt(2 * C), (Q, 2 * C, 2 * C))
         p[f"wp{l}"] = rng.normal(0, 1 / math.sqrt(C), (C, C))
         p[f"bp{l}"] = np.zeros(C)
-    p["W1"] = rng.normal(0, 1 / math.sqrt(C * 64), (H1, C * 64))
+    nf = C * (32 // HP) ** 2
+    p["W1"] = rng.normal(0, 1 / math.sqrt(nf), (H1, nf))
     p["b1"] = np.zeros(H1)
     p["W2"] = rng.normal(0, 1 / math.sqrt(H1), (NOUT, H1))
     p["b2"] = np.zeros(NOUT)
@@ -145,8 +147,8 @@ class FNO:
                 acts["Fm"].append(Fm.clone())
                 acts["z"].append(z)
             h, h_cl = hn, hn_cl
-        flat = self._e((B, C * 64), bf)
-        K.op("sg_head_pool", h, flat, B, C)
+        flat = self._e((B, C * (32 // HP) ** 2), bf)
+        K.op("sg_head_pool", h, flat, B, C, HP)
         u = self._e((B, H1), bf)
         pre1 = self._e((B, H1))
         K.gemm(flat, self.bf["W1"], u, bias=self.p["b1"], act=1, pre=pre1)
@@ -179,14 +181,14 @@ class FNO:
         K.gemm(dout, K.transpose(self.bf["W2"]), du)
         dpre1 = self._e((B, H1), bf)
         K.op("sg_gelu_bwd", du, a["pre1"], dpre1, B * H1)
-        g["W1"] = self._e((H1, C * 64))
+        g["W1"] = self._e((H1, C * (32 // HP) ** 2))
         K.gemm(K.transpose(dpre1), K.transpose(a["flat"]), g["W1"])
         g["b1"] = self._e((H1,))
         K.op("sg_colsum", dpre1, g["b1"], B, H1)
-        dflat = self._e((B, C * 64))
+        dflat = self._e((B, C * (32 // HP) ** 2))
         K.gemm(dpre1, K.transpose(self.bf["W1"]), dflat)
         dh = self._e((B, NS, C))                                       # channels-last
-        K.op("sg_head_unpool", dflat, dh, B, C)
+        K.op("sg_head_unpool", dflat, dh, B, C, HP)
         dz_cl = self._e((B, NS, C), bf)
         dz_cf = self._e((B, C, NS), bf)
         dYt = self._e((B * C, 2 * Q), bf)

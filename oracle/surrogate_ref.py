@@ -10,7 +10,7 @@ from __future__ import annotations
 
 import numpy as np
 
-C, NS, Q, NL, H1, NT, NOUT = 64, 1024, 256, 4, 512, 31 * 360, 22336
+C, NS, Q, NL, H1, NT, NOUT = 64, 1024, 256, 6, 512, 31 * 360, 22336
 
 
 def bf16(a):
@@ -51,12 +51,17 @@ def from_modes(Y, B):  # inverse of to_modes
     return Y.reshape(Q, B, 2, C).transpose(1, 3, 0, 2).reshape(B * C, 2 * Q)
 
 
+HP = 4   # the head's pooling factor (model.HP)
+
+
 def head_pool(h, B):
-    return h.reshape(B, C, 8, 4, 8, 4).mean(axis=(3, 5)).reshape(B, C * 64)
+    g = 32 // HP
+    return h.reshape(B, C, g, HP, g, HP).mean(axis=(3, 5)).reshape(B, C * g * g)
 
 
 def head_unpool(d, B):
-    return np.repeat(np.repeat(d.reshape(B, C, 8, 8), 4, axis=2), 4, axis=3).reshape(B, C, NS) / 16
+    g = 32 // HP
+    return np.repeat(np.repeat(d.reshape(B, C, g, g), HP, axis=2), HP, axis=3).reshape(B, C, NS) / (HP * HP)
 
 
 def loss_and_grads(p, x, y, D, E, w=None):
