@@ -238,6 +238,12 @@ int fdtd_get_status(fdtd_sim *sim, unsigned int *flags);
 #define FDTD_OPT_TBLOCK 5
 #define FDTD_OPT_TBLOCK_ROWS 6
 #define FDTD_OPT_TBLOCK_COLS 7   /* columns per lane of a tile: 1 (default), 2 (FP32, K = 2 or 4) */
+/* Broadband batch: steps between the running DFT's samples (rounded up to a
+ * multiple of the blocking depth K; default 16).  The pulse's spectrum lies
+ * far below the Nyquist frequency pi / stride of the sampled series for
+ * strides up to a few tens of steps on 5 nm cells, so the far field does not
+ * depend on it beyond rounding; fewer samples cost less FP64 work. */
+#define FDTD_OPT_DFT_STRIDE 8
 int fdtd_set_option(fdtd_sim *sim, int key, int value);
 int fdtd_get_option(fdtd_sim *sim, int key, int *value);
 

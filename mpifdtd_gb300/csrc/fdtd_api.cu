@@ -1701,11 +1701,12 @@ static int dft_bins(fdtd_sim *s, int nfreq, DftBins *bins)
   return FDTD_OK;
 }
 
-int fdtd_far_field_of_sums(fdtd_sim *s, const double *d_omega, int nfreq, const double2 *d_S, double2 *d_X)
+int fdtd_far_field_of_sums(fdtd_sim *s, const double *d_omega, int nfreq, const double2 *d_S, double2 *d_X,
+                           double scale)
 {
   if (!s->d_cells) return fail(FDTD_E_STATE, "no NTFF path (FDTD_CFG_NO_TIME_NTFF)");
   if (int rc = ensure_farfield(s)) return rc;
-  const std::complex<double> c = spectrum_coef(s);
+  const std::complex<double> c = spectrum_coef(s) * scale;
   DftView d{};
   d.omega = d_omega;
   d.nfreq = nfreq;

@@ -31,14 +31,19 @@
 // code reads it through the CW path's row table, one table per level) and the
 // phasors e^{i w t} of the block's sample time; after the tiles, a DFT kernel
 // reads the NTFF path samples the tiles left in their line buffers and adds
-// v e^{i w t} of the block's last level into per-instance sums
+// v e^{i w t} of the block's last level, every FDTD_OPT_DFT_STRIDE steps
+// (16 by default, a whole number of blocks), into per-instance sums
 // S[2][path][nfreq] (FP64), from which the time-domain NTFF's far field at
-// each frequency follows (fdtd_dft.cu).  One sample per K steps suffices: the
-// pulse's spectrum (a Gaussian of width 1/50 rad per step about its carrier,
-// 0.03-0.06 rad per step for 400-700 nm on 5 nm cells) is negligible long
-// before the Nyquist frequency pi/K of the decimated series, so its Fourier
-// sums at the wavelengths of interest are those of every step divided by K;
-// the incident pulse's sum (the normalisation) is taken over the same times.
+// each frequency follows (fdtd_dft.cu).  Sparse samples suffice: the pulse's
+// spectrum (a Gaussian of width 1/50 rad per step about its carrier, 0.03-0.06
+// rad per step for 400-700 nm on 5 nm cells) is negligible long before the
+// Nyquist frequency pi/stride of the sampled series (its nearest alias of a
+// wavelength of interest lies ~0.7 rad per step away at stride 8, where the
+// Gaussian is below e^-100), so the Fourier sums at the wavelengths of
+// interest are those of every step divided by the stride; the incident
+// pulse's sum (the normalisation) is taken over the same times.  The sums
+// hold the samples' sign and H average but not their 1/(4 pi C R), which the
+// far field applies.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -76,7 +81,7 @@ struct BatchInst {
   const SurfCell *cells;
   int ncell;
   double t0, w, inv_c;       // field.c:224-256: t0 = 500 - centre peak, carrier w_s, cos(0)/C
-  double coef;               // NTFF sample scale 1/(4 pi C R), mpiTM_UPML.c:852-854
+  double coef;               // NTFF sample scale 1/(4 pi C R), mpiTM_UPML.c:852-854 (applied by the far field)
 };
 
 constexpr int kBWarps = 4;
@@ -132,15 +137,18 @@ __global__ void batch_pulse_kernel(BatchInst<R> *inst, int K, const BatchClock *
 
 // Broadband: one warp per (instance, path cell), one lane per frequency.  The
 // E and H samples of the block's last level come from the tiles' line buffers
-// exactly as line_gather_kernel forms them (sign, H average, 1/(4 pi C R));
-// each lane adds v P[k] to the cell's sums.  Runs after both tile kernels of
-// the block and before the clock advances (the parity is the block's).  An
-// instance whose step_num ends inside the block takes no sample from it.
+// as line_gather_kernel forms them (sign, H average), in the fields' own
+// precision (GB300 issues one FP64 warp-instruction per 16 clocks per SM:
+// only the conversions and the accumulation run in FP64); each lane adds
+// v P[k] to the cell's sums.  Runs after both tile kernels of the block and
+// before the clock advances (the parity is the block's), in every `every`-th
+// block.  An instance whose step_num ends inside the block takes no sample.
 template <typename R, int K>
 __global__ void __launch_bounds__(128) batch_dft_kernel(const BatchInst<R> *inst, const BatchClock *clk,
-                                                         const double2 *P, int nfreq)
+                                                         const double2 *P, int nfreq, int every)
 {
   using T = typename Cplx<R>::T;
+  if ((clk->q + 1) % every != 0) return;
   const BatchInst<R> &I = inst[blockIdx.y];
   if (!I.src) return;
   const int c = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
@@ -157,10 +165,9 @@ __global__ void __launch_bounds__(128) batch_dft_kernel(const BatchInst<R> *inst
   tile::line_get(v, tb, K - 1, 0, i, j, e);
   tile::line_get(v, tb, K - 1, fh, i, j, h0);
   tile::line_get(v, tb, K - 1, fh, i1, j1, h1);
-  const double sg = sc.sign;
-  const double2 ev = make_double2(sg * (double)e.x * I.coef, sg * (double)e.y * I.coef);
-  const double2 hv = make_double2((sg * 0.5) * ((double)h0.x + (double)h1.x) * I.coef,
-                                  (sg * 0.5) * ((double)h0.y + (double)h1.y) * I.coef);
+  const R sg = (R)sc.sign, hs = sg * (R)0.5;  // exact: +-1, +-1/2
+  const double2 ev = make_double2((double)(sg * e.x), (double)(sg * e.y));
+  const double2 hv = make_double2((double)(hs * (h0.x + h1.x)), (double)(hs * (h0.y + h1.y)));
   for (int k = lane; k < nfreq; k += 32) {
     double2 *se = I.S + (size_t)c * nfreq + k, *sh = I.S + ((size_t)I.ncell + c) * nfreq + k;
     double2 ae = *se, ah = *sh;
@@ -241,6 +248,7 @@ struct fdtd_batch {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   void *d_inst = nullptr, *d_tint = nullptr, *d_tgen = nullptr, *d_clock = nullptr, *d_omega = nullptr;
   int n_int = 0, n_gen = 0, grid_int = 0, grid_gen = 0;
+  int dft_stride = 16, dft_every = 4;  // FDTD_OPT_DFT_STRIDE; blocks between DFT samples (stride / K)
   int planned_k = 0, planned_l = -1, planned_c = 0;
   std::vector<int> rows;  // tile rows of each instance
   cudaGraphExec_t graph = nullptr;
@@ -352,6 +360,11 @@ extern "C" int fdtd_batch_set_option(fdtd_batch *b, int key, int value)
   case FDTD_OPT_TBLOCK_ROWS:
     if (value < 0 || value > (1 << 20)) return set_error(FDTD_E_ARG, "tile rows must be in [0, 2^20]");
     b->L = value;
+    return FDTD_OK;
+  case FDTD_OPT_DFT_STRIDE:
+    if (value < 1 || value > 64) return set_error(FDTD_E_ARG, "DFT stride must be 1..64 steps");
+    b->dft_stride = value;
+    b->planned_k = 0;  // the graph bakes the stride in
     return FDTD_OK;
   case FDTD_OPT_TBLOCK_COLS:
     if (value != 1 && value != 2) return set_error(FDTD_E_ARG, "columns per lane must be 1 or 2");
@@ -493,6 +506,7 @@ static int batch_plan(fdtd_batch *b)
     b->graph = nullptr;
   }
   b->planned_k = K;
+  b->dft_every = std::max(1, (b->dft_stride + K - 1) / K);
   b->planned_l = b->L;
   b->planned_c = batch_cols(b);
   return FDTD_OK;
@@ -523,7 +537,7 @@ static void batch_block(fdtd_batch *b)
   cudaStreamWaitEvent(st, b->ev_join, 0);
   if (nfreq > 0)
     batch_dft_kernel<R, K><<<dim3((unsigned)((b->max_ncell + 3) / 4), (unsigned)n), 128, 0, st>>>(
-        inst, clk, (const double2 *)b->d_bb_phase, nfreq);
+        inst, clk, (const double2 *)b->d_bb_phase, nfreq, b->dft_every);
   batch_clock_kernel<<<1, 1, 0, st>>>((BatchClock *)b->d_clock, K);
 }
 
@@ -681,20 +695,21 @@ extern "C" int fdtd_batch_broadband(fdtd_batch *b, int nlam, const int *lambda_n
 
 // |A(w_k)|^2 of instance s: the incident pulse at x = 0 (field.c:224-256)
 // transformed with the samples' e^{i w t} at the times the DFT sampled (the
-// last level of every full K-step block: clock t = K-1, 2K-1, ...); dividing
-// by it leaves the response to a unit incident wave, the CW run's steady
-// state.  Cached by (t0, carrier, step_num, K): the instances of a sweep share it.
+// last level of every `dft_every`-th full K-step block: clock t = D-1,
+// 2D-1, ... with D = dft_every K); dividing by it leaves the response to a
+// unit incident wave, the CW run's steady state.  Cached by (t0, carrier,
+// step_num, D): the instances of a sweep share it.
 static const std::vector<double> &pulse_spectrum2(fdtd_batch *b, const fdtd_sim *s)
 {
-  const int nfreq = (int)b->bb_lam.size(), K = b->planned_k;
+  const int nfreq = (int)b->bb_lam.size(), D = b->planned_k * b->dft_every;
   const double t0 = -((s->geo.n_px / 2.0) * (cos(0.0) / s->c0)) + 500, w = s->geo.omega_s;
-  const std::array<double, 4> key{t0, w, (double)s->cfg.step_num, (double)K};
+  const std::array<double, 4> key{t0, w, (double)s->cfg.step_num, (double)D};
   for (const auto &e : b->bb_a2)
     if (e.first == key) return e.second;
   std::vector<double> a2(nfreq);
   for (int k = 0; k < nfreq; k++) {
     double ar = 0, ai = 0;
-    for (int t = K - 1; t < s->cfg.step_num; t += K) {
+    for (int t = D - 1; t < s->cfg.step_num; t += D) {
       const double r = -(t - t0), g = exp(-(r / 50.0) * (r / 50.0));
       const double ph = r * w + b->bb_freq[k] * (t - 1.0);
       ar += g * cos(ph);
@@ -718,7 +733,7 @@ static int broadband_spectra(fdtd_batch *b, int i0, int i1, double *out)
     if (!b->bb_S[i]) return set_error(FDTD_E_STATE, "no broadband run (fdtd_batch_broadband)");
     if (s->time != s->cfg.step_num) return set_error(FDTD_E_STATE, "instance %d has not run to its step_num", i);
     if (int rc = fdtd_far_field_of_sums(s, (const double *)b->d_bb_freq, nfreq, (const double2 *)b->bb_S[i],
-                                        (double2 *)b->d_bb_X + (size_t)i * per))
+                                        (double2 *)b->d_bb_X + (size_t)i * per, 1.0 / (4 * M_PI * s->c0 * 1.0e6)))
       return rc;
   }
   for (int i = i0; i < i1; i++) BCK(cudaStreamSynchronize(b->sims[i]->stream));

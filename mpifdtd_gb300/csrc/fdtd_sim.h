@@ -93,5 +93,7 @@ fdtd::StencilView<R> fdtd_view_of(fdtd_sim *s);
 // (device, E then H path samples, phasors of the E sample times) at the
 // frequencies omega[nfreq] (device, radians per step), with the simulation's
 // own path, shifts and spectrum coefficient (fdtd_api.cu; the broadband batch
-// keeps its sums outside the simulation).
-int fdtd_far_field_of_sums(fdtd_sim *s, const double *d_omega, int nfreq, const double2 *d_S, double2 *d_X);
+// keeps its sums outside the simulation), times `scale` (the batch's sums
+// leave out the samples' 1/(4 pi C R)).
+int fdtd_far_field_of_sums(fdtd_sim *s, const double *d_omega, int nfreq, const double2 *d_S, double2 *d_X,
+                           double scale);

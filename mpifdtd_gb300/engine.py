@@ -23,7 +23,7 @@ F64, F32 = 0, 1
 LAYOUT_GLOBAL, LAYOUT_SOLVER = 0, 1
 MODEL_NONE, MODEL_CIRCLE, MODEL_MORPHO, MODEL_ZIGZAG = 0, 1, 3, 5
 OPT_NTFF_MODE, OPT_NTFF_CHUNK, OPT_NTFF_BLOCK, OPT_ROWS = 1, 2, 3, 4
-OPT_TBLOCK, OPT_TBLOCK_ROWS, OPT_TBLOCK_COLS = 5, 6, 7
+OPT_TBLOCK, OPT_TBLOCK_ROWS, OPT_TBLOCK_COLS, OPT_DFT_STRIDE = 5, 6, 7, 8
 
 _ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "bad state", 5: "unsupported"}
 

@@ -19,10 +19,12 @@ LAMS = [400, 450, 500, 550, 600, 650, 700]
 FI = (800, 800, 5, 10, 500, 0, 1600)   # 160^2 cells of 5 nm, 10-cell UPML, carrier 500 nm
 
 
-def _broadband(precision, radii=(100.0, 150.0), eps=2.25, k=4):
+def _broadband(precision, radii=(100.0, 150.0), eps=2.25, k=4, stride=None):
     import mpifdtd_gb300 as m
     b = m.Batch("MPI_TM_UPML", [m.FieldInfo(*FI) for _ in radii], precision, no_time_ntff=False)
     b.set_option(m.OPT_TBLOCK, k)
+    if stride is not None:
+        b.set_option(m.OPT_DFT_STRIDE, stride)
     for s, r in zip(b.instances, radii):
         s.fill_model(m.MODEL_CIRCLE, [r, eps])
     b.broadband(LAMS)
@@ -51,12 +53,15 @@ def test_broadband_far_field_matches_mie_at_seven_wavelengths(precision):
             assert inten[k][0] >= 0.99 * inten[k].max() and inten[k][0] > 2 * inten[k][180], (r, lam)
 
 
-def test_broadband_dft_of_every_fourth_step_equals_every_step():
-    """The batch samples its DFT once per K-step block; with K = 1 it samples
-    every step.  The pulse's spectrum is far below the decimated series'
-    Nyquist frequency, so both give the same far fields (FP64 fields)."""
-    every, fourth = _broadband("f64", k=1), _broadband("f64", k=4)
-    for x, y in zip(fourth, every):
+def test_broadband_dft_of_every_sixteenth_step_equals_every_step():
+    """The batch samples its DFT every FDTD_OPT_DFT_STRIDE steps (16 by
+    default); with K = 1 and stride 1 it samples every step.  The pulse's
+    spectrum is far below the sampled series' Nyquist frequency, so both give
+    the same far fields (FP64 fields), and so does stride 4."""
+    every = _broadband("f64", k=1, stride=1)
+    for x, y in zip(_broadband("f64", k=4), every):
+        assert np.linalg.norm(x - y) / np.linalg.norm(y) < 1e-4
+    for x, y in zip(_broadband("f64", k=4, stride=4), every):
         assert np.linalg.norm(x - y) / np.linalg.norm(y) < 1e-4
 
 
