@@ -20,6 +20,7 @@
  */
 #ifndef MPIFDTD_GB300_H
 #define MPIFDTD_GB300_H
+#include <stddef.h>
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -213,9 +214,37 @@ int fdtd_get_stream(fdtd_sim *sim, void **stream);
 int fdtd_device_field(fdtd_sim *sim, int which, void **dptr, int *pitch, int *rows);
 
 /* Device status word: bit 0 = an NTFF deposit fell outside the accumulator
- * and was dropped (cannot happen within [0, step_num) on valid geometry). */
+ * and was dropped (cannot happen within [0, step_num) on valid geometry);
+ * bit 2 = fdtd_check_finite found a non-finite field value. */
 #define FDTD_STATUS_NTFF_RANGE 1u
+#define FDTD_STATUS_NONFINITE 4u
 int fdtd_get_status(fdtd_sim *sim, unsigned int *flags);
+
+/* Failure detection (the reference has none; a blown-up run only shows as
+ * NaN in its output files): counts the field values (every slot of the
+ * solver, PML auxiliaries included) with a non-finite real or imaginary part,
+ * on the device, and sets FDTD_STATUS_NONFINITE when there are any.  Nothing
+ * traps: the simulation stays usable. */
+int fdtd_check_finite(fdtd_sim *sim, long long *count);
+
+/* Checkpoint / resume (the reference has none: its reset only zeroes the
+ * fields, mpiTM_UPML.c:219-232).  An image holds the whole time-stepping
+ * state: the permittivity as given, every field slot, the time-domain NTFF
+ * accumulators, the running-DFT sums, the clock and the tuning options; the
+ * buffered NTFF steps are deposited first.  It loads into a simulation created
+ * with the same solver and fdtd_config (FDTD_E_ARG otherwise; a simulation
+ * without a running DFT takes the image's wavelengths), after which runs
+ * continue bit for bit as the saved simulation's would have.
+ *   fdtd_checkpoint_size   bytes of the image
+ *   fdtd_checkpoint_save   image into a host buffer of exactly that size
+ *   fdtd_checkpoint_load   image from a host buffer
+ *   fdtd_checkpoint_write  image into a file (64 MiB pinned staging chunks)
+ *   fdtd_checkpoint_read   image from a file */
+int fdtd_checkpoint_size(fdtd_sim *sim, size_t *bytes);
+int fdtd_checkpoint_save(fdtd_sim *sim, void *buf, size_t bytes);
+int fdtd_checkpoint_load(fdtd_sim *sim, const void *buf, size_t bytes);
+int fdtd_checkpoint_write(fdtd_sim *sim, const char *path);
+int fdtd_checkpoint_read(fdtd_sim *sim, const char *path);
 
 /* Tuning knobs (results are the same up to summation order).
  * NTFF deposit modes: 0 direct (three atomic adds per tap set every step),

@@ -487,6 +487,8 @@ static int derive_inv_eps(fdtd_sim *s)
   return FDTD_OK;
 }
 
+int fdtd_derive_inv_eps(fdtd_sim *s) { return derive_inv_eps(s); }
+
 // array offset of global cell (0,0): MPI arrays carry a one-cell halo
 static size_t global_origin(const fdtd_sim *s) { return s->mpi ? (size_t)s->pitch + 1 : 0; }
 

@@ -101,6 +101,7 @@ struct NtffWindow {
 // Device status bits (fdtd_get_status).
 constexpr unsigned int kStatusNtffRange = 1u;   // a deposit fell outside the accumulator
 constexpr unsigned int kStatusBadEps = 2u;      // a permittivity value was not finite and > 0
+constexpr unsigned int kStatusNonFinite = 4u;   // fdtd_check_finite found a non-finite field value
 
 // Launchers (fdtd_kernels.cu).  All take the stream they run on.
 template <typename R>

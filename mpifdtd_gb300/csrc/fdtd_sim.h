@@ -97,3 +97,8 @@ fdtd::StencilView<R> fdtd_view_of(fdtd_sim *s);
 // leave out the samples' 1/(4 pi C R)).
 int fdtd_far_field_of_sums(fdtd_sim *s, const double *d_omega, int nfreq, const double2 *d_S, double2 *d_X,
                            double scale);
+
+// 1/eps of the E components (or, for the split-field / NS solvers, a rebuild of
+// the per-cell coefficients before the next step) from the permittivity on the
+// device (fdtd_api.cu); FDTD_E_ARG if a value is not finite and > 0.
+int fdtd_derive_inv_eps(fdtd_sim *s);

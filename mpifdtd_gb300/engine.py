@@ -7,6 +7,7 @@ fails with the engine's own error.  There is no CPU path.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass
 from pathlib import Path
 
@@ -135,6 +136,12 @@ def load():
         "fdtd_batch_broadband": (I, [P, I, C.POINTER(I)]),
         "fdtd_batch_broadband_spectrum": (I, [P, I, dp]),
         "fdtd_batch_broadband_spectra": (I, [P, dp]),
+        "fdtd_check_finite": (I, [P, C.POINTER(C.c_longlong)]),
+        "fdtd_checkpoint_size": (I, [P, C.POINTER(C.c_size_t)]),
+        "fdtd_checkpoint_save": (I, [P, P, C.c_size_t]),
+        "fdtd_checkpoint_load": (I, [P, P, C.c_size_t]),
+        "fdtd_checkpoint_write": (I, [P, C.c_char_p]),
+        "fdtd_checkpoint_read": (I, [P, C.c_char_p]),
         "fdtd_last_error": (C.c_char_p, []),
         "fdtd_version": (C.c_char_p, []),
     }
@@ -156,6 +163,8 @@ def _dptr(a):
 
 
 CFG_NO_TIME_NTFF = 1
+STATUS_NTFF_RANGE = 1
+STATUS_NONFINITE = 4
 
 
 def _config(fi: FieldInfo, precision: int, flags: int = 0) -> _Config:
@@ -395,6 +404,41 @@ class Simulation:
 
     def reset(self):
         _check(self.lib.fdtd_reset(self.h))
+
+    # -- failure detection, checkpoint / resume
+    def check_finite(self) -> int:
+        """Number of field values with a non-finite part (fdtd_check_finite);
+        a non-zero count also sets STATUS_NONFINITE in `status`."""
+        n = C.c_longlong()
+        _check(self.lib.fdtd_check_finite(self.h, C.byref(n)))
+        return n.value
+
+    def checkpoint(self, path=None):
+        """The simulation's state as a checkpoint image: written to `path`, or
+        returned as a uint8 array when no path is given."""
+        if path is not None:
+            _check(self.lib.fdtd_checkpoint_write(self.h, os.fsencode(path)))
+            return None
+        n = C.c_size_t()
+        _check(self.lib.fdtd_checkpoint_size(self.h, C.byref(n)))
+        buf = np.empty(n.value, dtype=np.uint8)
+        _check(self.lib.fdtd_checkpoint_save(self.h, buf.ctypes.data, n.value))
+        return buf
+
+    def restore(self, image):
+        """Load a checkpoint image (a path, or the array `checkpoint()` returned)
+        into this simulation, created with the same solver and FieldInfo."""
+        if isinstance(image, (str, os.PathLike)):
+            with open(image, "rb") as f:
+                head = np.frombuffer(f.read(40), dtype=np.uint8)
+            _check(self.lib.fdtd_checkpoint_read(self.h, os.fsencode(image)))
+        else:
+            buf = np.ascontiguousarray(image, dtype=np.uint8)
+            head = buf[:40]
+            _check(self.lib.fdtd_checkpoint_load(self.h, buf.ctypes.data, buf.size))
+        nlam = int(head[36:40].view(np.int32)[0])     # the image's running-DFT wavelengths
+        if nlam > 0:
+            self._dft_n = nlam
 
     # -- outputs
     def _shape(self, layout):
