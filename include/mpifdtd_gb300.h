@@ -234,7 +234,9 @@ int fdtd_check_finite(fdtd_sim *sim, long long *count);
  * buffered NTFF steps are deposited first.  It loads into a simulation created
  * with the same solver and fdtd_config (FDTD_E_ARG otherwise; a simulation
  * without a running DFT takes the image's wavelengths), after which runs
- * continue bit for bit as the saved simulation's would have.
+ * continue as the saved simulation's would have: the fields and the DFT sums
+ * bit for bit, the NTFF accumulators to rounding (their deposit adds with
+ * FP64 atomics in no fixed order, as in any two runs).
  *   fdtd_checkpoint_size   bytes of the image
  *   fdtd_checkpoint_save   image into a host buffer of exactly that size
  *   fdtd_checkpoint_load   image from a host buffer

@@ -1722,6 +1722,22 @@ int fdtd_far_field_of_sums(fdtd_sim *s, const double *d_omega, int nfreq, const 
   return FDTD_OK;
 }
 
+int fdtd_far_field_of_sums_group(fdtd_sim *s, const double *d_omega, int nfreq, const double2 *const *d_S,
+                                 const int *d_idx, int nmaps, double2 *d_X, size_t x_stride, double scale,
+                                 cudaStream_t st)
+{
+  if (!s->d_cells) return fail(FDTD_E_STATE, "no NTFF path (FDTD_CFG_NO_TIME_NTFF)");
+  if (int rc = ensure_farfield(s)) return rc;
+  const std::complex<double> c = spectrum_coef(s) * scale;
+  DftBins bins{};
+  if (int rc = dft_bins(s, nfreq, &bins)) return rc;
+  launch_dft_farfield_group(ntff_view(s), d_S, d_idx, nmaps, d_omega, nfreq, s->tm ? 1 : 0, s->z0,
+                            (const double2 *)s->d_dirs, make_double2(c.real(), c.imag()), bins, d_X, x_stride, st);
+  s->launches += 2;
+  CK(cudaGetLastError());
+  return FDTD_OK;
+}
+
 // X[360][2 nlam]: the far-field component's Fourier sum at the two bins of each wavelength
 extern "C" int fdtd_dft_far_field(fdtd_sim *s, double *out_complex)
 {

@@ -49,6 +49,7 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <cstring>
 #include <new>
 #include <vector>
 
@@ -195,11 +196,20 @@ template <typename R, int K, bool TM, int CPL> constexpr int batch_min_blocks()
                   : sizeof(R) == 8 ? (K > 2 ? 3 : 4) : (K >= 8 ? 3 : K == 4 ? (TM ? 4 : 5) : 6);
 }
 
+// resident blocks per SM of the PML / edge work-list kernel: 4 (128 registers)
+// where the tile fits them with at most a few bytes of spill (TM, FP32, one
+// column per lane, K <= 4: 287 structures/s on the 256-cylinder sweep against
+// 272 at 3 blocks and 241 at 5), else 3
+template <typename R, int K, bool TM, int CPL> constexpr int batch_aux_blocks()
+{
+  return (TM && sizeof(R) == 4 && CPL == 1 && K <= 4) ? 4 : 3;
+}
+
 // Persistent: each warp claims the next tile of the list (sorted by cost,
 // largest first) until the list is exhausted, so the tail is one tile long
 // whatever the mix of tile heights and finished instances.
 template <typename R, int K, bool AUX, bool TM, int CPL>
-__global__ void __launch_bounds__(32 * kBWarps, (AUX ? 3 : batch_min_blocks<R, K, TM, CPL>()))
+__global__ void __launch_bounds__(32 * kBWarps, (AUX ? batch_aux_blocks<R, K, TM, CPL>() : batch_min_blocks<R, K, TM, CPL>()))
     batch_tile_kernel(const BatchInst<R> *__restrict__ inst, const int4 *__restrict__ tiles, int ntiles,
                       BatchClock *clk)
 {
@@ -261,6 +271,8 @@ struct fdtd_batch {
   std::vector<void *> bb_src;   // per instance: [kMaxTBlock][nxa] pulse rows (field precision)
   std::vector<void *> bb_S;     // per instance: [2][ncell][nfreq] DFT sums
   void *d_bb_X = nullptr;       // [n][360][nfreq] far fields of every instance
+  void *d_bb_Sptr = nullptr;    // [n] device copy of bb_S (the far field of a group of instances)
+  void *d_bb_idx = nullptr;     // [n] instances ordered by configuration group
   int max_nxa = 0, max_ncell = 0;
   std::vector<double> bb_freq;  // host copy of d_bb_freq
   // |A(w)|^2 of the incident pulse per (t0, carrier, step_num): the instances of a sweep share it
@@ -280,6 +292,8 @@ static void batch_free(fdtd_batch *b)
   cudaFree(b->d_bb_freq);
   cudaFree(b->d_bb_phase);
   cudaFree(b->d_bb_X);
+  cudaFree(b->d_bb_Sptr);
+  cudaFree(b->d_bb_idx);
   for (void *p : b->bb_src) cudaFree(p);
   for (void *p : b->bb_S) cudaFree(p);
   if (b->graph) cudaGraphExecDestroy(b->graph);
@@ -677,9 +691,11 @@ extern "C" int fdtd_batch_broadband(fdtd_batch *b, int nlam, const int *lambda_n
   cudaFree(b->d_bb_freq);
   cudaFree(b->d_bb_phase);
   cudaFree(b->d_bb_X);
+  cudaFree(b->d_bb_Sptr);
+  cudaFree(b->d_bb_idx);
   for (void *p : b->bb_src) cudaFree(p);
   for (void *p : b->bb_S) cudaFree(p);
-  b->d_bb_freq = b->d_bb_phase = b->d_bb_X = nullptr;
+  b->d_bb_freq = b->d_bb_phase = b->d_bb_X = b->d_bb_Sptr = b->d_bb_idx = nullptr;
   b->bb_src.assign(b->sims.size(), nullptr);
   b->bb_S.assign(b->sims.size(), nullptr);
   b->bb_lam.assign(lambda_nm, lambda_nm + nlam);
@@ -689,6 +705,8 @@ extern "C" int fdtd_batch_broadband(fdtd_batch *b, int nlam, const int *lambda_n
   BCK(cudaMemcpy(b->d_bb_freq, freq.data(), sizeof(double) * nlam, cudaMemcpyHostToDevice));
   BCK(cudaMalloc(&b->d_bb_phase, sizeof(double2) * (size_t)nlam));
   BCK(cudaMalloc(&b->d_bb_X, sizeof(double2) * 360 * (size_t)nlam * b->sims.size()));
+  BCK(cudaMalloc(&b->d_bb_Sptr, sizeof(void *) * b->sims.size()));
+  BCK(cudaMalloc(&b->d_bb_idx, sizeof(int) * b->sims.size()));
   b->planned_k = 0;  // buffers and graph are made again by the next run
   return FDTD_OK;
 }
@@ -721,25 +739,46 @@ static const std::vector<double> &pulse_spectrum2(fdtd_batch *b, const fdtd_sim 
   return b->bb_a2.back().second;
 }
 
-// Far fields of instances [i0, i1) into out[(i - i0)][nlam][360]: one
-// far-field launch per instance on its own stream, one copy back.
+// Far fields of instances [i0, i1) into out[(i - i0)][nlam][360].  Instances
+// created with the same configuration share one path: each such group is one
+// launch over all its maps (fdtd_far_field_of_sums_group), then one copy back.
 static int broadband_spectra(fdtd_batch *b, int i0, int i1, double *out)
 {
   if (b->bb_lam.empty()) return set_error(FDTD_E_STATE, "no broadband run (fdtd_batch_broadband)");
   const int nfreq = (int)b->bb_lam.size();
   const size_t per = 360 * (size_t)nfreq;
+  std::vector<std::vector<int>> groups;
   for (int i = i0; i < i1; i++) {
     fdtd_sim *s = b->sims[i];
     if (!b->bb_S[i]) return set_error(FDTD_E_STATE, "no broadband run (fdtd_batch_broadband)");
     if (s->time != s->cfg.step_num) return set_error(FDTD_E_STATE, "instance %d has not run to its step_num", i);
-    if (int rc = fdtd_far_field_of_sums(s, (const double *)b->d_bb_freq, nfreq, (const double2 *)b->bb_S[i],
-                                        (double2 *)b->d_bb_X + (size_t)i * per, 1.0 / (4 * M_PI * s->c0 * 1.0e6)))
-      return rc;
+    bool placed = false;
+    for (auto &g : groups)
+      if (std::memcmp(&b->sims[g[0]]->cfg, &s->cfg, sizeof(fdtd_config)) == 0) {
+        g.push_back(i);
+        placed = true;
+        break;
+      }
+    if (!placed) groups.push_back({i});
   }
-  for (int i = i0; i < i1; i++) BCK(cudaStreamSynchronize(b->sims[i]->stream));
+  std::vector<int> order;
+  for (const auto &g : groups) order.insert(order.end(), g.begin(), g.end());
+  BCK(cudaMemcpyAsync(b->d_bb_Sptr, b->bb_S.data(), sizeof(void *) * b->bb_S.size(), cudaMemcpyHostToDevice,
+                      b->stream));
+  BCK(cudaMemcpyAsync(b->d_bb_idx, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice, b->stream));
+  size_t off = 0;
+  for (const auto &g : groups) {
+    fdtd_sim *s = b->sims[g[0]];
+    if (int rc = fdtd_far_field_of_sums_group(s, (const double *)b->d_bb_freq, nfreq, (const double2 *const *)b->d_bb_Sptr,
+                                              (const int *)b->d_bb_idx + off, (int)g.size(), (double2 *)b->d_bb_X,
+                                              per, 1.0 / (4 * M_PI * s->c0 * 1.0e6), b->stream))
+      return rc;
+    off += g.size();
+  }
   std::vector<double2> X(per * (size_t)(i1 - i0));
-  BCK(cudaMemcpy(X.data(), (double2 *)b->d_bb_X + (size_t)i0 * per, sizeof(double2) * X.size(),
-                 cudaMemcpyDeviceToHost));
+  BCK(cudaMemcpyAsync(X.data(), (double2 *)b->d_bb_X + (size_t)i0 * per, sizeof(double2) * X.size(),
+                      cudaMemcpyDeviceToHost, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));  // also keeps `order` alive until its copy is done
   for (int i = i0; i < i1; i++) {
     const std::vector<double> &a2 = pulse_spectrum2(b, b->sims[i]);
     const double2 *x = X.data() + (size_t)(i - i0) * per;

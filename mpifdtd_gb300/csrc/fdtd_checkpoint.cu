@@ -16,8 +16,9 @@
 // solvers, the PML tables, the source tables, the NTFF path) is rebuilt from
 // the configuration and the permittivity; the buffered NTFF steps are
 // deposited before saving, so an image holds no pending work.  The tuning
-// options are stored and restored, so a resumed run rounds exactly as the
-// saved simulation would have.
+// options are stored and restored, so a resumed run's fields and DFT sums
+// round exactly as the saved simulation's would have (the NTFF accumulators
+// only to the order of their atomic adds, which no two runs share).
 #include <cuda_runtime.h>
 
 #include <algorithm>

@@ -205,6 +205,12 @@ struct DftBins {
 };
 void launch_dft_farfield(const NtffView &n, const DftView &d, int tm, double z0, const double2 *dir, double2 coef,
                          const DftBins &bins, double2 *X, cudaStream_t st);
+// The same far field for nmaps maps that share the path of n (one
+// configuration): map j's sums are S[idx[j]] ([2][ncell][nfreq]) and its far
+// field goes to X + idx[j] x_stride ([360][nfreq]); S and idx are device arrays.
+void launch_dft_farfield_group(const NtffView &n, const double2 *const *S, const int *idx, int nmaps,
+                               const double *omega, int nfreq, int tm, double z0, const double2 *dir, double2 coef,
+                               const DftBins &bins, double2 *X, size_t x_stride, cudaStream_t st);
 // The settings of a configuration that the reference hard-codes (fdtd_config:
 // courant_e4, pml_order, ntff_inset; 0 = the reference's value).
 inline double config_courant(const fdtd_config &c) { return c.courant_e4 > 0 ? c.courant_e4 / 1.0e4 : kC; }

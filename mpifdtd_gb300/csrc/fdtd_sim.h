@@ -97,6 +97,12 @@ fdtd::StencilView<R> fdtd_view_of(fdtd_sim *s);
 // leave out the samples' 1/(4 pi C R)).
 int fdtd_far_field_of_sums(fdtd_sim *s, const double *d_omega, int nfreq, const double2 *d_S, double2 *d_X,
                            double scale);
+// The same for nmaps instances that share s's configuration (hence its path):
+// instance idx[j]'s sums are d_S[idx[j]] and its far field goes to
+// d_X + idx[j] x_stride (d_S, d_idx: device arrays), launched on st.
+int fdtd_far_field_of_sums_group(fdtd_sim *s, const double *d_omega, int nfreq, const double2 *const *d_S,
+                                 const int *d_idx, int nmaps, double2 *d_X, size_t x_stride, double scale,
+                                 cudaStream_t st);
 
 // 1/eps of the E components (or, for the split-field / NS solvers, a rebuild of
 // the per-cell coefficients before the next step) from the permittivity on the

@@ -2,9 +2,11 @@
 (fdtd_check_finite), through the C ABI.
 
 A run interrupted by a checkpoint and resumed in a fresh simulation must end
-bit for bit where the uninterrupted run ends: fields, NTFF accumulators and
-running-DFT sums, with the buffered NTFF steps of the cut (37 steps: not a
-multiple of the 32-step deposit block) and the tuning options carried over.
+where the uninterrupted run ends, with the buffered NTFF steps of the cut (37
+steps: not a multiple of the 32-step deposit block) and the tuning options
+carried over: fields and running-DFT far fields bit for bit, the time-domain
+NTFF accumulators to rounding (their deposit adds with FP64 atomics in no
+fixed order, so two runs of one simulation differ there at the 1e-16 level).
 Failure detection is tested by injecting a NaN on the host: into a
 checkpoint image, which is then loaded.
 """
@@ -30,12 +32,17 @@ def _sim(solver, fi, precision="f64", tblock=0, dft=False, model=True):
 
 
 def _state(sim):
-    return [sim.field(w) for w in range(3)], [sim.ntff(w) for w in range(3)]
+    import mpifdtd_gb300 as m
+    upml = sim.solver in (m.TM_UPML_2D, m.TE_UPML_2D, m.MPI_TM_UPML_2D, m.MPI_TE_UPML_2D)
+    ntff = [sim.ntff(w) for w in range(3)] if upml else []   # NS / split-field: no time-domain NTFF
+    return [sim.field(w) for w in range(3)], ntff
 
 
 def _equal(a, b):
-    for x, y in zip(a[0] + a[1], b[0] + b[1]):
-        assert np.array_equal(x, y, equal_nan=False), np.abs(x - y).max()
+    for x, y in zip(a[0], b[0]):
+        assert np.array_equal(x, y), np.abs(x - y).max()
+    for x, y in zip(a[1], b[1]):
+        assert np.abs(x - y).max() <= 1e-13 * np.abs(y).max(), np.abs(x - y).max() / np.abs(y).max()
 
 
 CASES = [("MPI_TM_UPML", (400, 400, 5, 8, 500, 0, 200), "f64", 0, True),
