@@ -97,3 +97,30 @@ def test_broadband_rejects_te_and_missing_ntff_path():
     with pytest.raises(m.FdtdError):
         b.broadband(LAMS)
     b.close()
+
+
+def test_broadband_far_field_does_not_depend_on_the_batch_around_it():
+    """Instances of one configuration share a far-field launch (groups of up
+    to 16 maps over one path); an instance's spectrum is the same alone, in a
+    batch of 20 with a second configuration interleaved, and in any group
+    position."""
+    import mpifdtd_gb300 as m
+    other = (900, 900, 5, 10, 500, 0, 1600)
+    cfgs = [FI if q % 3 else other for q in range(20)]
+    radii = [90.0 + 4 * q for q in range(20)]
+
+    def run(fis, rs):
+        b = m.Batch("MPI_TM_UPML", [m.FieldInfo(*f) for f in fis], "f32", no_time_ntff=False)
+        b.set_option(m.OPT_TBLOCK, 4)
+        for s, r in zip(b.instances, rs):
+            s.fill_model(m.MODEL_CIRCLE, [r, 2.25])
+        b.broadband(LAMS)
+        b.run()
+        out = b.broadband_spectra()
+        b.close()
+        return out
+
+    mixed = run(cfgs, radii)
+    for q in (0, 1, 2, 17, 19):
+        alone = run([cfgs[q]], [radii[q]])[0]
+        np.testing.assert_array_equal(mixed[q], alone)
