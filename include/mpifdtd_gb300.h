@@ -260,9 +260,12 @@ int fdtd_checkpoint_read(fdtd_sim *sim, const char *path);
 #define FDTD_OPT_NTFF_CHUNK 2    /* mode 1: cells of a side per block (64..4096, 1024)  */
 #define FDTD_OPT_NTFF_BLOCK 3    /* mode 2: steps per deposit (1..64, default 32)       */
 #define FDTD_OPT_ROWS 4          /* stencil rows per thread: 1 (default), 2, 4 or 8     */
-/* Temporal blocking (MPI solvers, NTFF mode 2): fdtd_run advances K steps per
- * pass over the fields in HBM (K = 1, 2, 4; 8 in FP32; 0 = off, the default)
- * in tiles of 32-2K columns x FDTD_OPT_TBLOCK_ROWS rows (0 = automatic).  It
+/* Temporal blocking (UPML solvers, NTFF mode 2 or 3): fdtd_run advances K
+ * steps per pass over the fields in HBM (K = 1, 2, 4, and 8 in FP32 for the
+ * MPI solvers; 0 = off, the default) in tiles of 32-2K columns x
+ * FDTD_OPT_TBLOCK_ROWS rows (0 = automatic).  The serial solvers (TM_UPML,
+ * TE_UPML) block their own order, H half-step then E with the pulse
+ * (fdtdTM_upml.c:54-66, fdtdTE_upml.c:168-192).  It
  * holds a second set of fields on the device, and the fields move between the
  * two sets, so a pointer from fdtd_device_field is valid until the next
  * fdtd_run or fdtd_update.  fdtd_update (one step per call) never blocks. */
@@ -278,7 +281,7 @@ int fdtd_checkpoint_read(fdtd_sim *sim, const char *path);
 int fdtd_set_option(fdtd_sim *sim, int key, int value);
 int fdtd_get_option(fdtd_sim *sim, int key, int *value);
 
-/* Autotuner of the temporal blocking: times the one-step kernels and the
+/* Autotuner of the temporal blocking (MPI solvers): times the one-step kernels and the
  * blocked kernel at each depth K and tile height on this simulation's own
  * grid and fields (into the spare field set: the state does not change),
  * sets FDTD_OPT_TBLOCK / _ROWS / _COLS to the fastest, returns K and rows

@@ -38,7 +38,7 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp
                      f"-I{INCLUDE}"]
 CC_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-Wall", f"-I{INCLUDE}"]
 
-ENGINE_SOURCES = ["fdtd_kernels.cu", "fdtd_tblock.cu", "fdtd_batch.cu", "fdtd_api.cu", "fdtd_setup.cu", "ntff_noalloc.cu",
+ENGINE_SOURCES = ["fdtd_kernels.cu", "fdtd_tblock.cu", "fdtd_tblock_serial.cu", "fdtd_batch.cu", "fdtd_api.cu", "fdtd_setup.cu", "ntff_noalloc.cu",
                   "fdtd_farfield.cu", "fdtd_dft.cu", "fdtd_split.cu", "fdtd_checkpoint.cu"]
 # The model evaluators classify sub-cell samples with comparisons such as
 # px*px + py*py <= r*r (circleModel.c:45-57); a fused multiply-add could flip a

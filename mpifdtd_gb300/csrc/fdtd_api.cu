@@ -618,8 +618,9 @@ extern "C" int fdtd_set_option(fdtd_sim *s, int key, int value)
     if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8)
       return fail(FDTD_E_ARG, "temporal blocking depth must be 0, 1, 2, 4 or 8");
     if (value == 8 && !s->f32) return fail(FDTD_E_ARG, "temporal blocking depth 8 needs FP32 fields");
-    if (value > 0 && !s->mpi)
-      return fail(FDTD_E_UNSUPPORTED, "temporal blocking needs an MPI solver (E then H half-step)");
+    if (value > 0 && s->family != 0)
+      return fail(FDTD_E_UNSUPPORTED, "temporal blocking needs a UPML solver (split-field / NS: one step per launch)");
+    if (value == 8 && !s->mpi) return fail(FDTD_E_ARG, "the serial solvers block 1, 2 or 4 steps");
     s->tblock = value;
     return FDTD_OK;
   case FDTD_OPT_TBLOCK_ROWS:
@@ -1017,9 +1018,20 @@ static void enqueue_block(fdtd_sim *s, int K)
     t = t + 1.0;
     rc = 1.0 - exp(-pow(0.01 * t, 2));
   }
-  const double coef = 1.0 / (4 * M_PI * s->c0 * 1.0e6);  // mpiTM_UPML.c:852-854
+  if (!s->mpi) {  // serial: the pulse of the block's first step, as enqueue_step builds it
+    if (s->tm) {
+      tb.pulse[0] = pulse_step(s, t_first, 0, 0, 1.0);
+    } else {
+      const double co = cos((s->cfg.angle_deg + 90) * M_PI / 180.0);
+      const double si = sin((s->cfg.angle_deg + 90) * M_PI / 180.0);
+      if (co != 0.0) tb.pulse[0] = pulse_step(s, t_first, 0.5, 0.0, co);
+      if (si != 0.0) tb.pulse[1] = pulse_step(s, t_first, 0.0, 0.5, si);
+    }
+  }
+  const double coef = s->mpi ? 1.0 / (4 * M_PI * s->c0 * 1.0e6) : 1.0;  // mpiTM_UPML.c:852-854; serial: 1
   mark(s);
-  launch_tblock<R>(v, tb, K, s->tm, st);
+  if (s->mpi) launch_tblock<R>(v, tb, K, s->tm, st);
+  else launch_tblock_serial<R>(v, tb, K, s->tm, st);
   mark(s);
   mark(s);
   s->launches += (tb.s1 > tb.s0 && tb.nseg > 0 ? 1 : 0) + (tb.ntiles > 0 ? 1 : 0);
@@ -1391,8 +1403,8 @@ extern "C" int fdtd_run(fdtd_sim *s, int n_steps)
   if (n_steps > 0)
     if (int rc = before_step(s, s->time)) return rc;
   const int K = s->tblock;
-  const bool blocked = K > 0 && s->mpi && (s->ntff_mode == 3 || (s->ntff_mode == 2 && K <= s->ntff_block)) &&
-                       n_steps >= K;
+  const bool blocked = K > 0 && s->family == 0 &&
+                       (s->ntff_mode == 3 || (s->ntff_mode == 2 && K <= s->ntff_block)) && n_steps >= K;
   if (blocked)
     if (int rc = tb_prepare(s, K, s->tb_rows > 0 ? s->tb_rows : tb_auto_rows(s, K, tb_cols_for(s, K)),
                             tb_cols_for(s, K)))

@@ -147,11 +147,16 @@ struct TBlockView {
   int L;
   int cpl;             // columns per lane: 1, or 2 (FP32, K = 2 or 4)
   double2 sc[kMaxTBlock];  // CW source per level: ray_coef e^{-i w t}
+  SourceStep pulse[2];     // serial solvers: the pulse of the block's first step (TM [0] on Ez; TE [0] Ex, [1] Ey)
 };
 
 // Runs the interior and the general kernel of depth K (1, 2, 4 or 8).
 template <typename R>
 void launch_tblock(const StencilView<R> &v, const TBlockView<R> &tb, int K, bool tm, cudaStream_t st);
+// The same for the serial solvers (H half-step first, pulse source; K = 1, 2 or 4),
+// fdtd_tblock_serial.cu.
+template <typename R>
+void launch_tblock_serial(const StencilView<R> &v, const TBlockView<R> &tb, int K, bool tm, cudaStream_t st);
 // vals slots slot0 .. slot0+K-1 from the NTFF line samples of a blocked launch
 // (the samples ntff_gather_kernel takes from the fields after each step).
 template <typename R>

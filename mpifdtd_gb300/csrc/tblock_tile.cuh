@@ -601,6 +601,415 @@ __device__ __forceinline__ void te_tile(const StencilView<R> &v, const TBlockVie
   }
 }
 
+// ------------------------------------------------------------------ serial solvers
+//
+// The serial solvers step H before E (fdtdTM_upml.c:54-66, fdtdTE_upml.c:
+// 168-192) and drive E with the Gaussian pulse (field.c:224-256, tb.pulse:
+// the block's first step; level l adds l - 1 to its time).  Level l at front
+// row r computes H^l and then E^l, both at row h = r - l:
+//   H^l(h) from H^{l-1}(h), E^{l-1}(h) and E^{l-1}(h+1),
+//   E^l(h) from D^{l-1}(h), H^l(h) and H^l(h-1);
+// the level-0 state of front row r is E (D, J, 1/eps) and H (M) of row r.  With
+// the first front row r0 - K, E^l is exact from row r0 - K + l and H^l from
+// r0 - K + l - 1; each level loses one column on each side (H^l reads E^{l-1}
+// of column j+1, E^l reads H^l of column j-1).  The cell updates are those of
+// the one-step kernels (tm_h/tm_e, te_h/te_e).
+
+template <typename R, int K, bool AUX, int CPL = 1>
+__device__ __forceinline__ void tm_tile_hf(const StencilView<R> &v, const TBlockView<R> &tb, int strip, int r0,
+                                           int r1)
+{
+  static_assert(CPL == 1 || sizeof(R) == 4, "two columns per lane: FP32 only");
+  using T = typename Cplx<R>::T;
+  struct ES { T d, e, j; R ie; };
+  struct HS { T x, y, mx, my; };
+  const Lane<CPL> t = lane_of<K, CPL>(v, tb, strip, r0, r1);
+  const int j = t.j;
+  const size_t P = (size_t)v.P;
+  const T *Ez = v.f[0], *Dz = v.f[1], *Jz = v.f[2], *Hx = v.f[3], *Hy = v.f[4], *Mx = v.f[5], *My = v.f[6];
+  const R *IE = v.inv_eps[0];
+  ES E[K + 1][CPL];
+  HS H[K + 1][CPL];
+#pragma unroll
+  for (int l = 0; l <= K; l++)
+#pragma unroll
+    for (int q = 0; q < CPL; q++) {
+      E[l][q].d = E[l][q].e = E[l][q].j = czero<T>();
+      E[l][q].ie = (R)1;
+      H[l][q].x = H[l][q].y = H[l][q].mx = H[l][q].my = czero<T>();
+    }
+  auto load0 = [&](int r, ES *n, HS *m) {  // E (D, J, 1/eps) and H (M) of row r
+#pragma unroll
+    for (int q = 0; q < CPL; q++) {
+      n[q].d = n[q].e = n[q].j = czero<T>();
+      n[q].ie = (R)1;
+      m[q].x = m[q].y = m[q].mx = m[q].my = czero<T>();
+    }
+    if (r >= 1 && r <= v.ni) {
+      const size_t k = (size_t)r * P + j;
+      T ez[CPL], d[CPL], hx[CPL], hy[CPL];
+      R ie[CPL];
+      ld_cols<CPL>(Ez + k, t.jact, ez);
+      ld_cols<CPL>(Dz + k, t.jact, d);
+      ld_real<CPL>(IE + k, t.jact, ie);
+      ld_cols<CPL>(Hx + k, t.jact, hx);
+      ld_cols<CPL>(Hy + k, t.jact, hy);
+#pragma unroll
+      for (int q = 0; q < CPL; q++) {
+        n[q].e = ez[q];
+        n[q].d = d[q];
+        n[q].ie = ie[q];
+        m[q].x = hx[q];
+        m[q].y = hy[q];
+        if (AUX && t.jact[q] && !(t.yin[q] && x_in(v, r))) {
+          n[q].j = ldro(Jz + k + q);
+          m[q].mx = ldro(Mx + k + q);
+          m[q].my = ldro(My + k + q);
+        }
+      }
+    }
+  };
+  ES pe0[CPL], pe1[CPL];
+  HS ph0[CPL], ph1[CPL];
+  load0(t.r0 - K, pe0, ph0);
+  load0(t.r0 - K + 1, pe1, ph1);
+#pragma unroll 1
+  for (int r = t.r0 - K; r < t.r1 + K; r++) {
+    ES eo[CPL];  // E^{l-1} of row r - l (the previous front row's), entering level l
+    HS ho[CPL];  // H^{l-1} of row r - l
+#pragma unroll
+    for (int q = 0; q < CPL; q++) {
+      eo[q] = E[0][q];
+      ho[q] = H[0][q];
+      E[0][q] = pe0[q];
+      H[0][q] = ph0[q];
+      pe0[q] = pe1[q];
+      ph0[q] = ph1[q];
+    }
+    load0(r + 2, pe1, ph1);
+    {  // rows the tile loads two row-steps later
+      const int rp = r + 4;
+      if (rp >= 1 && rp <= v.ni) {
+        prefetch_row<CPL>(Ez + (size_t)rp * P + j, sizeof(T));
+        prefetch_row<CPL>(Dz + (size_t)rp * P + j, sizeof(T));
+        prefetch_row<CPL>(IE + (size_t)rp * P + j, sizeof(R));
+        prefetch_row<CPL>(Hx + (size_t)rp * P + j, sizeof(T));
+        prefetch_row<CPL>(Hy + (size_t)rp * P + j, sizeof(T));
+      }
+    }
+#pragma unroll
+    for (int l = 1; l <= K; l++) {
+      const int h = r - l;
+      const bool hrow = h >= 1 && h <= v.ni;
+      // H half (calcMB + calcH) at row h from E^{l-1} of rows h (eo) and h + 1 (E[l-1])
+      T ezr[CPL];  // Ez^{l-1}(h, j+1)
+      ezr[CPL - 1] = shdn(eo[0].e);
+#pragma unroll
+      for (int q = 0; q + 1 < CPL; q++) ezr[q] = eo[q + 1].e;
+      HS hn[CPL];
+#pragma unroll
+      for (int q = 0; q < CPL; q++) {
+        hn[q].x = hn[q].y = hn[q].mx = hn[q].my = czero<T>();
+        if (!AUX || (t.jact[q] && hrow)) {
+          const T dEx = csub(ezr[q], eo[q].e);
+          const T dEy = csub(eo[q].e, E[l - 1][q].e);
+          T hx = ho[q].x, hy = ho[q].y;
+          if (!AUX || (t.yin[q] && x_in(v, h))) {
+            hx.x -= v.inv_mu * dEx.x; hx.y -= v.inv_mu * dEx.y;
+            hy.x -= v.inv_mu * dEy.x; hy.y -= v.inv_mu * dEy.y;
+          } else {
+            T mx = ho[q].mx, my = ho[q].my;
+            tm_h_pml(v, h, j + q, dEx, dEy, hx, hy, mx, my);
+            hn[q].mx = mx;
+            hn[q].my = my;
+          }
+          hn[q].x = hx;
+          hn[q].y = hy;
+        }
+      }
+      HS hold[CPL];  // H^l of row h - 1
+#pragma unroll
+      for (int q = 0; q < CPL; q++) {
+        hold[q] = H[l][q];
+        H[l][q] = hn[q];
+      }
+      // E half (calcJD + calcE + pulse) at row h from H^l of rows h (hn) and h - 1 (hold)
+      T hxb[CPL];  // Hx^l(h, j-1)
+      hxb[0] = shup(hn[CPL - 1].x);
+#pragma unroll
+      for (int q = 1; q < CPL; q++) hxb[q] = hn[q - 1].x;
+      ES en[CPL];
+#pragma unroll
+      for (int q = 0; q < CPL; q++) {
+        en[q].ie = eo[q].ie;
+        en[q].d = en[q].e = en[q].j = czero<T>();
+        if (!AUX || (t.jact[q] && hrow)) {
+          T curl;
+          curl.x = ((hn[q].y.x - hold[q].y.x) - hn[q].x.x) + hxb[q].x;
+          curl.y = ((hn[q].y.y - hold[q].y.y) - hn[q].x.y) + hxb[q].y;
+          T dz = eo[q].d;
+          if (!AUX || (t.yin[q] && x_in(v, h))) {
+            dz = cadd(dz, curl);
+          } else {
+            T jz = eo[q].j;
+            tm_e_pml(v, h, j + q, curl, dz, jz);
+            en[q].j = jz;
+          }
+          en[q].d = dz;
+          T ez = dz;
+          if (!is_one(en[q].ie)) {
+            ez = cscale(dz, en[q].ie);
+            if (tb.pulse[0].kind) ez = pulse_source_call<R>(tb.pulse[0], h, j + q, en[q].ie, ez, (double)(l - 1));
+          }
+          en[q].e = ez;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < CPL; q++) {
+        const ES eold = E[l][q];  // E^l of row h - 1
+        E[l][q] = en[q];
+        if (t.lines && t.own[q] && h >= t.r0 && h < t.r1) {
+          line_put(v, tb, t, q, l - 1, h, 0, en[q].e);
+          line_put(v, tb, t, q, l - 1, h, 1, hn[q].x);
+          line_put(v, tb, t, q, l - 1, h, 2, hn[q].y);
+        }
+        eo[q] = eold;
+        ho[q] = hold[q];
+      }
+    }
+    {  // level K is final: E and H of row r - K
+      const int h = r - K;
+      if (h >= t.r0 && h < t.r1) {
+        const size_t k = (size_t)h * P + j;
+        T d[CPL], ez[CPL], hx[CPL], hy[CPL];
+#pragma unroll
+        for (int q = 0; q < CPL; q++) {
+          d[q] = E[K][q].d;
+          ez[q] = E[K][q].e;
+          hx[q] = H[K][q].x;
+          hy[q] = H[K][q].y;
+          if (AUX && t.own[q] && !(t.yin[q] && x_in(v, h))) {
+            tb.out[2][k + q] = E[K][q].j;
+            tb.out[5][k + q] = H[K][q].mx;
+            tb.out[6][k + q] = H[K][q].my;
+          }
+        }
+        st_cols<CPL>(tb.out[1] + k, t.own, d);
+        st_cols<CPL>(tb.out[0] + k, t.own, ez);
+        st_cols<CPL>(tb.out[3] + k, t.own, hx);
+        st_cols<CPL>(tb.out[4] + k, t.own, hy);
+      }
+    }
+  }
+}
+
+template <typename R, int K, bool AUX, int CPL = 1>
+__device__ __forceinline__ void te_tile_hf(const StencilView<R> &v, const TBlockView<R> &tb, int strip, int r0,
+                                           int r1)
+{
+  static_assert(CPL == 1 || sizeof(R) == 4, "two columns per lane: FP32 only");
+  using T = typename Cplx<R>::T;
+  struct ES { T dx, dy, ex, ey, jx, jy; R iex, iey; };
+  struct HS { T z, mz; };
+  const Lane<CPL> t = lane_of<K, CPL>(v, tb, strip, r0, r1);
+  const int j = t.j;
+  const size_t P = (size_t)v.P;
+  const T *Ex = v.f[0], *Ey = v.f[1], *Dx = v.f[2], *Dy = v.f[3], *Jx = v.f[4], *Jy = v.f[5], *Hz = v.f[6],
+          *Mz = v.f[7];
+  const R *IEX = v.inv_eps[0], *IEY = v.inv_eps[1];
+  ES E[K + 1][CPL];
+  HS H[K + 1][CPL];
+#pragma unroll
+  for (int l = 0; l <= K; l++)
+#pragma unroll
+    for (int q = 0; q < CPL; q++) {
+      E[l][q].dx = E[l][q].dy = E[l][q].ex = E[l][q].ey = E[l][q].jx = E[l][q].jy = czero<T>();
+      E[l][q].iex = E[l][q].iey = (R)1;
+      H[l][q].z = H[l][q].mz = czero<T>();
+    }
+  auto load0 = [&](int r, ES *n, HS *m) {  // E (D, J, 1/eps) and H (M) of row r
+#pragma unroll
+    for (int q = 0; q < CPL; q++) {
+      n[q].dx = n[q].dy = n[q].ex = n[q].ey = n[q].jx = n[q].jy = czero<T>();
+      n[q].iex = n[q].iey = (R)1;
+      m[q].z = m[q].mz = czero<T>();
+    }
+    if (r >= 1 && r <= v.ni) {
+      const size_t k = (size_t)r * P + j;
+      T ex[CPL], ey[CPL], dx[CPL], dy[CPL], hz[CPL];
+      R iex[CPL], iey[CPL];
+      ld_cols<CPL>(Ex + k, t.jact, ex);
+      ld_cols<CPL>(Ey + k, t.jact, ey);
+      ld_cols<CPL>(Dx + k, t.jact, dx);
+      ld_cols<CPL>(Dy + k, t.jact, dy);
+      ld_real<CPL>(IEX + k, t.jact, iex);
+      ld_real<CPL>(IEY + k, t.jact, iey);
+      ld_cols<CPL>(Hz + k, t.jact, hz);
+#pragma unroll
+      for (int q = 0; q < CPL; q++) {
+        n[q].ex = ex[q];
+        n[q].ey = ey[q];
+        n[q].dx = dx[q];
+        n[q].dy = dy[q];
+        n[q].iex = iex[q];
+        n[q].iey = iey[q];
+        m[q].z = hz[q];
+        if (AUX && t.jact[q] && !(t.yin[q] && x_in(v, r))) {
+          n[q].jx = ldro(Jx + k + q);
+          n[q].jy = ldro(Jy + k + q);
+          m[q].mz = ldro(Mz + k + q);
+        }
+      }
+    }
+  };
+  ES pe0[CPL], pe1[CPL];
+  HS ph0[CPL], ph1[CPL];
+  load0(t.r0 - K, pe0, ph0);
+  load0(t.r0 - K + 1, pe1, ph1);
+#pragma unroll 1
+  for (int r = t.r0 - K; r < t.r1 + K; r++) {
+    ES eo[CPL];
+    HS ho[CPL];
+#pragma unroll
+    for (int q = 0; q < CPL; q++) {
+      eo[q] = E[0][q];
+      ho[q] = H[0][q];
+      E[0][q] = pe0[q];
+      H[0][q] = ph0[q];
+      pe0[q] = pe1[q];
+      ph0[q] = ph1[q];
+    }
+    load0(r + 2, pe1, ph1);
+    {  // rows the tile loads two row-steps later
+      const int rp = r + 4;
+      if (rp >= 1 && rp <= v.ni) {
+        prefetch_row<CPL>(Ex + (size_t)rp * P + j, sizeof(T));
+        prefetch_row<CPL>(Ey + (size_t)rp * P + j, sizeof(T));
+        prefetch_row<CPL>(Dx + (size_t)rp * P + j, sizeof(T));
+        prefetch_row<CPL>(Dy + (size_t)rp * P + j, sizeof(T));
+        prefetch_row<CPL>(IEX + (size_t)rp * P + j, sizeof(R));
+        prefetch_row<CPL>(IEY + (size_t)rp * P + j, sizeof(R));
+        prefetch_row<CPL>(Hz + (size_t)rp * P + j, sizeof(T));
+      }
+    }
+#pragma unroll
+    for (int l = 1; l <= K; l++) {
+      const int h = r - l;
+      const bool hrow = h >= 1 && h <= v.ni;
+      // H half (calcMB + calcH) at row h from E^{l-1} of rows h (eo) and h + 1 (E[l-1])
+      T ext[CPL];  // Ex^{l-1}(h, j+1)
+      ext[CPL - 1] = shdn(eo[0].ex);
+#pragma unroll
+      for (int q = 0; q + 1 < CPL; q++) ext[q] = eo[q + 1].ex;
+      HS hn[CPL];
+#pragma unroll
+      for (int q = 0; q < CPL; q++) {
+        hn[q].z = hn[q].mz = czero<T>();
+        if (!AUX || (t.jact[q] && hrow)) {
+          T ce;  // Ey[i+1] - Ey - Ex[j+1] + Ex
+          ce.x = ((E[l - 1][q].ey.x - eo[q].ey.x) - ext[q].x) + eo[q].ex.x;
+          ce.y = ((E[l - 1][q].ey.y - eo[q].ey.y) - ext[q].y) + eo[q].ex.y;
+          T hz = ho[q].z;
+          if (!AUX || (t.yin[q] && x_in(v, h))) {
+            hz.x -= v.inv_mu * ce.x;
+            hz.y -= v.inv_mu * ce.y;
+          } else {
+            T mz = ho[q].mz;
+            te_h_pml(v, h, j + q, ce, hz, mz);
+            hn[q].mz = mz;
+          }
+          hn[q].z = hz;
+        }
+      }
+      HS hold[CPL];  // H^l of row h - 1
+#pragma unroll
+      for (int q = 0; q < CPL; q++) {
+        hold[q] = H[l][q];
+        H[l][q] = hn[q];
+      }
+      // E half (calcJD + calcE + pulse) at row h from H^l of rows h (hn) and h - 1 (hold)
+      T hzb[CPL];  // Hz^l(h, j-1)
+      hzb[0] = shup(hn[CPL - 1].z);
+#pragma unroll
+      for (int q = 1; q < CPL; q++) hzb[q] = hn[q - 1].z;
+      ES en[CPL];
+#pragma unroll
+      for (int q = 0; q < CPL; q++) {
+        en[q].iex = eo[q].iex;
+        en[q].iey = eo[q].iey;
+        en[q].dx = en[q].dy = en[q].ex = en[q].ey = en[q].jx = en[q].jy = czero<T>();
+        if (!AUX || (t.jact[q] && hrow)) {
+          const T hzk = hn[q].z;
+          const T cxv = csub(hzk, hzb[q]);  // Hz - Hz[j-1]
+          T cyv;                            // -Hz + Hz[i-1]
+          cyv.x = -hzk.x + hold[q].z.x;
+          cyv.y = -hzk.y + hold[q].z.y;
+          T dx = eo[q].dx, dy = eo[q].dy;
+          if (!AUX || (t.yin[q] && x_in(v, h))) {
+            dx = cadd(dx, cxv);
+            dy = cadd(dy, cyv);
+          } else {
+            T jx = eo[q].jx, jy = eo[q].jy;
+            te_e_pml(v, h, j + q, cxv, cyv, dx, dy, jx, jy);
+            en[q].jx = jx;
+            en[q].jy = jy;
+          }
+          en[q].dx = dx;
+          en[q].dy = dy;
+          T ex = dx, ey = dy;
+          if (!is_one(en[q].iex)) {
+            ex = cscale(dx, en[q].iex);
+            if (tb.pulse[0].kind) ex = pulse_source_call<R>(tb.pulse[0], h, j + q, en[q].iex, ex, (double)(l - 1));
+          }
+          if (!is_one(en[q].iey)) {
+            ey = cscale(dy, en[q].iey);
+            if (tb.pulse[1].kind) ey = pulse_source_call<R>(tb.pulse[1], h, j + q, en[q].iey, ey, (double)(l - 1));
+          }
+          en[q].ex = ex;
+          en[q].ey = ey;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < CPL; q++) {
+        const ES eold = E[l][q];  // E^l of row h - 1
+        E[l][q] = en[q];
+        if (t.lines && t.own[q] && h >= t.r0 && h < t.r1) {
+          line_put(v, tb, t, q, l - 1, h, 0, en[q].ex);
+          line_put(v, tb, t, q, l - 1, h, 1, en[q].ey);
+          line_put(v, tb, t, q, l - 1, h, 2, hn[q].z);
+        }
+        eo[q] = eold;
+        ho[q] = hold[q];
+      }
+    }
+    {  // level K is final: E and H of row r - K
+      const int h = r - K;
+      if (h >= t.r0 && h < t.r1) {
+        const size_t k = (size_t)h * P + j;
+        T dx[CPL], dy[CPL], ex[CPL], ey[CPL], hz[CPL];
+#pragma unroll
+        for (int q = 0; q < CPL; q++) {
+          dx[q] = E[K][q].dx;
+          dy[q] = E[K][q].dy;
+          ex[q] = E[K][q].ex;
+          ey[q] = E[K][q].ey;
+          hz[q] = H[K][q].z;
+          if (AUX && t.own[q] && !(t.yin[q] && x_in(v, h))) {
+            tb.out[4][k + q] = E[K][q].jx;
+            tb.out[5][k + q] = E[K][q].jy;
+            tb.out[7][k + q] = H[K][q].mz;
+          }
+        }
+        st_cols<CPL>(tb.out[2] + k, t.own, dx);
+        st_cols<CPL>(tb.out[3] + k, t.own, dy);
+        st_cols<CPL>(tb.out[0] + k, t.own, ex);
+        st_cols<CPL>(tb.out[1] + k, t.own, ey);
+        st_cols<CPL>(tb.out[6] + k, t.own, hz);
+      }
+    }
+  }
+}
+
 // NTFF surface samples of level lev from the line buffers (zero on the halo ring)
 template <typename R>
 __device__ __forceinline__ bool line_get(const StencilView<R> &v, const TBlockView<R> &tb, int lev, int f, int i,

@@ -152,11 +152,15 @@ def test_autotune_keeps_state_and_picks_a_valid_setting():
         assert rel(sim.field(w), ref[f"field{w}"]) <= TOL
 
 
-def test_tblock_rejects_serial_solver_and_fp64_depth8():
+def test_tblock_rejects_split_ns_solvers_and_bad_depths():
     m = _engine()
-    s = m.Simulation("TM_UPML", m.FieldInfo(300, 300, 5, 8, 100, 0, 100))
+    for solver in ("TM_2D", "NS_TE_2D"):               # split-field / NS: one step per launch
+        s = m.Simulation(solver, m.FieldInfo(300, 300, 5, 8, 100, 0, 100))
+        with pytest.raises(m.FdtdError):
+            s.set_option(m.OPT_TBLOCK, 2)
+    s = m.Simulation("TM_UPML", m.FieldInfo(300, 300, 5, 8, 100, 0, 100), "f32")
     with pytest.raises(m.FdtdError):
-        s.set_option(m.OPT_TBLOCK, 2)
+        s.set_option(m.OPT_TBLOCK, 8)                  # serial solvers: K = 1, 2, 4
     s = m.Simulation("MPI_TM_UPML", m.FieldInfo(300, 300, 5, 8, 100, 0, 100))
     with pytest.raises(m.FdtdError):
         s.set_option(m.OPT_TBLOCK, 8)
@@ -164,3 +168,76 @@ def test_tblock_rejects_serial_solver_and_fp64_depth8():
         s.set_option(m.OPT_TBLOCK, 3)
     with pytest.raises(m.FdtdError):
         s.set_option(m.OPT_TBLOCK_COLS, 2)   # FP64 fields
+
+
+# ---- the serial solvers (fdtdTM_upml.c:54-66, fdtdTE_upml.c:168-192): H half-step first, Gaussian pulse
+
+SERIAL_CASES = ["ser_tm_circle", "ser_te_circle"]
+
+
+@pytest.mark.parametrize("k,rows", [(1, 0), (2, 7), (4, 0), (4, 5), (2, 64)])
+@pytest.mark.parametrize("name", SERIAL_CASES)
+def test_tblock_serial_fp64_matches_reference_golden(name, k, rows):
+    """Fields, NTFF accumulators and the far-field spectrum (ntff*_TimeOutput)
+    of blocked serial runs against the reference's own serial solvers; the
+    TE case (20 degrees) drives both E components with the pulse."""
+    c = CASES[name]
+    sim = _run(name, k=k, rows=rows)
+    launches_blocked = sim.launches
+    got = capture([sim.field(w) for w in range(3)], [sim.eps(w) for w in range(3)],
+                  [sim.ntff(w) for w in range(3)], sim.array_size, c["kind"], c.get("rows", "all"))
+    got["spectrum"] = sim.spectrum()
+    ref = _golden(name)
+    bad = compare(got, {key: v for key, v in ref.items() if key.startswith(("field", "ntff", "spectrum"))}, TOL)
+    assert not bad, (name, k, rows, bad)
+    assert sim.status == 0
+    one = _run(name, k=0)
+    if k > 1:   # the blocked kernels ran: fewer launches than one step at a time
+        assert launches_blocked < one.launches, (launches_blocked, one.launches)
+
+
+@pytest.mark.parametrize("solver,angle", [("TM_UPML", 0), ("TE_UPML", 30)])
+@pytest.mark.parametrize("k,cols", [(1, 1), (2, 1), (4, 1), (2, 2), (4, 2)])
+def test_tblock_serial_fp32_equals_fp32_one_step(solver, angle, k, cols):
+    """1044^2 Mie cylinder, pulse source, interior and PML tiles: FP32 blocked
+    against FP32 one-step (same cell arithmetic up to FMA contraction)."""
+    m = _engine()
+    fi = m.FieldInfo(5220, 5220, 5, 10, 500, angle, 1200)
+    sims = []
+    for kk in (0, k):
+        s = m.Simulation(solver, fi, "f32")
+        s.fill_model(m.MODEL_CIRCLE, [500.0, 2.25])
+        s.set_option(m.OPT_TBLOCK, kk)
+        s.set_option(m.OPT_TBLOCK_COLS, cols)
+        s.set_option(m.OPT_TBLOCK_ROWS, 48 if cols == 2 else 0)
+        s.run(700)            # the pulse reaches the cylinder after ~500 steps
+        sims.append(s)
+    for w in range(3):
+        assert rel(sims[1].field(w), sims[0].field(w)) < 5e-6, (solver, k, w)
+        assert rel(sims[1].ntff(w), sims[0].ntff(w)) < 5e-6, (solver, k, w)
+    assert np.abs(sims[0].field(0)).max() > 0
+
+
+def test_tblock_serial_runs_split_across_calls_and_updates():
+    """A serial run through fdtd_update steps, then blocked runs whose lengths
+    K does not divide, ends where the reference's run does."""
+    m = _engine()
+    name = "ser_tm_circle"
+    c = CASES[name]
+    ref = _golden(name)
+    sim = m.Simulation(c["solver"], m.FieldInfo(*c["fi"]))
+    sim.set_option(m.OPT_NTFF_BLOCK, 7)
+    sim.set_option(m.OPT_TBLOCK, 4)
+    sim.set_eps(*_eps_for(name, c))
+    t = 0.0
+    for _ in range(3):
+        sim.update(t, 0.0)
+        t += 1.0
+    sim.time = t
+    rest = c["steps"] - 3
+    sim.run(rest // 2 + 1)
+    sim.run(rest - (rest // 2 + 1))
+    got = capture([sim.field(w) for w in range(3)], [sim.eps(w) for w in range(3)],
+                  [sim.ntff(w) for w in range(3)], sim.array_size, c["kind"], c.get("rows", "all"))
+    bad = compare(got, {key: v for key, v in ref.items() if key.startswith(("field", "ntff"))}, TOL)
+    assert not bad, bad
