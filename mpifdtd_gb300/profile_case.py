@@ -6,6 +6,7 @@
     python -m mpifdtd_gb300.profile_case onestep --solver MPI_TE_UPML --grid 4096 --precision f64 --steps 8
     python -m mpifdtd_gb300.profile_case farfield --grid 1024 [--solver MPI_TM_UPML]
     python -m mpifdtd_gb300.profile_case broadband --structures 64 --steps 2500
+    python -m mpifdtd_gb300.profile_case serial --solver TM_UPML --grid 16384 --precision f32 --k 4 [--cols 1] --steps 32
     python -m mpifdtd_gb300.profile_case all ...    (tblock and gemm, the blocked case first)
 
 tblock: the morpho ridge on a (grid + 32)^2 MPI_TM_UPML grid with temporal
@@ -14,7 +15,9 @@ events on the engine's stream.  onestep: the same ridge with the one-step
 kernels of any UPML solver (tm_e/tm_h, te_e/te_h).  farfield: a Mie cylinder
 run with the running DFT enabled, then the frequency-domain NTFF
 (frequency_kernel) and the DFT far field.  broadband: the surrogate's data
-generator, one batched pulse run over `structures` lamella maps.  gemm: C = A B^T in BF16 with FP32 output on
+generator, one batched pulse run over `structures` lamella maps.  serial: the
+ridge with a serial UPML solver (H half-step first, pulse source) blocked k
+steps per launch (0: one step), the whole step timed.  gemm: C = A B^T in BF16 with FP32 output on
 the surrogate's tcgen05 kernel, timed with CUDA events.  One JSON line each.
 """
 from __future__ import annotations
@@ -76,6 +79,32 @@ def onestep(a):
     print(json.dumps({"case": "onestep", "solver": a.solver, "grid": [sim.n_px, sim.n_py], "precision": a.precision,
                       "steps": a.steps, "ms_per_step": ms, "gcell_per_s": cells / ms / 1e6,
                       "ms_per_launch": {k: v / p["steps"] for k, v in p.items() if k != "steps"}}), flush=True)
+    sim.close()
+
+
+def serial(a):
+    import torch
+
+    import mpifdtd_gb300 as m
+    side = (a.grid + 32) * 2
+    sim = m.Simulation(a.solver, m.FieldInfo(side, side, 2, 16, 500, 0, 20000), a.precision)
+    sim.fill_model(m.MODEL_MORPHO, [600.0, 80.0, 90.0, 8.0, 50.0, 0.0, 2.43, 0.0])
+    sim.set_option(m.OPT_TBLOCK, a.k)
+    if a.cols != 1:
+        sim.set_option(m.OPT_TBLOCK_COLS, a.cols)
+    sim.run(8)
+    sim.synchronize()
+    st = torch.cuda.ExternalStream(sim.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    sim.run(a.steps)
+    sim.flush()
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / a.steps
+    print(json.dumps({"case": "serial", "solver": a.solver, "grid": [sim.n_px, sim.n_py], "precision": a.precision,
+                      "k": a.k, "cols": a.cols, "steps": a.steps, "ms_per_step": ms,
+                      "gcell_per_s": sim.n_px * sim.n_py / ms / 1e6, "status": sim.status}), flush=True)
     sim.close()
 
 
@@ -159,7 +188,7 @@ def sweep(a):
 
 def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m mpifdtd_gb300.profile_case")
-    ap.add_argument("case", choices=["tblock", "gemm", "sweep", "onestep", "farfield", "broadband", "all"])
+    ap.add_argument("case", choices=["tblock", "gemm", "sweep", "onestep", "farfield", "broadband", "serial", "all"])
     ap.add_argument("--solver", default="MPI_TM_UPML")
     ap.add_argument("--structures", type=int, default=64)
     ap.add_argument("--cols", type=int, default=1)
@@ -185,6 +214,8 @@ def main(argv=None):
         farfield(a)
     if a.case == "broadband":
         broadband(a)
+    if a.case == "serial":
+        serial(a)
 
 
 if __name__ == "__main__":
