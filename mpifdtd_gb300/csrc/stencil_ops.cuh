@@ -79,17 +79,6 @@ __device__ __forceinline__ void pulse_source(const SourceStep &s, int i, int j, 
   e.y = (R)((double)e.y + amp * sn);
 }
 
-// The same, called rather than inlined: the blocked tiles of the serial solvers
-// keep the double-precision exp / sincos out of their level loops' registers
-// (the pulse only touches cells with eps != 1).
-template <typename R>
-__device__ __noinline__ typename Cplx<R>::T pulse_source_call(SourceStep s, int i, int j, R ie,
-                                                               typename Cplx<R>::T e, double dt)
-{
-  pulse_source<R>(s, i, j, ie, e, dt);
-  return e;
-}
-
 template <typename R>
 __device__ __forceinline__ void apply_source(const StencilView<R> &v, const SourceStep &s, int i, int j, R ie,
                                              typename Cplx<R>::T &e)
