@@ -322,6 +322,7 @@ static void free_sim(fdtd_sim *s)
   }
   cudaFree(s->d_tbcol);
   cudaFree(s->d_tbrow);
+  cudaFree(s->d_ptab);
   cudaFree(s->d_tiles);
   for (int a = 0; a < 2; a++) { cudaFree(s->d_ieps64[a]); cudaFree(s->d_ieps32[a]); }
   for (int a = 0; a < 3; a++) cudaFree(s->d_eps[a]);
@@ -864,7 +865,11 @@ static int before_step(fdtd_sim *s, double time)
 static int tb_cols_for(const fdtd_sim *s, int K) { return s->tb_cols == 2 && s->f32 && (K == 2 || K == 4) ? 2 : 1; }
 
 // Tile rows when FDTD_OPT_TBLOCK_ROWS is 0: the tallest power of two in
-// [16, 512] that still gives 16 tiles (warps) per SM.
+// [16, 128] that gives at least four waves of tiles (16 resident warps per
+// SM), so that the last, partly filled wave is a small share of the launch.
+// On 16416² the autotuner's fastest is 128 rows (1.13 ms per FP32 TM step;
+// 256: 1.17, 512: 1.29); on 4128² taller tiles gave one or two waves and a
+// blocked step slower than the one-step kernels.
 static int tb_auto_rows(const fdtd_sim *s, int K, int cpl)
 {
   const int W = 32 * cpl - 2 * K;
@@ -872,8 +877,8 @@ static int tb_auto_rows(const fdtd_sim *s, int K, int cpl)
   int dev = 0, nsm = 152;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev))
     cudaGetLastError();
-  const long long want = 16LL * nsm;
-  int L = 512;
+  const long long want = 4 * 16LL * nsm;
+  int L = 128;
   while (L > 16 && nstrip * ((s->ni + L - 1) / L) < want) L >>= 1;
   return L;
 }
@@ -942,6 +947,7 @@ static int tb_prepare(fdtd_sim *s, int K, int L, int cpl)
     CK(cudaMalloc(&s->d_tbcol, (size_t)kMaxTBlock * 12 * s->nxa * s->esize));
     CK(cudaMalloc(&s->d_tbrow, (size_t)kMaxTBlock * 12 * s->pitch * s->esize));
   }
+  if (!s->mpi && !s->d_ptab) CK(cudaMalloc(&s->d_ptab, sizeof(PulseRow) * 2 * kMaxTBlock * (size_t)s->nxa));
   if (s->tb_built_k == K && s->tb_built_l == L && s->tb_built_c == cpl) return FDTD_OK;
   TilePlan plan;
   if (int rc = fdtd_plan_tiles(s, K, L, cpl, &plan)) return rc;
@@ -1027,6 +1033,16 @@ static void enqueue_block(fdtd_sim *s, int K)
       if (co != 0.0) tb.pulse[0] = pulse_step(s, t_first, 0.5, 0.0, co);
       if (si != 0.0) tb.pulse[1] = pulse_step(s, t_first, 0.0, 0.5, si);
     }
+    // at 0 degrees the pulse depends on the row only: one table per pulse and
+    // block instead of a double-precision exp and sincos per cell and level
+    if (s->cfg.angle_deg == 0 && s->d_ptab)
+      for (int p = 0; p < 2; p++)
+        if (tb.pulse[p].kind) {
+          PulseRow *tab = (PulseRow *)s->d_ptab + (size_t)p * kMaxTBlock * s->nxa;
+          launch_pulse_rows(tb.pulse[p], K, s->nxa, tab, st);
+          s->launches += 1;
+          tb.ptab[p] = tab;
+        }
   }
   const double coef = s->mpi ? 1.0 / (4 * M_PI * s->c0 * 1.0e6) : 1.0;  // mpiTM_UPML.c:852-854; serial: 1
   mark(s);

@@ -62,6 +62,13 @@ struct StencilView {
 };
 
 // Per-step source description.
+// Gaussian pulse of one row at one step, for 0 degrees (the pulse then depends
+// on the row only): a = dot g, (c, s) = (cos, sin) of its phase (stencil_ops.cuh
+// pulse_source computes the same values per cell)
+struct PulseRow {
+  double a, c, s, pad;
+};
+
 struct SourceStep {
   int kind;          // 0 none, 1 CW scattered wave (MPI solvers), 2 Gaussian pulse (serial)
   double s_re, s_im; // CW: ray_coef * e^{-i w t}
@@ -148,6 +155,7 @@ struct TBlockView {
   int cpl;             // columns per lane: 1, or 2 (FP32, K = 2 or 4)
   double2 sc[kMaxTBlock];  // CW source per level: ray_coef e^{-i w t}
   SourceStep pulse[2];     // serial solvers: the pulse of the block's first step (TM [0] on Ez; TE [0] Ex, [1] Ey)
+  const PulseRow *ptab[2]; // 0 degrees: pulse[p] per level and row, [K][nxa] (null: per cell)
 };
 
 // Runs the interior and the general kernel of depth K (1, 2, 4 or 8).
@@ -157,6 +165,8 @@ void launch_tblock(const StencilView<R> &v, const TBlockView<R> &tb, int K, bool
 // fdtd_tblock_serial.cu.
 template <typename R>
 void launch_tblock_serial(const StencilView<R> &v, const TBlockView<R> &tb, int K, bool tm, cudaStream_t st);
+// tab[l][i] = the pulse s at step s.time + l of array row i (l < K, i < nrow), 0 degrees only
+void launch_pulse_rows(const SourceStep &s, int K, int nrow, PulseRow *tab, cudaStream_t st);
 // vals slots slot0 .. slot0+K-1 from the NTFF line samples of a blocked launch
 // (the samples ntff_gather_kernel takes from the fields after each step).
 template <typename R>

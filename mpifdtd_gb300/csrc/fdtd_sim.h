@@ -45,6 +45,7 @@ struct fdtd_sim {
   int tb_rows = 0;              // rows per tile segment (FDTD_OPT_TBLOCK_ROWS), 0 = automatic
   void *d_f2[fdtd::kMaxSlots] = {};  // the other field set
   void *d_tbcol = nullptr, *d_tbrow = nullptr;  // NTFF line samples of kMaxTBlock levels
+  void *d_ptab = nullptr;       // serial solvers at 0 degrees: pulse row tables [2][kMaxTBlock][nxa] (PulseRow)
   void *d_tiles = nullptr;      // int4 (strip, r0, r1, -) work-list of the general kernel
   int ntiles = 0, tiles_cap = 0;
   int tb_s0 = 0, tb_s1 = 0, tb_ra = 1, tb_rb = 1, tb_nseg = 0, tb_L = 0;

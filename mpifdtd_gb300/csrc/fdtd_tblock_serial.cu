@@ -65,7 +65,33 @@ void launch_depth_hf(const StencilView<R> &v, const TBlockView<R> &tb, bool tm, 
   }
 }
 
+// tab[l][i]: pulse_source's values for row i at step s.time + l, its
+// operations in its order (the column term is 0 x (j + gap) = +0 at 0 degrees)
+__global__ void pulse_row_kernel(SourceStep s, int K, int nrow, PulseRow *tab)
+{
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= K * nrow) return;
+  const int l = q / nrow, i = q - l * nrow;
+  const double pos = __dadd_rn(__dmul_rn((double)i + s.gap_x, s.cos_per_c), 0.0);
+  const double r = __dsub_rn(pos, (s.time + (double)l) - s.t0);
+  const double qq = __ddiv_rn(r, 50.0);
+  const double g = exp(-(qq * qq));
+  double sn, cs;
+  sincos(r * s.w, &sn, &cs);
+  PulseRow p;
+  p.a = s.dot * g;
+  p.c = cs;
+  p.s = sn;
+  p.pad = 0.0;
+  tab[q] = p;
+}
+
 }  // namespace
+
+void launch_pulse_rows(const SourceStep &s, int K, int nrow, PulseRow *tab, cudaStream_t st)
+{
+  pulse_row_kernel<<<(K * nrow + 255) / 256, 256, 0, st>>>(s, K, nrow, tab);
+}
 
 template <typename R>
 void launch_tblock_serial(const StencilView<R> &v, const TBlockView<R> &tb, int K, bool tm, cudaStream_t st)

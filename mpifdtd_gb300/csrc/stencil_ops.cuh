@@ -79,6 +79,16 @@ __device__ __forceinline__ void pulse_source(const SourceStep &s, int i, int j, 
   e.y = (R)((double)e.y + amp * sn);
 }
 
+// The same from a row table entry (pulse at 0 degrees): the operations after
+// the pulse's own value are pulse_source's, in its order.
+template <typename R>
+__device__ __forceinline__ void pulse_row(const PulseRow &p, R ie, typename Cplx<R>::T &e)
+{
+  const double amp = p.a * ((double)ie - 1.0);
+  e.x = (R)((double)e.x + amp * p.c);
+  e.y = (R)((double)e.y + amp * p.s);
+}
+
 template <typename R>
 __device__ __forceinline__ void apply_source(const StencilView<R> &v, const SourceStep &s, int i, int j, R ie,
                                              typename Cplx<R>::T &e)

@@ -759,7 +759,10 @@ __device__ __forceinline__ void tm_tile_hf(const StencilView<R> &v, const TBlock
           T ez = dz;
           if (!is_one(en[q].ie)) {
             ez = cscale(dz, en[q].ie);
-            if (tb.pulse[0].kind) pulse_source<R>(tb.pulse[0], h, j + q, en[q].ie, ez, (double)(l - 1));
+            if (tb.pulse[0].kind) {
+              if (tb.ptab[0]) pulse_row<R>(tb.ptab[0][(size_t)(l - 1) * v.nxa + h], en[q].ie, ez);
+              else pulse_source<R>(tb.pulse[0], h, j + q, en[q].ie, ez, (double)(l - 1));
+            }
           }
           en[q].e = ez;
         }
@@ -959,11 +962,17 @@ __device__ __forceinline__ void te_tile_hf(const StencilView<R> &v, const TBlock
           T ex = dx, ey = dy;
           if (!is_one(en[q].iex)) {
             ex = cscale(dx, en[q].iex);
-            if (tb.pulse[0].kind) pulse_source<R>(tb.pulse[0], h, j + q, en[q].iex, ex, (double)(l - 1));
+            if (tb.pulse[0].kind) {
+              if (tb.ptab[0]) pulse_row<R>(tb.ptab[0][(size_t)(l - 1) * v.nxa + h], en[q].iex, ex);
+              else pulse_source<R>(tb.pulse[0], h, j + q, en[q].iex, ex, (double)(l - 1));
+            }
           }
           if (!is_one(en[q].iey)) {
             ey = cscale(dy, en[q].iey);
-            if (tb.pulse[1].kind) pulse_source<R>(tb.pulse[1], h, j + q, en[q].iey, ey, (double)(l - 1));
+            if (tb.pulse[1].kind) {
+              if (tb.ptab[1]) pulse_row<R>(tb.ptab[1][(size_t)(l - 1) * v.nxa + h], en[q].iey, ey);
+              else pulse_source<R>(tb.pulse[1], h, j + q, en[q].iey, ey, (double)(l - 1));
+            }
           }
           en[q].ex = ex;
           en[q].ey = ey;
