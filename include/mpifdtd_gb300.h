@@ -281,7 +281,7 @@ int fdtd_checkpoint_read(fdtd_sim *sim, const char *path);
 int fdtd_set_option(fdtd_sim *sim, int key, int value);
 int fdtd_get_option(fdtd_sim *sim, int key, int *value);
 
-/* Autotuner of the temporal blocking (MPI solvers): times the one-step kernels and the
+/* Autotuner of the temporal blocking (UPML solvers): times the one-step kernels and the
  * blocked kernel at each depth K and tile height on this simulation's own
  * grid and fields (into the spare field set: the state does not change),
  * sets FDTD_OPT_TBLOCK / _ROWS / _COLS to the fastest, returns K and rows

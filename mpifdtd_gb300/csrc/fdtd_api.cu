@@ -1101,20 +1101,38 @@ static int autotune_impl(fdtd_sim *s, int *k_out, int *rows_out, double *ms_out)
   SourceStep cw{};
   cw.kind = 1;
   cw.s_re = s->ray_coef;
-  double best = timed([&] {
+  // the serial solvers' sources: the pulse at the current step (enqueue_step's)
+  SourceStep pz{}, px{}, py{};
+  if (!s->mpi) {
     if (s->tm) {
+      pz = pulse_step(s, s->time, 0, 0, 1.0);
+    } else {
+      const double co = cos((s->cfg.angle_deg + 90) * M_PI / 180.0);
+      const double si = sin((s->cfg.angle_deg + 90) * M_PI / 180.0);
+      if (co != 0.0) px = pulse_step(s, s->time, 0.5, 0.0, co);
+      if (si != 0.0) py = pulse_step(s, s->time, 0.0, 0.5, si);
+    }
+  }
+  double best = timed([&] {
+    if (s->mpi && s->tm) {
       launch_tm_e<R>(vs, cw, st);
       launch_tm_h<R>(vs, st);
-    } else {
+    } else if (s->mpi) {
       launch_te_e<R>(vs, SourceStep{}, cw, st);
       launch_te_h<R>(vs, st);
+    } else if (s->tm) {  // fdtdTM_upml.c:54-66
+      launch_tm_h<R>(vs, st);
+      launch_tm_e<R>(vs, pz, st);
+    } else {             // fdtdTE_upml.c:168-192
+      launch_te_h<R>(vs, st);
+      launch_te_e<R>(vs, px, py, st);
     }
   });
   int best_k = 0, best_l = 0, best_c = 1;
   s->tune_table.assign({0.0, 0.0, 1.0, best});
   const int depths[4] = {1, 2, 4, 8};
   for (int K : depths) {
-    if (K == 8 && !s->f32) continue;
+    if (K == 8 && (!s->f32 || !s->mpi)) continue;
     for (int cpl = 1; cpl <= 2; cpl++) {
     if (cpl == 2 && !(s->f32 && (K == 2 || K == 4))) continue;
     for (int L = 16; L <= 512; L *= 2) {
@@ -1128,7 +1146,22 @@ static int autotune_impl(fdtd_sim *s, int *k_out, int *rows_out, double *ms_out)
       TBlockView<R> tb = tblock_view<R>(s, false);
       tb.sc[0] = make_double2(s->ray_coef, 0.0);
       for (int l = 1; l < K; l++) tb.sc[l] = tb.sc[0];
-      const double ms = timed([&] { launch_tblock<R>(v, tb, K, s->tm, st); }) / K;
+      tb.pulse[0] = s->tm ? pz : px;
+      tb.pulse[1] = s->tm ? SourceStep{} : py;
+      const bool tables = !s->mpi && s->cfg.angle_deg == 0 && s->d_ptab;
+      const double ms = timed([&] {
+        if (s->mpi) {
+          launch_tblock<R>(v, tb, K, s->tm, st);
+          return;
+        }
+        for (int p = 0; p < 2 && tables; p++)  // enqueue_block's per-launch pulse tables
+          if (tb.pulse[p].kind) {
+            PulseRow *tab = (PulseRow *)s->d_ptab + (size_t)p * kMaxTBlock * s->nxa;
+            launch_pulse_rows(tb.pulse[p], K, s->nxa, tab, st);
+            tb.ptab[p] = tab;
+          }
+        launch_tblock_serial<R>(v, tb, K, s->tm, st);
+      }) / K;
       s->tune_table.insert(s->tune_table.end(), {(double)K, (double)L, (double)cpl, ms});
       if (ms < best) {
         best = ms;
@@ -1154,7 +1187,7 @@ static int autotune_impl(fdtd_sim *s, int *k_out, int *rows_out, double *ms_out)
 extern "C" int fdtd_autotune(fdtd_sim *s, int *k_out, int *rows_out, double *ms_per_step_out)
 {
   if (!s) return fail(FDTD_E_ARG, "null simulation");
-  if (!s->mpi) return fail(FDTD_E_UNSUPPORTED, "temporal blocking needs an MPI solver (E then H half-step)");
+  if (s->family != 0) return fail(FDTD_E_UNSUPPORTED, "temporal blocking needs a UPML solver");
   if (int rc = flush_ntff(s)) return rc;
   return s->f32 ? autotune_impl<float>(s, k_out, rows_out, ms_per_step_out)
                 : autotune_impl<double>(s, k_out, rows_out, ms_per_step_out);

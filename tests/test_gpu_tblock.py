@@ -242,3 +242,26 @@ def test_tblock_serial_runs_split_across_calls_and_updates():
                   [sim.ntff(w) for w in range(3)], sim.array_size, c["kind"], c.get("rows", "all"))
     bad = compare(got, {key: v for key, v in ref.items() if key.startswith(("field", "ntff"))}, TOL)
     assert not bad, bad
+
+
+def test_autotune_serial_solver_keeps_state_and_picks_a_valid_setting():
+    """The autotuner times the serial solvers' own order (H half-step first,
+    pulse) and leaves the fields as they were; the run it tunes still meets
+    the golden vectors."""
+    m = _engine()
+    name = "ser_te_circle"
+    c = CASES[name]
+    ref = _golden(name)
+    sim = m.Simulation(c["solver"], m.FieldInfo(*c["fi"]))
+    sim.set_eps(*_eps_for(name, c))
+    half = c["steps"] // 2
+    sim.run(half)
+    before = [sim.field(w) for w in range(3)]
+    res = sim.autotune()
+    assert res["tblock"] in (0, 1, 2, 4) and res["stencil_ms_per_step"] > 0
+    assert all(k != 8 for k, _, _, _ in res["candidates"])
+    for w in range(3):
+        np.testing.assert_array_equal(sim.field(w), before[w])
+    sim.run(c["steps"] - half)
+    for w in range(3):
+        assert rel(sim.field(w), ref[f"field{w}"]) <= TOL
