@@ -196,20 +196,24 @@ template <typename R, int K, bool TM, int CPL> constexpr int batch_min_blocks()
                   : sizeof(R) == 8 ? (K > 2 ? 3 : 4) : (K >= 8 ? 3 : K == 4 ? (TM ? 4 : 5) : 6);
 }
 
-// resident blocks per SM of the PML / edge work-list kernel: 4 (128 registers)
-// where the tile fits them with at most a few bytes of spill (TM, FP32, one
-// column per lane, K <= 4: 287 structures/s on the 256-cylinder sweep against
-// 272 at 3 blocks and 241 at 5), else 3
-template <typename R, int K, bool TM, int CPL> constexpr int batch_aux_blocks()
+// The PML / edge work-list kernel runs 3 resident blocks per SM (162
+// registers for FP32 TM at K = 4), or 4 (WIDE: 128 registers, a few bytes of
+// spill) where the tile fits them (TM, FP32, one column per lane, K <= 4) and
+// the list has at least one tile per warp of 4 blocks per SM: each tile then
+// runs slower, but more run at once.  Sweeps of 256 / 64 / 32 cylinders: 287 /
+// 208 / 102 structures/s at 4 blocks, 272 / 196 / 128 at 3 (32 cylinders:
+// 1576 tiles for 2432 warps); 256 at 5 blocks (96 registers, 344 bytes of
+// spill): 241.
+template <typename R, int K, bool TM, int CPL> constexpr bool batch_aux_wide_ok()
 {
-  return (TM && sizeof(R) == 4 && CPL == 1 && K <= 4) ? 4 : 3;
+  return TM && sizeof(R) == 4 && CPL == 1 && K <= 4;
 }
 
 // Persistent: each warp claims the next tile of the list (sorted by cost,
 // largest first) until the list is exhausted, so the tail is one tile long
 // whatever the mix of tile heights and finished instances.
-template <typename R, int K, bool AUX, bool TM, int CPL>
-__global__ void __launch_bounds__(32 * kBWarps, (AUX ? batch_aux_blocks<R, K, TM, CPL>() : batch_min_blocks<R, K, TM, CPL>()))
+template <typename R, int K, bool AUX, bool TM, int CPL, bool WIDE = false>
+__global__ void __launch_bounds__(32 * kBWarps, (AUX ? (WIDE ? 4 : 3) : batch_min_blocks<R, K, TM, CPL>()))
     batch_tile_kernel(const BatchInst<R> *__restrict__ inst, const int4 *__restrict__ tiles, int ntiles,
                       BatchClock *clk)
 {
@@ -231,13 +235,13 @@ __global__ void __launch_bounds__(32 * kBWarps, (AUX ? batch_aux_blocks<R, K, TM
   }
 }
 
-template <typename R, int K, bool AUX, bool TM, int CPL>
+template <typename R, int K, bool AUX, bool TM, int CPL, bool WIDE = false>
 int persistent_grid(int ntiles)
 {
   int dev = 0, nsm = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_tile_kernel<R, K, AUX, TM, CPL>, 32 * kBWarps, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_tile_kernel<R, K, AUX, TM, CPL, WIDE>, 32 * kBWarps, 0);
   cudaGetLastError();
   const int want = (ntiles + kBWarps - 1) / kBWarps;
   return std::max(1, std::min(want, std::max(1, nsm) * std::max(1, per)));
@@ -258,6 +262,7 @@ struct fdtd_batch {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   void *d_inst = nullptr, *d_tint = nullptr, *d_tgen = nullptr, *d_clock = nullptr, *d_omega = nullptr;
   int n_int = 0, n_gen = 0, grid_int = 0, grid_gen = 0;
+  bool aux_wide = false;        // the work-list kernel at 4 blocks per SM (batch_aux_wide_ok, long list)
   int dft_stride = 16, dft_every = 4;  // FDTD_OPT_DFT_STRIDE; blocks between DFT samples (stride / K)
   int planned_k = 0, planned_l = -1, planned_c = 0;
   std::vector<int> rows;  // tile rows of each instance
@@ -541,7 +546,11 @@ static void batch_block(fdtd_batch *b)
   // the two tile kernels run side by side (fork onto the second stream, join)
   cudaEventRecord(b->ev_fork, st);
   cudaStreamWaitEvent(b->stream2, b->ev_fork, 0);
-  if (b->n_gen > 0)
+  constexpr bool wide_ok = batch_aux_wide_ok<R, K, TM, CPL>();
+  if (b->n_gen > 0 && wide_ok && b->aux_wide)
+    batch_tile_kernel<R, K, true, TM, CPL, wide_ok><<<b->grid_gen, 32 * kBWarps, 0, b->stream2>>>(
+        inst, (const int4 *)b->d_tgen, b->n_gen, clk);
+  else if (b->n_gen > 0)
     batch_tile_kernel<R, K, true, TM, CPL><<<b->grid_gen, 32 * kBWarps, 0, b->stream2>>>(
         inst, (const int4 *)b->d_tgen, b->n_gen, clk);
   cudaEventRecord(b->ev_join, b->stream2);
@@ -560,7 +569,14 @@ template <typename R, int K, bool TM, int CPL>
 static void batch_grids(fdtd_batch *b)
 {
   b->grid_int = persistent_grid<R, K, false, TM, CPL>(b->n_int);
-  b->grid_gen = persistent_grid<R, K, true, TM, CPL>(b->n_gen);
+  // the wide work-list kernel once the list gives every warp of 4 blocks per SM a tile
+  constexpr bool wide_ok = batch_aux_wide_ok<R, K, TM, CPL>();
+  int dev = 0, nsm = 152;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev))
+    cudaGetLastError();
+  b->aux_wide = wide_ok && b->n_gen >= 4 * kBWarps * nsm;
+  b->grid_gen = b->aux_wide ? persistent_grid<R, K, true, TM, CPL, wide_ok>(b->n_gen)
+                            : persistent_grid<R, K, true, TM, CPL>(b->n_gen);
 }
 
 // dispatch on (K, columns per lane, TM) of the batch
